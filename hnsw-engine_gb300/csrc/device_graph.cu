@@ -1,0 +1,523 @@
+// device_graph.cu -- the hgd_* C ABI: graph mirror in HBM and batch launches.
+//
+// HBM layout of a graph (all arrays resident for the index's lifetime):
+//   vecs    n x pd float32, 64-byte rows (pd = dim rounded up to 16)
+//   l0      n x l0s uint32 ids, l0s = 2M rounded up to 16 (M = 16: 128 B, one
+//           aligned line per list); unused slots hold 0xFFFFFFFF, so the
+//           count word of the file layout is not needed
+//   up      per node with level L >= 1, L blocks of ups = M rounded up to 16
+//           ids (M = 16: 64 B), padded the same way; up_blk[id] = first block
+//   labels  n x uint64 (read only when writing results)
+//   alive   n bits, 1 = not deleted (soft deletes flip one bit)
+// Per call: queries, per-query ef / k, filter bitsets translated to internal
+// ids, the work-queue counter and per-warp scratch (spill pool, visited bitmap).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "hnswgpu_device.h"
+#include "search_common.cuh"
+
+namespace hg {
+int slots_for(uint32_t pd);
+cudaError_t launch_inv_norm(const float* qs, uint32_t nq, uint32_t dim, float* out, cudaStream_t st);
+cudaError_t launch_search(const SearchParams& P, const float* inv, int blocks, int warps_per_block, cudaStream_t st);
+int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, uint32_t R, uint32_t C);
+cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bits, const uint64_t* labels, uint32_t n,
+                                    uint32_t* out, cudaStream_t st);
+}  // namespace hg
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define HG_CUDA(call)                                                                              \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) {                                                                       \
+      return fail(e_ == cudaErrorMemoryAllocation ? HGD_ENOMEM : HGD_ECUDA,                        \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                             \
+    }                                                                                              \
+  } while (0)
+
+// A grow-only device buffer.
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t n = std::max<size_t>(need, 256);
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    size_t n = std::max<size_t>(need, 256);
+    cudaError_t e = cudaMallocHost(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+uint32_t round_up(uint32_t v, uint32_t m) { return (v + m - 1) / m * m; }
+uint32_t next_pow2(uint32_t v) {
+  uint32_t p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+}  // namespace
+
+namespace hg {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace hg
+
+struct hgd_graph {
+  int device = 0;
+  int order = HGD_ORDER_AVX512;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;  // one batch at a time per graph (its scratch is shared)
+  // graph
+  uint64_t n = 0, dim = 0, pd = 0, M = 0;
+  int metric = 0, max_level = -1;
+  uint32_t entry = hg::kNoId;
+  uint32_t l0s = 0, ups = 0;
+  bool identity_labels = true, dedup = false;
+  uint64_t num_deleted = 0;
+  DBuf vecs, l0, up, up_blk, labels, alive;
+  std::vector<uint32_t> alive_host;
+  // per call
+  DBuf q, efq, kq, fsel, fptrs, fbits, inv, out, nres, counters;
+  DBuf work;  // [0] work counter, [1] overflow count, [2] rerun work counter
+  DBuf ovf_list, pool, bitmaps, pool_big, bitmaps_big;
+  PinnedBuf pin_in, pin_out;
+  uint64_t pool_slots = 0, pool_cap = 0, big_slots = 0;
+};
+
+extern "C" {
+
+const char* hgd_last_error(void) { return g_err.c_str(); }
+
+int hgd_graph_upload(const hgd_graph_view* v, int device, int order, hgd_graph** out) {
+  if (!v || !out) return fail(HGD_EINVAL, "hgd_graph_upload: null argument");
+  if (order != HGD_ORDER_AVX512)
+    return fail(HGD_EINVAL, "hgd_graph_upload: only the AVX-512 summation order is implemented on the GPU");
+  if (v->count >= 0xFFFFFFFFull) return fail(HGD_EINVAL, "hgd_graph_upload: count exceeds 32-bit ids");
+  if (v->padded_dim % 16 != 0 || v->padded_dim < v->dim || v->dim == 0)
+    return fail(HGD_EINVAL, "hgd_graph_upload: padded_dim must be dim rounded up to 16");
+  if (hg::slots_for(static_cast<uint32_t>(v->padded_dim)) > 33)
+    return fail(HGD_EINVAL, "hgd_graph_upload: padded dimension above 1024 is not supported on the GPU");
+  if (v->M < 2 || v->M > 2048) return fail(HGD_EINVAL, "hgd_graph_upload: invalid M");
+  auto* g = new hgd_graph();
+  g->device = device;
+  g->order = order;
+  auto cleanup = [&](int code) {
+    hgd_graph_free(g);
+    return code;
+  };
+  {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cleanup(fail(HGD_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
+    e = cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return cleanup(fail(HGD_ECUDA, cudaGetErrorString(e)));
+    e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cleanup(fail(HGD_ECUDA, cudaGetErrorString(e)));
+  }
+  const uint64_t n = v->count;
+  g->n = n;
+  g->dim = v->dim;
+  g->pd = v->padded_dim;
+  g->M = v->M;
+  g->metric = v->metric;
+  g->max_level = v->max_level;
+  g->entry = v->entry_point;
+  const uint32_t M0 = static_cast<uint32_t>(2 * v->M);
+  g->l0s = round_up(M0, 16);
+  g->ups = round_up(static_cast<uint32_t>(v->M), 16);
+
+  // host re-layout
+  std::vector<uint32_t> l0(static_cast<size_t>(n) * g->l0s, hg::kNoId);
+  std::vector<uint32_t> mark(n, hg::kNoId);
+  uint64_t list_no = 0;
+  auto dup_check = [&](const uint32_t* ids, uint32_t cnt) {
+    for (uint32_t j = 0; j < cnt; ++j) {
+      if (mark[ids[j]] == static_cast<uint32_t>(list_no)) g->dedup = true;
+      mark[ids[j]] = static_cast<uint32_t>(list_no);
+    }
+    ++list_no;
+  };
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint32_t* src = v->level0 + i * (1 + M0);
+    const uint32_t cnt = std::min(src[0], M0);
+    std::memcpy(&l0[i * g->l0s], src + 1, cnt * 4);
+    dup_check(src + 1, cnt);
+  }
+  std::vector<uint32_t> up_blk(n, hg::kNoId);
+  uint64_t blocks = 0;
+  for (uint64_t i = 0; i < n; ++i) blocks += v->levels[i];
+  std::vector<uint32_t> up(std::max<uint64_t>(blocks, 1) * g->ups, hg::kNoId);
+  uint64_t b = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const int L = v->levels[i];
+    if (L == 0) continue;
+    up_blk[i] = static_cast<uint32_t>(b);
+    for (int lc = 1; lc <= L; ++lc, ++b) {
+      const uint32_t* src = v->upper + v->upper_offset[i] + static_cast<uint64_t>(lc - 1) * (1 + v->M);
+      const uint32_t cnt = std::min<uint32_t>(src[0], static_cast<uint32_t>(v->M));
+      std::memcpy(&up[b * g->ups], src + 1, cnt * 4);
+      dup_check(src + 1, cnt);
+    }
+  }
+  for (uint64_t i = 0; i < n && g->identity_labels; ++i) g->identity_labels = v->labels[i] == i;
+  g->alive_host.assign((n + 31) / 32 + 1, 0u);
+  for (uint64_t i = 0; i < n; ++i) {
+    if (v->deleted[i] == 0) g->alive_host[i >> 5] |= 1u << (i & 31);
+    else ++g->num_deleted;
+  }
+
+  auto up_copy = [&](DBuf& d, const void* src, size_t bytes) -> int {
+    cudaError_t e = d.ensure(std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return fail(HGD_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (bytes) {
+      e = cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    }
+    return HGD_OK;
+  };
+  int rc;
+  if ((rc = up_copy(g->vecs, v->vectors, n * g->pd * 4)) != HGD_OK) return cleanup(rc);
+  if ((rc = up_copy(g->l0, l0.data(), l0.size() * 4)) != HGD_OK) return cleanup(rc);
+  if ((rc = up_copy(g->up, up.data(), up.size() * 4)) != HGD_OK) return cleanup(rc);
+  if ((rc = up_copy(g->up_blk, up_blk.data(), up_blk.size() * 4)) != HGD_OK) return cleanup(rc);
+  if ((rc = up_copy(g->labels, v->labels, n * 8)) != HGD_OK) return cleanup(rc);
+  if ((rc = up_copy(g->alive, g->alive_host.data(), g->alive_host.size() * 4)) != HGD_OK) return cleanup(rc);
+  *out = g;
+  return HGD_OK;
+}
+
+int hgd_graph_set_order(hgd_graph* g, int order) {
+  if (!g) return fail(HGD_EINVAL, "hgd_graph_set_order: null graph");
+  if (order != HGD_ORDER_AVX512)
+    return fail(HGD_EINVAL, "hgd_graph_set_order: only the AVX-512 summation order is implemented on the GPU");
+  g->order = order;
+  return HGD_OK;
+}
+
+int hgd_graph_set_deleted(hgd_graph* g, uint32_t id, int deleted) {
+  if (!g) return fail(HGD_EINVAL, "hgd_graph_set_deleted: null graph");
+  if (id >= g->n) return fail(HGD_EINVAL, "hgd_graph_set_deleted: id out of range");
+  std::lock_guard<std::mutex> lock(g->mu);
+  uint32_t& word = g->alive_host[id >> 5];
+  const uint32_t bit = 1u << (id & 31);
+  const bool was_alive = (word & bit) != 0;
+  if (deleted && was_alive) {
+    word &= ~bit;
+    ++g->num_deleted;
+  } else if (!deleted && !was_alive) {
+    word |= bit;
+    --g->num_deleted;
+  } else {
+    return HGD_OK;
+  }
+  HG_CUDA(cudaSetDevice(g->device));
+  HG_CUDA(cudaMemcpyAsync(g->alive.as<uint32_t>() + (id >> 5), &word, 4, cudaMemcpyHostToDevice, g->stream));
+  HG_CUDA(cudaStreamSynchronize(g->stream));
+  return HGD_OK;
+}
+
+void hgd_graph_free(hgd_graph* g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  for (DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->q, &g->efq, &g->kq, &g->fsel,
+                  &g->fptrs, &g->fbits, &g->inv, &g->out, &g->nres, &g->counters, &g->work, &g->ovf_list, &g->pool,
+                  &g->bitmaps, &g->pool_big, &g->bitmaps_big})
+    d->release();
+  g->pin_in.release();
+  g->pin_out.release();
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+}
+
+uint64_t hgd_graph_device_bytes(const hgd_graph* g) {
+  if (!g) return 0;
+  uint64_t t = 0;
+  for (const DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->q, &g->efq, &g->kq,
+                        &g->fsel, &g->fptrs, &g->fbits, &g->inv, &g->out, &g->nres, &g->counters, &g->work,
+                        &g->ovf_list, &g->pool, &g->bitmaps, &g->pool_big, &g->bitmaps_big})
+    t += d->bytes;
+  return t;
+}
+
+int hgd_search(hgd_graph* g, const hgd_search_args* a) {
+  if (!g || !a) return fail(HGD_EINVAL, "hgd_search: null argument");
+  if (a->k == 0) return fail(HGD_EINVAL, "search_batch: k must be > 0");
+  if (a->nq == 0) return HGD_OK;
+  if (!a->queries || !a->out) return fail(HGD_EINVAL, "search_batch: null pointer");
+  if (a->nq >= 0xFFFFFFFFull) return fail(HGD_EINVAL, "hgd_search: too many queries in one batch");
+  if (a->precision != HGD_PREC_FP32) return fail(HGD_EINVAL, "hgd_search: precision not available in this build");
+  if (a->num_filters && !a->filters) return fail(HGD_EINVAL, "hgd_search: null filter table");
+  std::lock_guard<std::mutex> lock(g->mu);
+  HG_CUDA(cudaSetDevice(g->device));
+  cudaStream_t st = a->stream ? static_cast<cudaStream_t>(a->stream) : g->stream;
+  const uint64_t nq = a->nq;
+  const uint32_t dim = static_cast<uint32_t>(g->dim);
+
+  // ---- effective ef bound ----
+  uint32_t ef_max = a->ef ? a->ef : a->ef_default;
+  if (a->ef_per_query && !a->queries_on_device) {
+    ef_max = 0;
+    for (uint64_t i = 0; i < nq; ++i) {
+      const uint32_t e = a->ef_per_query[i] ? a->ef_per_query[i] : a->ef_default;
+      ef_max = std::max(ef_max, e);
+    }
+  }
+  ef_max = std::max(ef_max, a->k);
+  if (ef_max == 0) return fail(HGD_EINVAL, "hgd_search: ef is 0");
+  if (a->k_per_query && !a->queries_on_device)
+    for (uint64_t i = 0; i < nq; ++i)
+      if (a->k_per_query[i] == 0 || a->k_per_query[i] > a->k)
+        return fail(HGD_EINVAL, "hgd_search: per-query k must be in 1..k");
+
+  // ---- inputs to the device ----
+  const float* d_q = a->queries;
+  const uint32_t* d_ef = a->ef_per_query;
+  const uint32_t* d_k = a->k_per_query;
+  if (!a->queries_on_device) {
+    HG_CUDA(g->q.ensure(nq * dim * 4));
+    HG_CUDA(cudaMemcpyAsync(g->q.p, a->queries, nq * dim * 4, cudaMemcpyHostToDevice, st));
+    d_q = g->q.as<float>();
+    if (a->ef_per_query) {
+      HG_CUDA(g->efq.ensure(nq * 4));
+      HG_CUDA(cudaMemcpyAsync(g->efq.p, a->ef_per_query, nq * 4, cudaMemcpyHostToDevice, st));
+      d_ef = g->efq.as<uint32_t>();
+    }
+    if (a->k_per_query) {
+      HG_CUDA(g->kq.ensure(nq * 4));
+      HG_CUDA(cudaMemcpyAsync(g->kq.p, a->k_per_query, nq * 4, cudaMemcpyHostToDevice, st));
+      d_k = g->kq.as<uint32_t>();
+    }
+  }
+  // ---- filters -> id-space bitsets ----
+  const uint32_t nw = static_cast<uint32_t>((g->n + 31) / 32) + 1;
+  const int32_t* d_fsel = nullptr;
+  const uint32_t* const* d_fptrs = nullptr;
+  if (a->num_filters > 0) {
+    uint64_t label_words = 0;
+    for (uint32_t f = 0; f < a->num_filters; ++f)
+      if (a->filters[f].label_space) label_words += (a->filters[f].num_bits + 63) / 64;
+    HG_CUDA(g->fbits.ensure(static_cast<uint64_t>(a->num_filters) * nw * 4 + label_words * 8 + 64));
+    uint32_t* idbits = g->fbits.as<uint32_t>();
+    uint64_t* lw = reinterpret_cast<uint64_t*>(idbits + static_cast<uint64_t>(a->num_filters) * nw + 1);
+    lw = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(lw) + 7) & ~uintptr_t(7));
+    std::vector<const uint32_t*> ptrs(a->num_filters);
+    for (uint32_t f = 0; f < a->num_filters; ++f) {
+      const hgd_bitset& bs = a->filters[f];
+      uint32_t* dst = idbits + static_cast<uint64_t>(f) * nw;
+      ptrs[f] = dst;
+      const uint64_t words64 = (bs.num_bits + 63) / 64;
+      if (words64 && !bs.words) return fail(HGD_EINVAL, "hgd_search: null filter words");
+      if (bs.label_space) {
+        if (words64) HG_CUDA(cudaMemcpyAsync(lw, bs.words, words64 * 8, cudaMemcpyHostToDevice, st));
+        HG_CUDA(hg::launch_translate_filter(lw, bs.num_bits, g->labels.as<uint64_t>(),
+                                            static_cast<uint32_t>(g->n), dst, st));
+        lw += words64;
+      } else {
+        // id space: copy min(num_bits, n) bits, the rest not allowed
+        HG_CUDA(cudaMemsetAsync(dst, 0, nw * 4, st));
+        const uint64_t bits = std::min<uint64_t>(bs.num_bits, g->n);
+        const uint64_t full = bits / 64;
+        if (full) HG_CUDA(cudaMemcpyAsync(dst, bs.words, full * 8, cudaMemcpyHostToDevice, st));
+        if (bits % 64) {
+          uint64_t last = bs.words[full] & ((1ull << (bits % 64)) - 1);
+          // staged through pinned memory: the source must outlive the async copy
+          HG_CUDA(g->pin_in.ensure(8));
+          std::memcpy(g->pin_in.p, &last, 8);
+          HG_CUDA(cudaMemcpyAsync(dst + 2 * full, g->pin_in.p, 8, cudaMemcpyHostToDevice, st));
+          HG_CUDA(cudaStreamSynchronize(st));
+        }
+      }
+    }
+    HG_CUDA(g->fptrs.ensure(a->num_filters * sizeof(void*)));
+    HG_CUDA(cudaMemcpyAsync(g->fptrs.p, ptrs.data(), a->num_filters * sizeof(void*), cudaMemcpyHostToDevice, st));
+    d_fptrs = g->fptrs.as<const uint32_t* const>();
+    HG_CUDA(g->fsel.ensure(nq * 4));
+    if (a->filter_of_query) {
+      for (uint64_t i = 0; i < nq; ++i)
+        if (a->filter_of_query[i] >= static_cast<int32_t>(a->num_filters))
+          return fail(HGD_EINVAL, "hgd_search: filter index out of range");
+      HG_CUDA(cudaMemcpyAsync(g->fsel.p, a->filter_of_query, nq * 4, cudaMemcpyHostToDevice, st));
+    } else {
+      HG_CUDA(cudaMemsetAsync(g->fsel.p, 0, nq * 4, st));
+    }
+    d_fsel = g->fsel.as<int32_t>();
+  }
+  // ---- cosine: 1/||q|| per query ----
+  const float* d_inv = nullptr;
+  if (g->metric == HGD_METRIC_COSINE) {
+    HG_CUDA(g->inv.ensure(nq * 4));
+    HG_CUDA(hg::launch_inv_norm(d_q, static_cast<uint32_t>(nq), dim, g->inv.as<float>(), st));
+    d_inv = g->inv.as<float>();
+  }
+  // ---- outputs ----
+  void* d_out = a->out;
+  uint32_t* d_nres = a->nres;
+  if (!a->out_on_device) {
+    HG_CUDA(g->out.ensure(nq * a->k * 16));
+    d_out = g->out.p;
+    if (a->nres) {
+      HG_CUDA(g->nres.ensure(nq * 4));
+      d_nres = g->nres.as<uint32_t>();
+    }
+  }
+  unsigned long long* d_cnt = nullptr;
+  if (a->counters) {
+    HG_CUDA(g->counters.ensure(nq * hg::kCounters * 8));
+    d_cnt = g->counters.as<unsigned long long>();
+  }
+
+  // ---- launch shape ----
+  hg::SearchParams P{};
+  P.vecs = g->vecs.as<float>();
+  P.l0 = g->l0.as<uint32_t>();
+  P.up = g->up.as<uint32_t>();
+  P.up_blk = g->up_blk.as<uint32_t>();
+  P.labels = g->labels.as<uint64_t>();
+  P.alive = g->alive.as<uint32_t>();
+  P.n = static_cast<uint32_t>(g->n);
+  P.pd = static_cast<uint32_t>(g->pd);
+  P.dim = dim;
+  P.M = static_cast<uint32_t>(g->M);
+  P.M0 = static_cast<uint32_t>(2 * g->M);
+  P.l0_stride = g->l0s;
+  P.up_stride = g->ups;
+  P.metric = g->metric;
+  P.max_level = g->max_level;
+  P.entry = g->entry;
+  P.tagged = g->n < (1ull << 24) ? 1 : 0;
+  P.dedup = g->dedup ? 1 : 0;
+  P.deleted_any = g->num_deleted > 0 ? 1 : 0;
+  P.queries = d_q;
+  P.nq = static_cast<uint32_t>(nq);
+  P.efq = d_ef;
+  P.kq = d_k;
+  P.ef_all = a->ef;
+  P.ef_default = a->ef_default;
+  P.k_all = a->k;
+  P.k_stride = a->k;
+  P.fbits = d_fptrs;
+  P.fsel = d_fsel;
+  P.num_filters = a->num_filters;
+  P.out = d_out;
+  P.nres = d_nres;
+  P.counters = d_cnt;
+  P.R = round_up(ef_max, 32);
+  P.C = std::max<uint32_t>(128, next_pow2(ef_max + 32));
+  P.H = ef_max <= 24 ? 1024 : (ef_max <= 96 ? 2048 : 4096);
+  if (a->cand_cap) {
+    if (a->cand_cap < 128 || (a->cand_cap & (a->cand_cap - 1)))
+      return fail(HGD_EINVAL, "hgd_search: cand_cap must be a power of two >= 128");
+    P.C = a->cand_cap;
+  }
+  if (a->hash_slots) {
+    if (a->hash_slots < 256 || (a->hash_slots & (a->hash_slots - 1)))
+      return fail(HGD_EINVAL, "hgd_search: hash_slots must be a power of two >= 256");
+    P.H = a->hash_slots;
+  }
+  const uint32_t wbytes = hg::warp_smem_bytes(P.H, P.R, P.C);
+  int wpb = static_cast<int>(std::min<uint32_t>(4, (227u * 1024u) / wbytes));
+  if (a->warps_per_block) {
+    if (a->warps_per_block > 4) return fail(HGD_EINVAL, "hgd_search: warps_per_block must be 1..4");
+    wpb = std::min<int>(wpb, static_cast<int>(a->warps_per_block));
+  }
+  if (wpb < 1) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
+  const int occ_blocks = hg::search_occupancy(P.pd, g->metric, wpb, P.H, P.R, P.C);
+  if (occ_blocks < 1) return fail(HGD_ECUDA, "hgd_search: the search kernel cannot be resident with this shape");
+  const uint64_t want_blocks = (nq + wpb - 1) / wpb;
+  const int blocks = static_cast<int>(std::min<uint64_t>(want_blocks, static_cast<uint64_t>(g->sms) * occ_blocks));
+  const uint64_t slots = static_cast<uint64_t>(blocks) * wpb;
+  const uint64_t bw = (g->n + 31) / 32 + 1;
+  uint64_t pool_cap = std::min<uint64_t>(std::max<uint64_t>(g->n, 1), 8192);
+  if (a->pool_cap) pool_cap = std::max<uint64_t>(a->pool_cap, 32);
+  HG_CUDA(g->pool.ensure(slots * pool_cap * 8));
+  HG_CUDA(g->bitmaps.ensure(slots * bw * 4));
+  HG_CUDA(g->work.ensure(64));
+  HG_CUDA(g->ovf_list.ensure(nq * 4));
+  HG_CUDA(cudaMemsetAsync(g->work.p, 0, 64, st));
+  P.pool = g->pool.as<uint64_t>();
+  P.pool_cap = pool_cap;
+  P.bitmaps = g->bitmaps.as<uint32_t>();
+  P.bitmap_words = bw;
+  P.work = g->work.as<uint32_t>();
+  P.ovf_count = g->work.as<uint32_t>() + 1;
+  P.ovf_list = g->ovf_list.as<uint32_t>();
+  {
+    cudaError_t e = hg::launch_search(P, d_inv, blocks, wpb, st);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("search kernel launch: ") + cudaGetErrorString(e));
+  }
+  // ---- rerun of queries whose spill pool overflowed: pool of n entries ----
+  {
+    const uint64_t big_slots = static_cast<uint64_t>(g->sms);
+    const uint64_t big_cap = std::max<uint64_t>(g->n, 1);
+    HG_CUDA(g->pool_big.ensure(big_slots * big_cap * 8));
+    HG_CUDA(g->bitmaps_big.ensure(big_slots * bw * 4));
+    hg::SearchParams B = P;
+    B.nq_dev = g->work.as<uint32_t>() + 1;
+    B.qidx = g->ovf_list.as<uint32_t>();
+    B.work = g->work.as<uint32_t>() + 2;
+    B.pool = g->pool_big.as<uint64_t>();
+    B.pool_cap = big_cap;
+    B.bitmaps = g->bitmaps_big.as<uint32_t>();
+    B.ovf_count = g->work.as<uint32_t>() + 3;  // cannot overflow: cap = n
+    B.ovf_list = g->ovf_list.as<uint32_t>();
+    cudaError_t e = hg::launch_search(B, d_inv, static_cast<int>(big_slots), 1, st);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("rerun kernel launch: ") + cudaGetErrorString(e));
+  }
+  // ---- results back ----
+  if (!a->out_on_device) {
+    HG_CUDA(cudaMemcpyAsync(a->out, d_out, nq * a->k * 16, cudaMemcpyDeviceToHost, st));
+    if (a->nres) HG_CUDA(cudaMemcpyAsync(a->nres, d_nres, nq * 4, cudaMemcpyDeviceToHost, st));
+  }
+  if (a->counters)
+    HG_CUDA(cudaMemcpyAsync(a->counters, d_cnt, nq * hg::kCounters * 8, cudaMemcpyDeviceToHost, st));
+  if (a->synchronize || !a->out_on_device || a->counters) HG_CUDA(cudaStreamSynchronize(st));
+  return HGD_OK;
+}
+
+}  // extern "C"

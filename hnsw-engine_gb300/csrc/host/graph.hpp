@@ -1,0 +1,180 @@
+// graph.hpp -- host state behind hnsw::Index.
+//
+// The arrays are those of the reference's Index::Impl
+// (src/index_impl.hpp:193-214) and of FORMAT v1, so a loaded file can be
+// re-saved byte for byte and uploaded to HBM without conversion:
+//   vectors   count x padded_dim float32 (64-byte aligned rows, zero tail)
+//   level0    count x (1 + 2M) uint32  [n, ids...]
+//   upper     per node with level L >= 1: L blocks of (1 + M) uint32
+//   labels    count x uint64;  levels count x uint8;  deleted count x uint8
+#pragma once
+
+#include <atomic>
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <shared_mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "hnsw/index.hpp"
+#include "hnswgpu_device.h"
+
+namespace hnsw::gb {
+
+inline constexpr std::size_t kRowAlign = 64;  // bytes; rows are padded to 16 floats
+inline constexpr std::size_t kPadFloats = 16;
+inline constexpr uint32_t kNoNode = ~uint32_t{0};
+inline constexpr int kMaxLevel = 64;
+inline constexpr std::size_t kStripes = 4096;
+
+inline std::size_t round_up(std::size_t v, std::size_t m) { return (v + m - 1) / m * m; }
+
+template <typename T>
+struct Aligned64 {
+  using value_type = T;
+  Aligned64() noexcept = default;
+  template <typename U>
+  Aligned64(const Aligned64<U>&) noexcept {}  // NOLINT
+  T* allocate(std::size_t n) {
+    if (n == 0) return nullptr;
+    return static_cast<T*>(::operator new(round_up(n * sizeof(T), kRowAlign), std::align_val_t{kRowAlign}));
+  }
+  void deallocate(T* p, std::size_t) noexcept { ::operator delete(p, std::align_val_t{kRowAlign}); }
+  template <typename U>
+  bool operator==(const Aligned64<U>&) const noexcept {
+    return true;
+  }
+};
+
+/// (distance, internal id) with the reference's total order (index_impl.hpp:58-71).
+struct Cand {
+  float dist;
+  uint32_t id;
+};
+inline bool closer(const Cand& a, const Cand& b) noexcept {
+  return a.dist < b.dist || (a.dist == b.dist && a.id < b.id);
+}
+struct CloserFirst {  // heap comparator: max-heap on (dist, id)
+  bool operator()(const Cand& a, const Cand& b) const noexcept { return closer(a, b); }
+};
+struct FartherFirst {  // heap comparator: min-heap on (dist, id)
+  bool operator()(const Cand& a, const Cand& b) const noexcept { return closer(b, a); }
+};
+
+/// Read-only file mapping (load with mmap = true).
+class Mapping {
+ public:
+  Mapping() = default;
+  explicit Mapping(const std::string& path);
+  ~Mapping();
+  Mapping(Mapping&& o) noexcept;
+  Mapping& operator=(Mapping&& o) noexcept;
+  Mapping(const Mapping&) = delete;
+  Mapping& operator=(const Mapping&) = delete;
+  const unsigned char* data() const noexcept { return data_; }
+  std::size_t size() const noexcept { return size_; }
+
+ private:
+  void reset() noexcept;
+  const unsigned char* data_ = nullptr;
+  std::size_t size_ = 0;
+};
+
+/// Per-thread scratch of the CPU builder (the graph search during insertion).
+struct BuildScratch {
+  std::vector<uint32_t> mark;
+  uint32_t epoch = 0;
+  std::vector<Cand> cand, res, tmp;
+  std::vector<uint32_t> nbuf;
+  void begin(std::size_t n) {
+    if (mark.size() < n) {
+      mark.assign(n, 0);
+      epoch = 0;
+    }
+    if (++epoch == 0) {
+      std::fill(mark.begin(), mark.end(), 0u);
+      epoch = 1;
+    }
+  }
+};
+
+}  // namespace hnsw::gb
+
+namespace hnsw {
+
+struct Index::Impl {
+  Params params;
+  std::size_t dim = 0, padded_dim = 0, M = 0, M0 = 0, ef_construction = 0, ef_search = 10;
+  double mL = 0.0;
+  std::size_t l0_stride = 0, upper_stride = 0;
+  simd::Isa isa = simd::Isa::AVX512;
+  simd::DistanceFn kernel = nullptr;
+  bool is_l2 = true;
+
+  std::vector<float, gb::Aligned64<float>> vec_store;
+  std::vector<uint32_t, gb::Aligned64<uint32_t>> l0_store;
+  std::vector<uint32_t> upper_store;
+  std::vector<uint64_t> label_store;
+  std::vector<uint8_t> level_store;
+  const float* vecs = nullptr;
+  uint32_t* l0 = nullptr;
+  uint32_t* upper = nullptr;
+  const uint64_t* labels = nullptr;
+  const uint8_t* levels = nullptr;
+
+  std::vector<uint64_t> upper_offset;
+  std::vector<uint8_t> deleted;
+  std::size_t num_deleted = 0;
+  std::unordered_map<uint64_t, uint32_t> label_to_id;
+  std::size_t count = 0, capacity = 0, upper_used = 0;
+  uint32_t entry_point = gb::kNoNode;
+  int max_level = -1;
+  uint64_t rng_state = 0;
+  gb::Mapping mapping;
+  bool read_only = false;
+
+  mutable std::shared_mutex api_mutex;
+  std::mutex top_mutex;
+  std::unique_ptr<std::mutex[]> stripes{new std::mutex[gb::kStripes]};
+  std::mutex scratch_mutex;
+  std::vector<std::unique_ptr<gb::BuildScratch>> scratch_free;
+
+  // GPU mirror (rebuilt lazily after add; tombstones are patched in place)
+  int device = 0;
+  mutable std::mutex dev_mutex;
+  mutable hgd_graph* dev = nullptr;
+  mutable bool dev_stale = true;
+
+  explicit Impl(const Params& p);
+  ~Impl();
+
+  float dist(const float* a, const float* b) const noexcept {
+    const float r = kernel(a, b, padded_dim);
+    return is_l2 ? r : 1.0f - r;
+  }
+  const float* vec(uint32_t id) const noexcept { return vecs + std::size_t{id} * padded_dim; }
+  uint32_t* list0(uint32_t id) const noexcept { return l0 + std::size_t{id} * l0_stride; }
+  uint32_t* list(uint32_t id, int level) const noexcept {
+    return level == 0 ? list0(id) : upper + upper_offset[id] + std::size_t(level - 1) * upper_stride;
+  }
+  std::size_t degree_cap(int level) const noexcept { return level == 0 ? M0 : M; }
+  std::mutex& lock_of(uint32_t id) const noexcept { return stripes[id & (gb::kStripes - 1)]; }
+  void bind_pointers();
+  void grow(std::size_t n);
+
+  // construction (build.cpp)
+  int draw_level();
+  uint32_t append(const float* v, uint64_t label);
+  void link(uint32_t id);
+  std::unique_ptr<gb::BuildScratch> take_scratch();
+  void give_scratch(std::unique_ptr<gb::BuildScratch> s);
+
+  // device mirror (index.cpp)
+  hgd_graph* device_graph() const;
+};
+
+}  // namespace hnsw

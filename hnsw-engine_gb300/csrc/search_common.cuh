@@ -1,0 +1,59 @@
+// search_common.cuh -- types shared by the search kernels and their host launcher.
+#pragma once
+#include <cstdint>
+
+namespace hg {
+
+constexpr uint32_t kNoId = 0xFFFFFFFFu;
+constexpr int kCounters = 8;
+enum : uint32_t { kTierBitmap = 1u, kTierPool = 2u, kTierRerun = 4u };
+
+// Everything one launch of the query kernel reads.  Device pointers unless noted.
+struct SearchParams {
+  // ---- graph (resident) ----
+  const float* vecs;        // n x pd, 64-byte rows, prepared (cosine: unit)
+  const uint32_t* l0;       // n x l0_stride neighbour ids, kNoId padded
+  const uint32_t* up;       // upper blocks of up_stride ids, kNoId padded
+  const uint32_t* up_blk;   // n: block index of level 1 (levels 1..L contiguous)
+  const uint64_t* labels;   // n
+  const uint32_t* alive;    // n bits: 1 = not deleted
+  uint32_t n, pd, dim, M, M0, l0_stride, up_stride;
+  int32_t metric, max_level;
+  uint32_t entry;
+  int32_t tagged;           // n < 2^24: visited hash slots carry an 8-bit epoch
+  int32_t dedup;            // some neighbour list repeats an id
+  int32_t deleted_any;      // num_deleted > 0 (reference switches to the filtered variant)
+  // ---- batch ----
+  const float* queries;     // nq x dim raw
+  uint32_t nq;
+  const uint32_t* nq_dev;   // if set, nq is read from here (rerun pass)
+  const uint32_t* qidx;     // if set, the i-th work item is query qidx[i]
+  const uint32_t* efq;      // per query ef (0 = default) or null
+  const uint32_t* kq;       // per query k or null
+  uint32_t ef_all, ef_default, k_all, k_stride;
+  const uint32_t* const* fbits;  // per filter: id-space bitset (n bits)
+  const int32_t* fsel;           // per query filter index (-1 none) or null
+  uint32_t num_filters;
+  void* out;                     // 16-byte records
+  uint32_t* nres;                // per query result count or null
+  // ---- per-warp shared layout ----
+  uint32_t H;  // visited hash slots (power of two)
+  uint32_t R;  // result capacity (>= every ef)
+  uint32_t C;  // candidate head capacity (power of two, >= 64)
+  // ---- global scratch, per warp slot ----
+  uint64_t* pool;           // candidate spill pool
+  uint64_t pool_cap;        // entries per slot
+  uint32_t* bitmaps;        // visited bitmap tier
+  uint64_t bitmap_words;    // words per slot
+  uint32_t* work;           // work-queue counter (zeroed before launch)
+  uint32_t* ovf_list;       // queries whose pool overflowed
+  uint32_t* ovf_count;
+  unsigned long long* counters;  // nq x kCounters or null
+};
+
+__host__ __device__ inline uint32_t warp_smem_bytes(uint32_t H, uint32_t R, uint32_t C) {
+  // hash + results + candidates (+32 slack) + two 32-entry staging arrays
+  return 4u * H + 8u * R + 8u * (C + 32u) + 2u * 8u * 32u;
+}
+
+}  // namespace hg

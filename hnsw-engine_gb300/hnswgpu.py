@@ -1,0 +1,409 @@
+"""Python binding of libhnswgpu over its C ABI (include/hnswgpu.h).
+
+Mirrors the reference's Python module (python/bindings.cpp:114-233): the same
+``Index`` constructor, ``add`` / ``search`` / ``save`` / ``load`` /
+``mark_deleted`` / properties, the same filter forms (None, a callable on
+labels, a bool mask over labels, an integer allow-list) and the same int64
+ids with -1 padding.  Queries are answered on the GPU; there is no CPU search
+path, and importing this module without the built library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libhnswgpu.so"
+
+HG_OK, HG_EINVAL, HG_ERUNTIME, HG_ERANGE = 0, 1, 2, 3
+METRICS = {"l2": 0, "ip": 1, "inner_product": 1, "cosine": 2}
+METRIC_NAMES = {0: "l2", 1: "ip", 2: "cosine"}
+ORDERS = {"scalar": 0, "avx2": 1, "avx512": 2, "neon": 3}
+INVALID_LABEL = 0xFFFFFFFFFFFFFFFF
+NCOUNTERS = 8
+
+NEIGHBOR = np.dtype([("label", "<u8"), ("distance", "<f4"), ("reserved", "<u4")])
+
+PRED = C.CFUNCTYPE(C.c_int, C.c_uint64, C.c_void_p)
+
+
+class _Filter(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("words", C.c_void_p), ("num_labels", C.c_uint64),
+                ("fn", PRED), ("ctx", C.c_void_p)]
+
+
+class _BatchOptions(C.Structure):
+    _fields_ = [("ef_per_query", C.c_void_p), ("k_per_query", C.c_void_p), ("filters", C.POINTER(_Filter)),
+                ("num_filters", C.c_size_t), ("filter_of_query", C.c_void_p), ("stream", C.c_void_p),
+                ("precision", C.c_int32), ("reserved", C.c_int32), ("counters", C.c_void_p),
+                ("hash_slots", C.c_uint32), ("cand_cap", C.c_uint32), ("warps_per_block", C.c_uint32),
+                ("pool_cap", C.c_uint32)]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libhnswgpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() (or hnsw-engine_gb300/build.py)")
+        L = C.CDLL(str(LIB_PATH))
+        vp, sz, u64, i32 = C.c_void_p, C.c_size_t, C.c_uint64, C.c_int
+        L.hg_last_error.restype = C.c_char_p
+        L.hg_index_create.argtypes = [sz, i32, sz, sz, sz, u64, C.POINTER(vp)]
+        L.hg_index_load.argtypes = [C.c_char_p, i32, C.POINTER(vp)]
+        L.hg_index_save.argtypes = [vp, C.c_char_p]
+        L.hg_index_free.argtypes = [vp]
+        L.hg_index_add_batch.argtypes = [vp, vp, vp, sz, sz]
+        L.hg_index_search.argtypes = [vp, vp, sz, sz, C.POINTER(_Filter), vp, C.POINTER(sz)]
+        L.hg_index_search_batch.argtypes = [vp, vp, sz, sz, sz, vp, sz, C.POINTER(_Filter)]
+        L.hg_index_search_batch_ex.argtypes = [vp, vp, sz, sz, sz, vp, C.POINTER(_BatchOptions)]
+        L.hg_index_mark_deleted.argtypes = [vp, u64]
+        L.hg_index_is_deleted.argtypes = [vp, u64, C.POINTER(i32)]
+        L.hg_index_contains.argtypes = [vp, u64, C.POINTER(i32)]
+        L.hg_index_get_vector.argtypes = [vp, u64, vp, sz]
+        L.hg_index_set_ef.argtypes = [vp, sz]
+        L.hg_index_set_device.argtypes = [vp, i32]
+        for name in ("size", "dim", "M", "ef_construction", "ef", "capacity", "memory_usage"):
+            fn = getattr(L, f"hg_index_{name}")
+            fn.argtypes = [vp]
+            fn.restype = sz
+        for name in ("metric", "max_level", "read_only"):
+            fn = getattr(L, f"hg_index_{name}")
+            fn.argtypes = [vp]
+            fn.restype = i32
+        L.hg_bruteforce_create.argtypes = [sz, i32, C.POINTER(vp)]
+        L.hg_bruteforce_add.argtypes = [vp, vp, vp, sz]
+        L.hg_bruteforce_search_batch.argtypes = [vp, vp, sz, sz, vp, C.POINTER(_Filter)]
+        L.hg_bruteforce_free.argtypes = [vp]
+        L.hg_set_distance_order.argtypes = [i32]
+        L.hg_get_distance_order.restype = i32
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc == HG_OK:
+        return
+    msg = lib().hg_last_error().decode(errors="replace")
+    if rc == HG_EINVAL:
+        raise ValueError(msg)
+    if rc == HG_ERANGE:
+        raise IndexError(msg)
+    raise RuntimeError(msg)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def set_distance_order(name: str):
+    """Summation order reproduced by indexes created/loaded afterwards (simd::set_active)."""
+    _check(lib().hg_set_distance_order(ORDERS[name]))
+
+
+def distance_order() -> str:
+    return {v: k for k, v in ORDERS.items()}[lib().hg_get_distance_order()]
+
+
+def _to_labels(ids, n: int, start: int) -> np.ndarray:
+    if ids is None:
+        return np.arange(start, start + n, dtype=np.uint64)
+    arr = np.asarray(ids)
+    if arr.ndim == 0:
+        arr = arr.reshape(1)
+    if arr.ndim != 1 or arr.shape[0] != n:
+        raise ValueError(f"ids: expected shape ({n},)")
+    if arr.dtype.kind == "i":
+        if (arr < 0).any():
+            raise ValueError("ids: labels must be non-negative")
+        return arr.astype(np.uint64)
+    if arr.dtype.kind == "u":
+        return arr.astype(np.uint64)
+    raise TypeError("ids: expected an integer array")
+
+
+class _FilterHolder:
+    """Keeps a C filter description and the memory it points to alive."""
+
+    def __init__(self, spec):
+        self.struct = None
+        self.keep = []
+        if spec is None:
+            return
+        f = _Filter()
+        if isinstance(spec, (np.ndarray, list, tuple)):
+            arr = np.asarray(spec)
+            if arr.ndim != 1:
+                raise ValueError("filter: expected a 1-D array")
+            if arr.dtype.kind == "b":
+                words = _pack_mask(arr)
+                f.kind, f.num_labels = 1, arr.shape[0]
+            elif arr.dtype.kind in "iu":
+                labels = _to_labels(arr, arr.shape[0], 0)
+                size = int(labels.max()) + 1 if labels.size else 0
+                mask = np.zeros(size, dtype=bool)
+                mask[labels.astype(np.int64)] = True
+                words = _pack_mask(mask)
+                f.kind, f.num_labels = 1, size
+            else:
+                raise TypeError("filter: array must be bool (mask over labels) or integer (allowed labels)")
+            self.keep.append(words)
+            f.words = words.ctypes.data
+        elif isinstance(spec, tuple) is False and hasattr(spec, "words") and hasattr(spec, "num_labels"):
+            words = np.ascontiguousarray(spec.words, dtype=np.uint64)
+            self.keep.append(words)
+            f.kind, f.words, f.num_labels = 1, words.ctypes.data, int(spec.num_labels)
+        elif callable(spec):
+            fn = PRED(lambda label, ctx: 1 if spec(int(label)) else 0)
+            self.keep.append(fn)
+            f.kind, f.fn = 2, fn
+        else:
+            raise TypeError("filter: expected None, a callable(label) -> bool, a bool mask or an id array")
+        self.struct = f
+
+    def ref(self):
+        return None if self.struct is None else C.byref(self.struct)
+
+
+def _pack_mask(mask: np.ndarray) -> np.ndarray:
+    n = mask.shape[0]
+    nwords = max((n + 63) // 64, 1)
+    padded = np.zeros(nwords * 64, dtype=bool)
+    padded[:n] = mask
+    return np.packbits(padded.reshape(-1, 8), axis=1, bitorder="little").reshape(-1).view(np.uint64).copy()
+
+
+class Bitset:
+    """A BitsetFilter given directly as words (bit l of words[l >> 6])."""
+
+    def __init__(self, words, num_labels: int):
+        self.words = np.ascontiguousarray(words, dtype=np.uint64)
+        self.num_labels = int(num_labels)
+
+
+class Index:
+    """HNSW index (hnsw::Index); construction on the CPU, queries on the GPU."""
+
+    def __init__(self, dim: int = 0, metric: str = "l2", M: int = 16, ef_construction: int = 200,
+                 max_elements: int = 0, seed: int = 100, _handle=None):
+        self._h = None
+        if _handle is not None:
+            self._h = _handle
+            return
+        h = C.c_void_p()
+        if metric not in METRICS:
+            raise ValueError(f"unknown metric '{metric}' (expected l2, ip or cosine)")
+        _check(lib().hg_index_create(dim, METRICS[metric], M, ef_construction, max_elements, seed, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().hg_index_free(self._h)
+            self._h = None
+
+    @staticmethod
+    def load(path, mmap: bool = False) -> "Index":
+        h = C.c_void_p()
+        _check(lib().hg_index_load(str(path).encode(), 1 if mmap else 0, C.byref(h)))
+        return Index(_handle=h)
+
+    def save(self, path):
+        _check(lib().hg_index_save(self._h, str(path).encode()))
+
+    def add(self, vectors, ids=None, num_threads: int = 0):
+        v = np.ascontiguousarray(vectors, dtype=np.float32)
+        if v.ndim == 1:
+            v = v.reshape(1, -1)
+        if v.shape[1] != self.dim:
+            raise ValueError(f"vectors: expected shape (n, {self.dim})")
+        labels = _to_labels(ids, v.shape[0], len(self))
+        _check(lib().hg_index_add_batch(self._h, _ptr(v), _ptr(labels), v.shape[0], num_threads))
+
+    def _queries(self, queries):
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        single = q.ndim == 1
+        if single:
+            q = q.reshape(1, -1)
+        if q.ndim != 2 or q.shape[1] != self.dim:
+            raise ValueError(f"queries: expected shape (n, {self.dim})")
+        return q, single
+
+    def search_raw(self, queries, k: int = 10, ef: int = 0, filter=None) -> np.ndarray:
+        """search_batch into hnsw::Neighbor records (labels uint64, kInvalidLabel padding)."""
+        if k <= 0:
+            raise ValueError("k must be > 0")
+        q, _ = self._queries(queries)
+        out = np.empty(q.shape[0] * k, dtype=NEIGHBOR)
+        fh = _FilterHolder(filter)
+        _check(lib().hg_index_search_batch(self._h, _ptr(q), q.shape[0], k, ef or 0, _ptr(out), 0, fh.ref()))
+        return out.reshape(q.shape[0], k)
+
+    def search(self, queries, k: int = 10, ef=None, num_threads: int = 0, filter=None):
+        """(ids int64 with -1 padding, distances float32), as the reference's binding returns."""
+        if k <= 0:
+            raise ValueError("k must be > 0")
+        q, single = self._queries(queries)
+        rec = self.search_raw(q, k, ef or 0, filter)
+        ids = rec["label"].astype(np.int64)  # kInvalidLabel -> -1
+        d = rec["distance"].copy()
+        return (ids[0], d[0]) if single else (ids, d)
+
+    def search_one(self, q, k: int = 10, ef: int = 0, filter=None):
+        """Index::search: at most k results, no padding."""
+        q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1)
+        out = np.empty(k, dtype=NEIGHBOR)
+        n = C.c_size_t()
+        fh = _FilterHolder(filter)
+        _check(lib().hg_index_search(self._h, _ptr(q), k, ef, fh.ref(), _ptr(out), C.byref(n)))
+        return out[:n.value]
+
+    def search_batch_ex(self, queries, k: int, ef: int = 0, ef_per_query=None, k_per_query=None, filters=None,
+                        filter_of_query=None, stream=None, precision: int = 0, counters: bool = False,
+                        hash_slots: int = 0, cand_cap: int = 0, warps_per_block: int = 0, pool_cap: int = 0):
+        q, _ = self._queries(queries)
+        nq = q.shape[0]
+        out = np.empty(nq * k, dtype=NEIGHBOR)
+        opt = _BatchOptions()
+        keep = []
+        if ef_per_query is not None:
+            a = np.ascontiguousarray(ef_per_query, dtype=np.uint32)
+            keep.append(a)
+            opt.ef_per_query = a.ctypes.data
+        if k_per_query is not None:
+            a = np.ascontiguousarray(k_per_query, dtype=np.uint32)
+            keep.append(a)
+            opt.k_per_query = a.ctypes.data
+        holders = [_FilterHolder(f) for f in (filters or [])]
+        if holders:
+            arr = (_Filter * len(holders))(*[h.struct for h in holders])
+            keep.append(arr)
+            opt.filters = C.cast(arr, C.POINTER(_Filter))
+            opt.num_filters = len(holders)
+        if filter_of_query is not None:
+            a = np.ascontiguousarray(filter_of_query, dtype=np.int32)
+            keep.append(a)
+            opt.filter_of_query = a.ctypes.data
+        if stream is not None:
+            opt.stream = stream
+        opt.precision = precision
+        opt.hash_slots, opt.cand_cap = hash_slots, cand_cap
+        opt.warps_per_block, opt.pool_cap = warps_per_block, pool_cap
+        cnt = None
+        if counters:
+            cnt = np.zeros((nq, NCOUNTERS), dtype=np.uint64)
+            opt.counters = cnt.ctypes.data
+        _check(lib().hg_index_search_batch_ex(self._h, _ptr(q), nq, k, ef, _ptr(out), C.byref(opt)))
+        out = out.reshape(nq, k)
+        return (out, cnt) if counters else out
+
+    def set_ef(self, ef: int):
+        _check(lib().hg_index_set_ef(self._h, ef))
+
+    def set_device(self, device: int):
+        _check(lib().hg_index_set_device(self._h, device))
+
+    def mark_deleted(self, label: int):
+        if label < 0:
+            raise ValueError("labels are non-negative")
+        _check(lib().hg_index_mark_deleted(self._h, int(label)))
+
+    def is_deleted(self, label: int) -> bool:
+        if label < 0:
+            return False
+        r = C.c_int()
+        _check(lib().hg_index_is_deleted(self._h, int(label), C.byref(r)))
+        return bool(r.value)
+
+    def __contains__(self, label) -> bool:
+        if label < 0:
+            return False
+        r = C.c_int()
+        _check(lib().hg_index_contains(self._h, int(label), C.byref(r)))
+        return bool(r.value)
+
+    def get_vector(self, label: int) -> np.ndarray:
+        if label < 0:
+            raise ValueError("labels are non-negative")
+        out = np.empty(self.dim, dtype=np.float32)
+        _check(lib().hg_index_get_vector(self._h, int(label), _ptr(out), self.dim))
+        return out
+
+    def __len__(self):
+        return lib().hg_index_size(self._h)
+
+    @property
+    def dim(self):
+        return lib().hg_index_dim(self._h)
+
+    @property
+    def metric(self):
+        return METRIC_NAMES[lib().hg_index_metric(self._h)]
+
+    @property
+    def M(self):
+        return lib().hg_index_M(self._h)
+
+    @property
+    def ef_construction(self):
+        return lib().hg_index_ef_construction(self._h)
+
+    @property
+    def ef(self):
+        return lib().hg_index_ef(self._h)
+
+    @ef.setter
+    def ef(self, v):
+        self.set_ef(v)
+
+    @property
+    def capacity(self):
+        return lib().hg_index_capacity(self._h)
+
+    @property
+    def max_level(self):
+        return lib().hg_index_max_level(self._h)
+
+    @property
+    def read_only(self):
+        return bool(lib().hg_index_read_only(self._h))
+
+    @property
+    def memory_usage(self):
+        return lib().hg_index_memory_usage(self._h)
+
+    def __repr__(self):
+        return (f"<hnswgpu.Index dim={self.dim} metric={self.metric} M={self.M} size={len(self)}"
+                + (" read_only" if self.read_only else "") + ">")
+
+
+class BruteForceIndex:
+    """Exact k-NN (hnsw::BruteForceIndex) on the GPU."""
+
+    def __init__(self, dim: int, metric: str = "l2"):
+        self._h = None
+        h = C.c_void_p()
+        _check(lib().hg_bruteforce_create(dim, METRICS[metric], C.byref(h)))
+        self._h = h
+        self.dim = dim
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().hg_bruteforce_free(self._h)
+            self._h = None
+
+    def add(self, vectors, labels=None):
+        v = np.ascontiguousarray(vectors, dtype=np.float32).reshape(-1, self.dim)
+        lab = None if labels is None else np.ascontiguousarray(labels, dtype=np.uint64)
+        _check(lib().hg_bruteforce_add(self._h, _ptr(v), _ptr(lab), v.shape[0]))
+
+    def search_raw(self, queries, k: int, filter=None) -> np.ndarray:
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self.dim)
+        out = np.empty(q.shape[0] * k, dtype=NEIGHBOR)
+        fh = _FilterHolder(filter)
+        _check(lib().hg_bruteforce_search_batch(self._h, _ptr(q), q.shape[0], k, _ptr(out), fh.ref()))
+        return out.reshape(q.shape[0], k)

@@ -1,0 +1,134 @@
+#pragma once
+// hnsw::Index for GB300: the reference's public C++ API
+// (include/hnsw/index.hpp:14-118) with queries answered on the GPU.
+//
+// The graph lives in host memory exactly as the reference lays it out
+// (FORMAT v1 sections) and is mirrored into HBM on first use; mutations
+// (add, mark_deleted) update the mirror before the next search.  search /
+// search_batch run the greedy descent and layer-0 beam search as CUDA
+// kernels and return the reference's ids and distances.
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "hnsw/filter.hpp"
+#include "hnsw/metric.hpp"
+
+namespace hnsw {
+
+struct Params {
+  std::size_t dim = 0;
+  Metric metric = Metric::L2;
+  std::size_t M = 16;
+  std::size_t ef_construction = 200;
+  std::size_t max_elements = 0;  ///< 0 = grow geometrically
+  uint64_t seed = 100;
+};
+
+struct Neighbor {
+  uint64_t label;
+  float distance;
+};
+
+inline constexpr uint64_t kInvalidLabel = ~uint64_t{0};
+
+/// Options beyond the reference's signature, for batched/served callers.
+struct SearchOptions {
+  const uint32_t* ef_per_query = nullptr;  ///< nq entries (host), overrides ef
+  const uint32_t* k_per_query = nullptr;   ///< nq entries (host), each <= k
+  const Filter* const* filters = nullptr;  ///< per-query filter table
+  std::size_t num_filters = 0;
+  const int32_t* filter_of_query = nullptr;  ///< nq entries, -1 = none
+  void* stream = nullptr;                    ///< cudaStream_t; nullptr = the index's own stream
+  int precision = 0;                         ///< 0 fp32, 1 fp16, 2 fp8 (traversal; exact fp32 rerank)
+  uint64_t* counters = nullptr;              ///< optional nq x 8 traversal counters
+  // launch shape (0 = automatic): visited-hash slots, candidate head
+  // capacity, warps per block, spill-pool entries per warp
+  uint32_t hash_slots = 0, cand_cap = 0, warps_per_block = 0, pool_cap = 0;
+};
+
+class Index {
+ public:
+  explicit Index(const Params& params);
+  ~Index();
+  Index(Index&&) noexcept;
+  Index& operator=(Index&&) noexcept;
+  Index(const Index&) = delete;
+  Index& operator=(const Index&) = delete;
+
+  void add(const float* vec, uint64_t label);
+  void add_batch(const float* vecs, const uint64_t* labels, std::size_t n, std::size_t num_threads = 0);
+
+  std::vector<Neighbor> search(const float* q, std::size_t k, std::size_t ef = 0, const Filter* f = nullptr) const;
+  /// num_threads is accepted for source compatibility; the GPU runs all queries.
+  void search_batch(const float* qs, std::size_t nq, std::size_t k, std::size_t ef, Neighbor* out,
+                    std::size_t num_threads = 0, const Filter* f = nullptr) const;
+  /// Batched search with per-query ef / k / filter and an explicit stream.
+  void search_batch_ex(const float* qs, std::size_t nq, std::size_t k, std::size_t ef, Neighbor* out,
+                       const SearchOptions& opt) const;
+
+  void mark_deleted(uint64_t label);
+  bool is_deleted(uint64_t label) const;
+  bool contains(uint64_t label) const;
+
+  std::size_t size() const;
+  std::size_t dim() const noexcept;
+  Metric metric() const noexcept;
+  const Params& params() const noexcept;
+  std::size_t capacity() const;
+  std::size_t ef() const;
+  void set_ef(std::size_t ef);
+  int max_level() const;
+  bool read_only() const noexcept;
+  std::size_t memory_usage() const;
+  std::vector<float> get_vector(uint64_t label) const;
+
+  void save(const std::string& path) const;
+  static Index load(const std::string& path, bool mmap = false);
+
+  /// CUDA device the graph is mirrored to (default 0); call before the first search.
+  void set_device(int device);
+
+  struct Impl;
+  Impl* impl() const noexcept { return impl_.get(); }
+
+ private:
+  explicit Index(std::unique_ptr<Impl> impl);
+  std::unique_ptr<Impl> impl_;
+};
+
+namespace tuning {
+/// Kept for source compatibility with the reference's ablation switch (the
+/// GPU kernels overlap gathers through warps, not software prefetch).
+void set_prefetch(bool enabled) noexcept;
+bool prefetch_enabled() noexcept;
+}  // namespace tuning
+
+/// Exact search over all vectors (ground truth), on the GPU.
+class BruteForceIndex {
+ public:
+  BruteForceIndex(std::size_t dim, Metric metric);
+  ~BruteForceIndex();
+  BruteForceIndex(BruteForceIndex&&) noexcept;
+  BruteForceIndex& operator=(BruteForceIndex&&) noexcept;
+  void add(const float* vecs, const uint64_t* labels, std::size_t n);
+  std::vector<Neighbor> search(const float* q, std::size_t k, const Filter* f = nullptr) const;
+  void search_batch(const float* qs, std::size_t nq, std::size_t k, Neighbor* out, std::size_t num_threads = 0,
+                    const Filter* f = nullptr) const;
+  std::size_t size() const noexcept { return labels_.size(); }
+  std::size_t dim() const noexcept { return dim_; }
+
+  struct Dev;
+
+ private:
+  std::size_t dim_;
+  Metric metric_;
+  std::vector<float> data_;
+  std::vector<uint64_t> labels_;
+  mutable std::unique_ptr<Dev> dev_;
+};
+
+}  // namespace hnsw

@@ -1,0 +1,132 @@
+/* hnswgpu.h -- C ABI of hnsw-gb300 for foreign-function callers.
+ *
+ * Each entry point is one hnsw::Index operation (GPU-answered queries, CPU
+ * construction, FORMAT v1 files), with plain pointers and sizes and an
+ * integer status instead of exceptions: HG_OK, or HG_EINVAL where the
+ * reference throws std::invalid_argument, HG_ERANGE for std::out_of_range,
+ * HG_ERUNTIME for std::runtime_error (I/O, corrupt file, read-only, full,
+ * CUDA failure).  hg_last_error() returns the message of the last failure on
+ * the calling thread.
+ *
+ * Reference interface each entry point replaces (paths within hnsw-engine):
+ *   hg_index_create        Index(const Params&)                 include/hnsw/index.hpp:39; src/index.cpp:48-67
+ *   hg_index_load          Index::load(path, mmap)              include/hnsw/index.hpp:86; src/persist.cpp:476-541
+ *   hg_index_save          Index::save                          include/hnsw/index.hpp:83; src/persist.cpp:421-474
+ *   hg_index_free          ~Index                               include/hnsw/index.hpp:40
+ *   hg_index_add_batch     Index::add_batch                     include/hnsw/index.hpp:50; src/index.cpp:273-306
+ *   hg_index_search        Index::search                        include/hnsw/index.hpp:55; src/search_layer.cpp:173-178
+ *   hg_index_search_batch  Index::search_batch                  include/hnsw/index.hpp:59; src/search_layer.cpp:180-194
+ *   hg_index_search_batch_ex  search_batch with per-query ef/k/filter (one reference call per group)
+ *   hg_index_mark_deleted  Index::mark_deleted                  include/hnsw/index.hpp:64; src/index.cpp:308-318
+ *   hg_index_is_deleted / hg_index_contains / hg_index_get_vector / accessors
+ *                          include/hnsw/index.hpp:65-81;  src/index.cpp:320-379
+ *   hg_index_set_ef        Index::set_ef                        src/index.cpp:352-356
+ *   hg_bruteforce_*        BruteForceIndex                      include/hnsw/index.hpp:103-118; src/brute_force.cpp
+ *   hg_set_distance_order  simd::set_active                     include/hnsw/metric.hpp:212
+ * Filters: hg_filter describes a BitsetFilter (label bitset) or a
+ * FunctionFilter (a predicate callback), include/hnsw/filter.hpp:12-48.
+ */
+#ifndef HNSWGPU_H
+#define HNSWGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { HG_OK = 0, HG_EINVAL = 1, HG_ERUNTIME = 2, HG_ERANGE = 3 };
+enum { HG_METRIC_L2 = 0, HG_METRIC_IP = 1, HG_METRIC_COSINE = 2 };
+enum { HG_ORDER_SCALAR = 0, HG_ORDER_AVX2 = 1, HG_ORDER_AVX512 = 2, HG_ORDER_NEON = 3 };
+enum { HG_FILTER_NONE = 0, HG_FILTER_BITSET = 1, HG_FILTER_PREDICATE = 2 };
+
+#define HG_INVALID_LABEL (~(uint64_t)0)
+
+typedef struct hg_index hg_index;
+typedef struct hg_bruteforce hg_bruteforce;
+
+/* Layout of hnsw::Neighbor: 16 bytes, the last 4 are zero. */
+typedef struct {
+  uint64_t label;
+  float distance;
+  uint32_t reserved;
+} hg_neighbor;
+
+/* A label filter.  BITSET: bit l of words[l / 64] allows label l, labels >=
+ * num_labels are rejected.  PREDICATE: fn(label, ctx) != 0 allows label; it
+ * is called once per node of the index before the GPU search starts. */
+typedef struct {
+  int32_t kind;
+  int32_t reserved;
+  const uint64_t* words;
+  uint64_t num_labels;
+  int (*fn)(uint64_t label, void* ctx);
+  void* ctx;
+} hg_filter;
+
+/* Optional batch controls (hnsw::SearchOptions). */
+typedef struct {
+  const uint32_t* ef_per_query;    /* nq entries or NULL */
+  const uint32_t* k_per_query;     /* nq entries (each 1..k) or NULL */
+  const hg_filter* filters;        /* filter table */
+  size_t num_filters;
+  const int32_t* filter_of_query;  /* nq entries, -1 = none; NULL = filter 0 for all */
+  void* stream;                    /* cudaStream_t, NULL = the index's own */
+  int32_t precision;               /* 0 fp32; 1 fp16; 2 fp8 traversal with exact fp32 rerank */
+  int32_t reserved;
+  uint64_t* counters;              /* nq x 8 traversal counters or NULL */
+  uint32_t hash_slots;             /* launch shape, 0 = automatic: visited-hash slots per warp */
+  uint32_t cand_cap;               /* candidate head capacity per warp */
+  uint32_t warps_per_block;
+  uint32_t pool_cap;               /* spill-pool entries per warp before a query is rerun */
+} hg_batch_options;
+
+const char* hg_last_error(void);
+
+int hg_index_create(size_t dim, int metric, size_t M, size_t ef_construction, size_t max_elements, uint64_t seed,
+                    hg_index** out);
+int hg_index_load(const char* path, int mmap, hg_index** out);
+int hg_index_save(const hg_index* idx, const char* path);
+void hg_index_free(hg_index* idx);
+int hg_index_add_batch(hg_index* idx, const float* vecs, const uint64_t* labels, size_t n, size_t num_threads);
+
+int hg_index_search(const hg_index* idx, const float* q, size_t k, size_t ef, const hg_filter* filter,
+                    hg_neighbor* out, size_t* n_out);
+int hg_index_search_batch(const hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef, hg_neighbor* out,
+                          size_t num_threads, const hg_filter* filter);
+int hg_index_search_batch_ex(const hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef,
+                             hg_neighbor* out, const hg_batch_options* opt);
+
+int hg_index_mark_deleted(hg_index* idx, uint64_t label);
+int hg_index_is_deleted(const hg_index* idx, uint64_t label, int* out);
+int hg_index_contains(const hg_index* idx, uint64_t label, int* out);
+int hg_index_get_vector(const hg_index* idx, uint64_t label, float* out, size_t dim);
+int hg_index_set_ef(hg_index* idx, size_t ef);
+int hg_index_set_device(hg_index* idx, int device);
+
+size_t hg_index_size(const hg_index* idx);
+size_t hg_index_dim(const hg_index* idx);
+int hg_index_metric(const hg_index* idx);
+size_t hg_index_M(const hg_index* idx);
+size_t hg_index_ef_construction(const hg_index* idx);
+size_t hg_index_ef(const hg_index* idx);
+size_t hg_index_capacity(const hg_index* idx);
+int hg_index_max_level(const hg_index* idx);
+int hg_index_read_only(const hg_index* idx);
+size_t hg_index_memory_usage(const hg_index* idx);
+
+int hg_bruteforce_create(size_t dim, int metric, hg_bruteforce** out);
+int hg_bruteforce_add(hg_bruteforce* bf, const float* vecs, const uint64_t* labels, size_t n);
+int hg_bruteforce_search_batch(const hg_bruteforce* bf, const float* qs, size_t nq, size_t k, hg_neighbor* out,
+                               const hg_filter* filter);
+void hg_bruteforce_free(hg_bruteforce* bf);
+
+/* Distance summation order for indexes created or loaded afterwards. */
+int hg_set_distance_order(int order);
+int hg_get_distance_order(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HNSWGPU_H */

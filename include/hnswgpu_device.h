@@ -1,0 +1,133 @@
+/* hnswgpu_device.h -- the CUDA side of hnsw-gb300 behind a plain C ABI.
+ *
+ * This is the thin layer the C++20 host code (hnsw::Index) calls: it takes
+ * the graph in the reference's in-memory layout as host pointers, mirrors it
+ * into HBM once, and runs the batched query path as sm_103a kernels.  No C++
+ * types, exceptions or STL cross this boundary: every call returns an
+ * HGD_* status and hgd_last_error() describes the last failure on the calling
+ * thread.
+ *
+ * Reference interfaces this layer replaces (paths within hnsw-engine):
+ *   hgd_graph_upload      the arrays behind Index::Impl       src/index_impl.hpp:193-214
+ *   hgd_graph_set_deleted the tombstone write of mark_deleted  src/index.cpp:308-318
+ *   hgd_search            search_unlocked over a batch         src/search_layer.cpp:146-194
+ *   hgd_bruteforce        BruteForceIndex::search_batch        src/brute_force.cpp:34-69
+ */
+#ifndef HNSWGPU_DEVICE_H
+#define HNSWGPU_DEVICE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  HGD_OK = 0,
+  HGD_EINVAL = 1,   /* bad argument (std::invalid_argument on the C++ side) */
+  HGD_ERUNTIME = 2, /* runtime failure (std::runtime_error) */
+  HGD_ECUDA = 3,    /* a CUDA call failed */
+  HGD_ENOMEM = 4    /* device memory exhausted */
+};
+
+enum { HGD_METRIC_L2 = 0, HGD_METRIC_IP = 1, HGD_METRIC_COSINE = 2 };
+
+/* Summation order of the distance reduction: the order of the reference's
+ * kernel on the host whose results are to be reproduced bit for bit. */
+enum { HGD_ORDER_SCALAR = 0, HGD_ORDER_AVX2 = 1, HGD_ORDER_AVX512 = 2, HGD_ORDER_NEON = 3 };
+
+/* Traversal precision: FP32 is the reference's arithmetic; FP16 / FP8 (E4M3
+ * with a per-vector scale) walk the graph on a compressed copy of the
+ * vectors and rerank the final pool in exact FP32. */
+enum { HGD_PREC_FP32 = 0, HGD_PREC_FP16 = 1, HGD_PREC_FP8 = 2 };
+
+#define HGD_NCOUNTERS 8 /* per query: upper lists, upper distances, layer-0 lists,
+                           layer-0 distances, visited, peak candidates, results,
+                           tier flags (1 global visited set, 2 spill pool, 4 rerun) */
+
+typedef struct hgd_graph hgd_graph;
+
+/* A graph as Index::Impl holds it (FORMAT v1 sections + derived arrays). */
+typedef struct {
+  uint64_t count;
+  uint64_t dim;
+  uint64_t padded_dim;
+  uint64_t M;
+  int32_t metric;
+  int32_t max_level;
+  uint32_t entry_point;
+  uint32_t reserved;
+  const float* vectors;         /* count x padded_dim, prepared (cosine: unit) */
+  const uint32_t* level0;       /* count x (1 + 2M): [n, ids...] */
+  const uint32_t* upper;        /* upper_used words: per node, levels 1..L of [n, ids(M)] */
+  uint64_t upper_used;
+  const uint64_t* upper_offset; /* count, in uint32 units */
+  const uint64_t* labels;       /* count */
+  const uint8_t* levels;        /* count */
+  const uint8_t* deleted;       /* count, 0/1 */
+} hgd_graph_view;
+
+/* A filter bitset: bit b of words[b >> 6].  label_space = 1: indexed by
+ * external label (BitsetFilter); 0: indexed by internal id (already
+ * translated on the host, e.g. a FunctionFilter).  Host memory. */
+typedef struct {
+  const uint64_t* words;
+  uint64_t num_bits;
+  int32_t label_space;
+  int32_t reserved;
+} hgd_bitset;
+
+/* One batch.  Records of `out` are 16 bytes: {uint64 label, float distance,
+ * uint32 zero}, the layout of hnsw::Neighbor; rows have stride k. */
+typedef struct {
+  const float* queries;          /* nq x dim, raw (cosine normalised on device) */
+  int32_t queries_on_device;     /* 1: queries / ef / k arrays are device pointers */
+  int32_t out_on_device;         /* 1: out / nres are device pointers */
+  uint64_t nq;
+  uint32_t k;                    /* row stride of out, >= every per-query k */
+  uint32_t ef;                   /* 0: use ef_default */
+  uint32_t ef_default;           /* the index's set_ef value */
+  uint32_t precision;            /* HGD_PREC_* */
+  const uint32_t* ef_per_query;  /* nullable; 0 entries mean ef_default */
+  const uint32_t* k_per_query;   /* nullable */
+  const hgd_bitset* filters;     /* host array of num_filters bitsets */
+  uint32_t num_filters;
+  uint32_t reserved;
+  const int32_t* filter_of_query; /* host, nq entries, -1 = unfiltered; NULL: filter 0 for all if any */
+  void* out;                     /* nq*k records */
+  uint32_t* nres;                /* nullable: per-query result count (no padding) */
+  void* stream;                  /* cudaStream_t; NULL = the graph's stream */
+  uint64_t* counters;            /* nullable host array, nq x HGD_NCOUNTERS */
+  int32_t synchronize;           /* 1: return after the results are in `out` */
+  int32_t reserved2;
+  /* launch shape; 0 = chosen from ef (the autotuner's table) */
+  uint32_t hash_slots;           /* visited hash per warp (power of two >= 256) */
+  uint32_t cand_cap;             /* candidate head per warp (power of two >= 128) */
+  uint32_t warps_per_block;      /* 1..4 */
+  uint32_t pool_cap;             /* spill pool entries per warp before a rerun */
+} hgd_search_args;
+
+int hgd_graph_upload(const hgd_graph_view* view, int device, int order, hgd_graph** out);
+int hgd_graph_set_deleted(hgd_graph* g, uint32_t id, int deleted);
+int hgd_graph_set_order(hgd_graph* g, int order);
+void hgd_graph_free(hgd_graph* g);
+/* Device bytes held by the mirror (vectors, lists, labels, bitsets, scratch). */
+uint64_t hgd_graph_device_bytes(const hgd_graph* g);
+
+int hgd_search(hgd_graph* g, const hgd_search_args* a);
+
+/* Exact k-NN over n prepared vectors (dim, unpadded), labels per row. */
+typedef struct hgd_flat hgd_flat;
+int hgd_flat_upload(const float* prepared, const uint64_t* labels, uint64_t n, uint64_t dim, int metric, int device,
+                    int order, hgd_flat** out);
+void hgd_flat_free(hgd_flat* f);
+int hgd_bruteforce(hgd_flat* f, const float* queries, uint64_t nq, uint32_t k, const hgd_bitset* filter, void* out,
+                   void* stream);
+
+const char* hgd_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HNSWGPU_DEVICE_H */
