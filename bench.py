@@ -1,0 +1,328 @@
+"""Benchmark of the batched HNSW query path on GB300.
+
+Workload (default): batched L2 at 200k -- n=200,000 vectors of d=128 from a
+256-cluster integer Gaussian mixture (seed 0), M=16, ef_construction=200,
+10,000 queries (seed 1) per step with per-query ef drawn uniformly from
+{10,20,40,80,160,320}, k=10, answered in one persistent launch.  The data
+are synthetic stand-ins with SIFT's shape (the ann-benchmarks sets are not
+available offline); recall@10 is measured against exact k-NN.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is QPS with queries already in HBM
+(device pointers, CUDA events on the launch stream, L2 flushed between
+steps); `e2e` is QPS through the host C ABI with pinned host buffers, the
+host->device copy of the queries and the device->host copy of the results
+inside the timed region.  --impl reference times the reference algorithm on
+the host cores (the oracle's C restatement of search_batch, all threads).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "hnsw-engine_gb300"))
+sys.path.insert(0, str(REPO / "oracle"))
+
+N_BASE, DIM, CLUSTERS, NQ, K = 200_000, 128, 256, 10_000, 10
+EF_CHOICES = (10, 20, 40, 80, 160, 320)
+M, EFC = 16, 200
+METRIC = "QPS at recall@10>=0.95 (batched mixed-ef search, 200k x 128 L2)"
+WORKLOAD = "batched-L2-200k: n=200000 d=128 M=16 efC=200, 10000 queries/step, per-query ef U{10..320}, k=10"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(rank: int):
+    import workloads
+
+    base, queries = workloads.int_mixture(N_BASE, DIM, CLUSTERS, NQ)
+    efs = np.random.default_rng(3 + rank).choice(np.array(EF_CHOICES, dtype=np.uint32), size=NQ)
+    return base, queries, efs
+
+
+def algorithmic_bytes(cnt: np.ndarray) -> float:
+    """Bytes a query must move: query row, upper/level-0 lists, one row per
+    distance, the tombstone bit word per level-0 candidate, the output row."""
+    row = 4 * 128
+    up_list, l0_list = 4 * (1 + M), 4 * (1 + 2 * M)
+    per_q = (4 * DIM + cnt[:, 0] * up_list + cnt[:, 1] * row + cnt[:, 2] * l0_list + cnt[:, 3] * row + K * 16)
+    return float(per_q.sum())
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = max(mx, float(f[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    import hnswgpu
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    base, queries, efs = workload(rank)
+    # graph: built with the library's CPU add_batch (all host threads), saved in
+    # FORMAT v1 and loaded back -- the file a CPU reference would also load
+    tmp = Path(tempfile.mkdtemp(prefix="hnswbench"))
+    gpath = tmp / "graph.idx"
+    t0 = time.time()
+    ix = hnswgpu.Index(DIM, "l2", M, EFC)
+    ix.add(base, num_threads=0)
+    ix.save(gpath)
+    build_s = time.time() - t0
+    ix = hnswgpu.Index.load(gpath)
+    ix.set_device(local)
+
+    # ground truth: exact k-NN on the GPU (brute force), FP32 exact on integer data
+    bf = hnswgpu.BruteForceIndex(DIM, "l2")
+    bf.add(base)
+    gt = bf.search_raw(queries, K)["label"].astype(np.int64)
+    del bf
+
+    stream = torch.cuda.Stream(device=dev)
+    q_d = torch.from_numpy(queries).to(dev)
+    ef_d = torch.from_numpy(efs.astype(np.int32)).to(dev)
+    out_d = torch.empty((NQ, K, 4), dtype=torch.int32, device=dev)  # 16-byte records
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+    ef_max = int(efs.max())
+
+    def step_device():
+        ix.search_device(q_d.data_ptr(), NQ, K, ef_max, out_d.data_ptr(), stream.cuda_stream, ef_ptr=ef_d.data_ptr())
+
+    # recall and traversal counters of this batch (untimed)
+    rec, cnt = ix.search_batch_ex(queries, K, ef_per_query=efs, counters=True)
+    got = rec["label"].astype(np.int64)
+    import workloads
+
+    recall = workloads.recall_at_k(got, gt)
+    alg_bytes = algorithmic_bytes(cnt)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            step_device()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        clocks = Clocks(local)
+        with clocks:
+            wall0 = time.perf_counter()
+            for i in range(args.steps):
+                flush.zero_()
+                ev[i][0].record(stream)
+                step_device()
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - wall0
+        if world > 1:
+            torch.distributed.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_ms = sum(step_ms)
+    # device output equals the host-path output
+    dev_rec = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(NQ, K)
+    if not np.array_equal(dev_rec["label"], rec["label"]):
+        raise RuntimeError("device-resident batch differs from the host-path batch")
+
+    # e2e through the host C ABI with pinned host buffers
+    q_pin = torch.from_numpy(queries).pin_memory()
+    ef_pin = torch.from_numpy(efs.astype(np.uint32).view(np.int32)).pin_memory()
+    out_pin = torch.empty((NQ, K, 4), dtype=torch.int32).pin_memory()
+    qn = q_pin.numpy()
+    efn = ef_pin.numpy().view(np.uint32)
+    e2e_ms = []
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup + args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ix.search_batch_ex(qn, K, ef_per_query=efn, stream=stream.cuda_stream,
+                               out=out_pin.numpy().view(hnswgpu.NEIGHBOR).reshape(-1))
+            b.record(stream)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                e2e_ms.append(a.elapsed_time(b))
+    e2e_total = sum(e2e_ms)
+
+    times = torch.tensor([dev_ms, e2e_total], dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    dev_ms, e2e_total = float(times[0]), float(times[1])
+    qps = world * NQ * args.steps / (dev_ms / 1e3)
+    e2e_qps = world * NQ * args.steps / (e2e_total / 1e3)
+    per_launch_ms = dev_ms / args.steps
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    result = {
+        "metric": METRIC, "value": round(qps, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(per_launch_ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian mixture, SIFT shape)",
+        "config": {"workload": WORKLOAD, "global_batch": world * NQ, "recall_at_10": round(recall, 4),
+                   "ef_mix": list(EF_CHOICES), "l2_flush": "256 MiB write before every timed step",
+                   "parallelism": f"replicas x{world} (queries per replica fixed)", "build_s": round(build_s, 2),
+                   "mean_l0_expansions": round(float(cnt[:, 2].mean()), 2),
+                   "mean_l0_distances": round(float(cnt[:, 3].mean()), 2)},
+        "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": int(NQ * DIM * 4 + NQ * 4),
+                "d2h_bytes_per_step": int(NQ * K * 16)},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(alg_bytes)},
+        "clocks": clocks.summary(),
+        "wall_s": round(wall, 3),
+    }
+    if rank == 0 and world == 1:
+        result["cpu_baseline"] = cpu_baseline(gpath, queries, efs)
+    return result
+
+
+def cpu_baseline(gpath, queries, efs, sample=None):
+    """The reference algorithm (oracle restatement of search_batch) on the host
+    cores, grouped per ef like one reference call per group."""
+    import pyoracle
+
+    threads = os.cpu_count() or 1
+    ox = pyoracle.OracleIndex(gpath, isa=pyoracle.host_isa())
+    nq = queries.shape[0] if sample is None else sample
+    qs, es = queries[:nq], efs[:nq]
+    t0 = time.perf_counter()
+    for ef in EF_CHOICES:
+        sel = es == ef
+        if sel.any():
+            ox.search_batch(qs[sel], K, int(ef), threads=threads)
+    el = time.perf_counter() - t0
+    return {"value": round(nq / el, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{nq} queries of the same mixed-ef batch, one search_batch per ef group, "
+                      f"{threads} threads, distance order {pyoracle.host_isa()}"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference algorithm on the host cores."""
+    if rank != 0:
+        return None
+    import hnswgpu  # only to build the same graph file
+
+    base, queries, efs = workload(0)
+    tmp = Path(tempfile.mkdtemp(prefix="hnswref"))
+    gpath = tmp / "graph.idx"
+    ix = hnswgpu.Index(DIM, "l2", M, EFC)
+    ix.add(base, num_threads=0)
+    ix.save(gpath)
+    sample = 4000
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(gpath, queries, efs, sample=sample)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = statistics.median(vals)
+    ms = sample / v * 1e3
+    return {"metric": METRIC, "value": round(v, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian mixture, SIFT shape)",
+            "config": {"workload": WORKLOAD}, "impl": "reference",
+            "cpu_baseline": {"value": round(v, 1), "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{sample} queries per step of the mixed-ef batch, all host threads"},
+            "e2e": {"value": round(v, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_ours(args, rank, world, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

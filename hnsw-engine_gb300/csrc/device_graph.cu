@@ -449,7 +449,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   P.counters = d_cnt;
   P.R = round_up(ef_max, 32);
   P.C = std::max<uint32_t>(128, next_pow2(ef_max + 32));
-  P.H = ef_max <= 24 ? 1024 : (ef_max <= 96 ? 2048 : 4096);
+  P.H = ef_max <= 16 ? 2048 : 4096;
   if (a->cand_cap) {
     if (a->cand_cap < 128 || (a->cand_cap & (a->cand_cap - 1)))
       return fail(HGD_EINVAL, "hgd_search: cand_cap must be a power of two >= 128");
@@ -487,6 +487,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   P.work = g->work.as<uint32_t>();
   P.ovf_count = g->work.as<uint32_t>() + 1;
   P.ovf_list = g->ovf_list.as<uint32_t>();
+  P.err = g->work.as<uint32_t>() + 4;
   {
     cudaError_t e = hg::launch_search(P, d_inv, blocks, wpb, st);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("search kernel launch: ") + cudaGetErrorString(e));
@@ -516,7 +517,13 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   }
   if (a->counters)
     HG_CUDA(cudaMemcpyAsync(a->counters, d_cnt, nq * hg::kCounters * 8, cudaMemcpyDeviceToHost, st));
-  if (a->synchronize || !a->out_on_device || a->counters) HG_CUDA(cudaStreamSynchronize(st));
+  HG_CUDA(g->pin_out.ensure(8));
+  HG_CUDA(cudaMemcpyAsync(g->pin_out.p, g->work.as<uint32_t>() + 4, 4, cudaMemcpyDeviceToHost, st));
+  if (a->synchronize || !a->out_on_device || a->counters) {
+    HG_CUDA(cudaStreamSynchronize(st));
+    if (*static_cast<uint32_t*>(g->pin_out.p) != 0)
+      return fail(HGD_EINVAL, "hgd_search: a per-query ef or k exceeds the bound given for this batch");
+  }
   return HGD_OK;
 }
 

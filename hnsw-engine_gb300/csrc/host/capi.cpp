@@ -174,6 +174,8 @@ int hg_index_search_batch_ex(const hg_index* idx, const float* qs, size_t nq, si
       opt.cand_cap = o->cand_cap;
       opt.warps_per_block = o->warps_per_block;
       opt.pool_cap = o->pool_cap;
+      opt.queries_on_device = o->queries_on_device != 0;
+      opt.out_on_device = o->out_on_device != 0;
     }
     idx->index.search_batch_ex(qs, nq, k, ef, reinterpret_cast<hnsw::Neighbor*>(out), opt);
   });

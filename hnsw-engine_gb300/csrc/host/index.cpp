@@ -113,6 +113,7 @@ void Index::search_batch_ex(const float* qs, std::size_t nq, std::size_t k, std:
   std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
   const Impl& im = *impl_;
   if (im.count == 0) {
+    if (opt.out_on_device) throw std::invalid_argument("search_batch: empty index with a device output buffer");
     for (std::size_t i = 0; i < nq * k; ++i) out[i] = Neighbor{kInvalidLabel, std::numeric_limits<float>::infinity()};
     return;
   }
@@ -139,7 +140,9 @@ void Index::search_batch_ex(const float* qs, std::size_t nq, std::size_t k, std:
   a.out = out;
   a.stream = opt.stream;
   a.counters = opt.counters;
-  a.synchronize = 1;
+  a.queries_on_device = opt.queries_on_device ? 1 : 0;
+  a.out_on_device = opt.out_on_device ? 1 : 0;
+  a.synchronize = opt.out_on_device ? 0 : 1;
   a.hash_slots = opt.hash_slots;
   a.cand_cap = opt.cand_cap;
   a.warps_per_block = opt.warps_per_block;

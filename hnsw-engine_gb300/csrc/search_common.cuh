@@ -49,6 +49,7 @@ struct SearchParams {
   uint32_t* ovf_list;       // queries whose pool overflowed
   uint32_t* ovf_count;
   unsigned long long* counters;  // nq x kCounters or null
+  uint32_t* err;                 // set to 1 if a per-query ef / k exceeds this launch's capacity
 };
 
 __host__ __device__ inline uint32_t warp_smem_bytes(uint32_t H, uint32_t R, uint32_t C) {

@@ -455,8 +455,21 @@ __device__ void refill(Warp& w, Cands& c, const SearchParams& P, bool res_full, 
 }
 
 // Insert the sorted accepted batch stA[0..m) into the candidate queue.
-__device__ void cand_insert(Warp& w, Cands& c, const SearchParams& P, int m, int lane) {
+// res_full / worst_d: once the result set is full, head keys farther than the
+// worst result are dropped before anything would spill to the pool.
+__device__ void cand_insert(Warp& w, Cands& c, const SearchParams& P, int m, bool res_full, float worst_d,
+                            int lane) {
   if (m <= 0) return;
+  if (res_full && c.ct - c.ch + m > static_cast<int>(P.C) - c.ch) {
+    // first head index whose distance exceeds the worst result
+    int lo = c.ch, hi = c.ct;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (key_dist(w.cand[mid]) > worst_d) hi = mid;
+      else lo = mid + 1;
+    }
+    c.ct = lo;
+  }
   int mh = m;
   if (c.pn > 0) {
     const bool lt = lane < m && w.stA[lane] < c.pmin;
@@ -542,6 +555,11 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
     uint32_t ef = P.efq ? P.efq[q] : P.ef_all;
     if (ef == 0) ef = P.ef_default;
     if (ef < k) ef = k;
+    if (ef > P.R || k > P.k_stride || k == 0) {
+      // device-side arrays promised a smaller bound: refuse this query
+      if (lane == 0) atomicExch(P.err, 1u);
+      continue;
+    }
     const uint32_t* fb = nullptr;
     if (P.fsel) {
       const int32_t f = P.fsel[q];
@@ -725,11 +743,10 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
           const int mA = __popc(acc), mE = __popc(ins);
           s = warp_merge(w.res, s, static_cast<int>(ef), w.stE, mE, lane);
           int mAk = mA;
-          if (s >= static_cast<int>(ef)) {
-            const float wd = key_dist(w.res[s - 1]);
-            mAk = __popc(__ballot_sync(kFull, lane < mA && key_dist(w.stA[lane]) <= wd));
-          }
-          cand_insert(w, c, P, mAk, lane);
+          const bool full = s >= static_cast<int>(ef);
+          const float wd = full ? key_dist(w.res[s - 1]) : 0.0f;
+          if (full) mAk = __popc(__ballot_sync(kFull, lane < mA && key_dist(w.stA[lane]) <= wd));
+          cand_insert(w, c, P, mAk, full, wd, lane);
           if (c.overflow) break;
         }
         if (c.overflow) break;

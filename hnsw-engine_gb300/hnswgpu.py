@@ -39,7 +39,7 @@ class _BatchOptions(C.Structure):
                 ("num_filters", C.c_size_t), ("filter_of_query", C.c_void_p), ("stream", C.c_void_p),
                 ("precision", C.c_int32), ("reserved", C.c_int32), ("counters", C.c_void_p),
                 ("hash_slots", C.c_uint32), ("cand_cap", C.c_uint32), ("warps_per_block", C.c_uint32),
-                ("pool_cap", C.c_uint32)]
+                ("pool_cap", C.c_uint32), ("queries_on_device", C.c_int32), ("out_on_device", C.c_int32)]
 
 
 _lib = None
@@ -264,10 +264,14 @@ class Index:
 
     def search_batch_ex(self, queries, k: int, ef: int = 0, ef_per_query=None, k_per_query=None, filters=None,
                         filter_of_query=None, stream=None, precision: int = 0, counters: bool = False,
-                        hash_slots: int = 0, cand_cap: int = 0, warps_per_block: int = 0, pool_cap: int = 0):
+                        hash_slots: int = 0, cand_cap: int = 0, warps_per_block: int = 0, pool_cap: int = 0,
+                        out=None):
         q, _ = self._queries(queries)
         nq = q.shape[0]
-        out = np.empty(nq * k, dtype=NEIGHBOR)
+        if out is None:
+            out = np.empty(nq * k, dtype=NEIGHBOR)
+        elif out.dtype != NEIGHBOR or out.size != nq * k or not out.flags.c_contiguous:
+            raise ValueError("out: expected a contiguous NEIGHBOR array of nq*k records")
         opt = _BatchOptions()
         keep = []
         if ef_per_query is not None:
@@ -300,6 +304,19 @@ class Index:
         _check(lib().hg_index_search_batch_ex(self._h, _ptr(q), nq, k, ef, _ptr(out), C.byref(opt)))
         out = out.reshape(nq, k)
         return (out, cnt) if counters else out
+
+    def search_device(self, q_ptr: int, nq: int, k: int, ef: int, out_ptr: int, stream: int = 0,
+                      ef_ptr: int = 0, k_ptr: int = 0):
+        """Enqueue a batch whose queries (nq x dim float32), optional per-query
+        ef / k (uint32) and output records (nq x k x 16 bytes) live in device
+        memory; returns once the work is on `stream` (a cudaStream_t handle)."""
+        opt = _BatchOptions()
+        opt.queries_on_device, opt.out_on_device = 1, 1
+        opt.ef_per_query = ef_ptr or None
+        opt.k_per_query = k_ptr or None
+        opt.stream = stream or None
+        _check(lib().hg_index_search_batch_ex(self._h, C.c_void_p(q_ptr), nq, k, ef, C.c_void_p(out_ptr),
+                                              C.byref(opt)))
 
     def set_ef(self, ef: int):
         _check(lib().hg_index_set_ef(self._h, ef))

@@ -48,6 +48,9 @@ struct SearchOptions {
   // launch shape (0 = automatic): visited-hash slots, candidate head
   // capacity, warps per block, spill-pool entries per warp
   uint32_t hash_slots = 0, cand_cap = 0, warps_per_block = 0, pool_cap = 0;
+  /// device-resident batches: queries / ef / k (and out) are device pointers;
+  /// with out_on_device the call only enqueues work on `stream`.
+  bool queries_on_device = false, out_on_device = false;
 };
 
 class Index {

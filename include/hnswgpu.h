@@ -80,6 +80,10 @@ typedef struct {
   uint32_t cand_cap;               /* candidate head capacity per warp */
   uint32_t warps_per_block;
   uint32_t pool_cap;               /* spill-pool entries per warp before a query is rerun */
+  int32_t queries_on_device;       /* 1: qs, ef_per_query, k_per_query are device pointers
+                                      (then ef must bound every per-query ef) */
+  int32_t out_on_device;           /* 1: out is a device pointer; the call returns once the
+                                      work is queued on `stream` */
 } hg_batch_options;
 
 const char* hg_last_error(void);
