@@ -528,3 +528,70 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free batch over an uploaded graph (hg_index_search_batch_noalloc)
+// ---------------------------------------------------------------------------
+namespace hg {
+uint32_t noalloc_max_nodes();
+uint32_t noalloc_max_queries();
+uint32_t noalloc_max_ef();
+cudaError_t launch_search_noalloc(SearchParams P, int device, bool cosine, cudaStream_t st);
+
+// Queries (nq x dim float32) and out (nq x k records) are device pointers;
+// one ef for the batch (0: ef_default), no filters.  Nothing is allocated:
+// scratch comes from the library's static device array, so batches that
+// overlap on the GPU race on it.  Returns an HGD_* status.
+int search_noalloc(hgd_graph* g, const float* d_queries, uint64_t nq, uint32_t k, uint32_t ef, uint32_t ef_default,
+                   void* d_out, void* stream) {
+  if (!g || !d_queries || !d_out) return fail(HGD_EINVAL, "search (no-alloc): null pointer");
+  if (k == 0) return fail(HGD_EINVAL, "search (no-alloc): k must be > 0");
+  if (nq == 0) return HGD_OK;
+  if (nq > noalloc_max_queries())
+    return fail(HGD_EINVAL, "search (no-alloc): at most " + std::to_string(noalloc_max_queries()) +
+                                " queries per call");
+  if (g->n > noalloc_max_nodes())
+    return fail(HGD_EINVAL, "search (no-alloc): graphs above " + std::to_string(noalloc_max_nodes()) +
+                                " nodes need the allocating entry points");
+  uint32_t e = ef ? ef : ef_default;
+  e = std::max(e, k);
+  if (e == 0 || e > noalloc_max_ef())
+    return fail(HGD_EINVAL, "search (no-alloc): ef (after max(ef, k)) must be 1.." +
+                                std::to_string(noalloc_max_ef()));
+  HG_CUDA(cudaSetDevice(g->device));
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : g->stream;
+  hg::SearchParams P{};
+  P.vecs = g->vecs.as<float>();
+  P.l0 = g->l0.as<uint32_t>();
+  P.up = g->up.as<uint32_t>();
+  P.up_blk = g->up_blk.as<uint32_t>();
+  P.labels = g->labels.as<uint64_t>();
+  P.alive = g->alive.as<uint32_t>();
+  P.n = static_cast<uint32_t>(g->n);
+  P.pd = static_cast<uint32_t>(g->pd);
+  P.dim = static_cast<uint32_t>(g->dim);
+  P.M = static_cast<uint32_t>(g->M);
+  P.M0 = static_cast<uint32_t>(2 * g->M);
+  P.l0_stride = g->l0s;
+  P.up_stride = g->ups;
+  P.metric = g->metric;
+  P.max_level = g->max_level;
+  P.entry = g->entry;
+  P.tagged = g->n < (1ull << 24) ? 1 : 0;
+  P.dedup = g->dedup ? 1 : 0;
+  P.deleted_any = g->num_deleted > 0 ? 1 : 0;
+  P.queries = d_queries;
+  P.nq = static_cast<uint32_t>(nq);
+  P.ef_all = e;
+  P.ef_default = e;
+  P.k_all = k;
+  P.k_stride = k;
+  P.out = d_out;
+  P.R = round_up(e, 32);
+  P.C = std::max<uint32_t>(128, next_pow2(e + 32));
+  P.H = 4096;
+  const cudaError_t ce = hg::launch_search_noalloc(P, g->device, g->metric == HGD_METRIC_COSINE, st);
+  if (ce != cudaSuccess) return fail(HGD_ECUDA, std::string("search (no-alloc): ") + cudaGetErrorString(ce));
+  return HGD_OK;
+}
+}  // namespace hg

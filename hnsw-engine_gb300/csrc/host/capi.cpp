@@ -7,8 +7,15 @@
 #include <string>
 #include <vector>
 
+#include "graph.hpp"
 #include "hnsw/index.hpp"
 #include "hnswgpu.h"
+
+namespace hg {
+// device_graph.cu: batch over a mirrored graph with scratch from a static device array
+int search_noalloc(hgd_graph* g, const float* d_queries, uint64_t nq, uint32_t k, uint32_t ef, uint32_t ef_default,
+                   void* d_out, void* stream);
+}  // namespace hg
 
 struct hg_index {
   hnsw::Index index;
@@ -260,6 +267,30 @@ int hg_bruteforce_search_batch(const hg_bruteforce* bf, const float* qs, size_t 
 }
 
 void hg_bruteforce_free(hg_bruteforce* bf) { delete bf; }
+
+int hg_index_search_batch_noalloc(const hg_index* idx, const float* queries, size_t nq, size_t k, size_t ef,
+                                  hg_neighbor* out, void* stream) {
+  return guarded([&] {
+    if (!idx) throw std::invalid_argument("search_batch (no-alloc): null index");
+    if (k == 0) throw std::invalid_argument("search_batch: k must be > 0");
+    if (k > 0xFFFFFFFFull || ef > 0xFFFFFFFFull) throw std::invalid_argument("search_batch: k / ef out of range");
+    const hnsw::Index::Impl* im = idx->index.impl();
+    std::shared_lock<std::shared_mutex> lk(im->api_mutex);
+    hgd_graph* g = nullptr;
+    {
+      std::lock_guard<std::mutex> dg(im->dev_mutex);
+      if (im->dev == nullptr || im->dev_stale)
+        throw std::runtime_error(
+            "search_batch (no-alloc): the graph is not mirrored on the GPU; run one allocating search first");
+      g = im->dev;
+    }
+    const uint32_t ef_default = static_cast<uint32_t>(std::min<size_t>(im->ef_search, 0xFFFFFFFFull));
+    const int rc = hg::search_noalloc(g, queries, nq, static_cast<uint32_t>(k), static_cast<uint32_t>(ef),
+                                      ef_default, out, stream);
+    if (rc == HGD_EINVAL) throw std::invalid_argument(hgd_last_error());
+    if (rc != HGD_OK) throw std::runtime_error(hgd_last_error());
+  });
+}
 
 int hg_set_distance_order(int order) {
   return guarded([&] {

@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "search_common.cuh"
 
@@ -896,6 +897,110 @@ int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, u
   if (S <= 17) return occupancy_s<17, 2>(metric, threads, smem);
   if (S <= 33) return occupancy_s<33, 1>(metric, threads, smem);
   return 0;
+}
+
+}  // namespace hg
+
+// ---------------------------------------------------------------------------
+// Batches that allocate nothing.
+//
+// Some callers cannot call cudaMalloc while they search: a serving process
+// that hands the GPU to other work under a fixed memory budget, code running
+// inside a region where allocation would synchronise the device or is
+// forbidden, or a host framework that owns every device allocation itself.
+// For them the search kernel also runs with its scratch (work counters, spill
+// pools, visited bitmaps, the rerun list and the cosine norms) placed in the
+// file-scope array below instead of buffers the library allocates.  Every
+// GPU that loads the library holds this array (about 15.4 MiB) until the
+// process exits.
+// ---------------------------------------------------------------------------
+namespace hg {
+namespace {
+
+constexpr uint32_t kNaMaxNodes = 1u << 20;    // largest graph
+constexpr uint32_t kNaMaxQueries = 1u << 16;  // largest batch
+constexpr uint32_t kNaMaxEf = 512;            // largest ef (after max(ef, k))
+constexpr int kNaWarpsPerBlock = 4;
+constexpr int kNaBlocks = 12;
+constexpr uint64_t kNaSlots = static_cast<uint64_t>(kNaWarpsPerBlock) * kNaBlocks;
+constexpr uint64_t kNaPoolCap = 2048;                    // spill keys per warp before the rerun pass
+constexpr uint64_t kNaBitmapWords = kNaMaxNodes / 32 + 1;
+
+// byte layout of the array
+constexpr size_t kNaOffCounters = 0;  // u32: [0] work, [1] overflow count, [2] rerun work, [3] spare, [4] error
+constexpr size_t kNaOffOvf = 256;
+constexpr size_t kNaOffInv = kNaOffOvf + 4ull * kNaMaxQueries;
+constexpr size_t kNaOffPool = kNaOffInv + 4ull * kNaMaxQueries;
+constexpr size_t kNaOffBitmaps = kNaOffPool + 8ull * kNaSlots * kNaPoolCap;
+constexpr size_t kNaOffBigPool = kNaOffBitmaps + 4ull * kNaSlots * kNaBitmapWords;
+constexpr size_t kNaOffBigBitmap = kNaOffBigPool + 8ull * kNaMaxNodes;
+constexpr size_t kNaBytes = kNaOffBigBitmap + 4ull * kNaBitmapWords;
+static_assert(kNaOffPool % 8 == 0 && kNaOffBigPool % 8 == 0, "8-byte keys need 8-byte alignment");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+std::mutex g_na_mutex;
+void* g_na_address[64] = {};
+
+// Device address of the array on the current device, looked up once per
+// device (host code cannot use the symbol itself as a device pointer).
+cudaError_t noalloc_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  if (g_na_address[device] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_na_address[device] = p;
+  }
+  *out = static_cast<unsigned char*>(g_na_address[device]);
+  return cudaSuccess;
+}
+
+}  // namespace
+
+uint32_t noalloc_max_nodes() { return kNaMaxNodes; }
+uint32_t noalloc_max_queries() { return kNaMaxQueries; }
+uint32_t noalloc_max_ef() { return kNaMaxEf; }
+
+// Enqueue one batch with scratch from the static array.  P carries the graph
+// and the batch (shape H/R/C included); its scratch fields are filled here.
+// The caller made `device` current.
+cudaError_t launch_search_noalloc(SearchParams P, int device, bool cosine, cudaStream_t st) {
+  unsigned char* base = nullptr;
+  cudaError_t e = noalloc_scratch(device, &base);
+  if (e != cudaSuccess) return e;
+  uint32_t* ctr = reinterpret_cast<uint32_t*>(base + kNaOffCounters);
+  e = cudaMemsetAsync(ctr, 0, 256, st);  // counters and flags must start at zero
+  if (e != cudaSuccess) return e;
+  float* inv = nullptr;
+  if (cosine) {
+    inv = reinterpret_cast<float*>(base + kNaOffInv);
+    e = launch_inv_norm(P.queries, P.nq, P.dim, inv, st);
+    if (e != cudaSuccess) return e;
+  }
+  P.pool = reinterpret_cast<uint64_t*>(base + kNaOffPool);
+  P.pool_cap = kNaPoolCap;
+  P.bitmaps = reinterpret_cast<uint32_t*>(base + kNaOffBitmaps);
+  P.bitmap_words = kNaBitmapWords;
+  P.work = ctr;
+  P.ovf_count = ctr + 1;
+  P.ovf_list = reinterpret_cast<uint32_t*>(base + kNaOffOvf);
+  P.err = ctr + 4;
+  P.nq_dev = nullptr;
+  P.qidx = nullptr;
+  e = launch_search(P, inv, kNaBlocks, kNaWarpsPerBlock, st);
+  if (e != cudaSuccess) return e;
+  // queries whose spill pool overflowed: one warp with a pool of n keys
+  SearchParams B = P;
+  B.nq_dev = ctr + 1;
+  B.qidx = P.ovf_list;
+  B.work = ctr + 2;
+  B.pool = reinterpret_cast<uint64_t*>(base + kNaOffBigPool);
+  B.pool_cap = kNaMaxNodes;
+  B.bitmaps = reinterpret_cast<uint32_t*>(base + kNaOffBigBitmap);
+  B.ovf_count = ctr + 3;
+  return launch_search(B, inv, 1, 1, st);
 }
 
 }  // namespace hg

@@ -80,6 +80,7 @@ def lib():
         L.hg_bruteforce_add.argtypes = [vp, vp, vp, sz]
         L.hg_bruteforce_search_batch.argtypes = [vp, vp, sz, sz, vp, C.POINTER(_Filter)]
         L.hg_bruteforce_free.argtypes = [vp]
+        L.hg_index_search_batch_noalloc.argtypes = [vp, vp, sz, sz, sz, vp, vp]
         L.hg_set_distance_order.argtypes = [i32]
         L.hg_get_distance_order.restype = i32
         _lib = L
@@ -317,6 +318,18 @@ class Index:
         opt.stream = stream or None
         _check(lib().hg_index_search_batch_ex(self._h, C.c_void_p(q_ptr), nq, k, ef, C.c_void_p(out_ptr),
                                               C.byref(opt)))
+
+    def search_noalloc(self, q_ptr: int, nq: int, k: int, ef: int, out_ptr: int, stream: int = 0):
+        """hg_index_search_batch_noalloc: a batch that allocates no device memory.
+
+        For callers that cannot call cudaMalloc while searching.  q_ptr (nq x dim
+        float32) and out_ptr (nq x k 16-byte records) are device addresses the
+        caller owns; scratch is the library's static device array, so batches
+        overlapping on the GPU race.  The graph must already be on the GPU (run
+        any allocating search once first).  Limits: nq <= 65536, index size
+        <= 2^20, max(ef, k) <= 512."""
+        _check(lib().hg_index_search_batch_noalloc(self._h, C.c_void_p(q_ptr), nq, k, ef, C.c_void_p(out_ptr),
+                                                   C.c_void_p(stream) if stream else None))
 
     def set_ef(self, ef: int):
         _check(lib().hg_index_set_ef(self._h, ef))

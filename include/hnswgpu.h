@@ -126,6 +126,25 @@ int hg_bruteforce_search_batch(const hg_bruteforce* bf, const float* qs, size_t 
                                const hg_filter* filter);
 void hg_bruteforce_free(hg_bruteforce* bf);
 
+/* A batch that allocates nothing on the device.  For callers that cannot
+ * call cudaMalloc while they search -- a serving process that runs next to
+ * other GPU work under a fixed memory budget, code inside a region where an
+ * allocation would synchronise the device or is not permitted, a framework
+ * that owns every device allocation.  Queries (nq x dim float32) and out
+ * (nq x k hg_neighbor records) are device pointers the caller allocated; one
+ * ef for the batch (0 = the index's set_ef value); no filter (tombstones
+ * apply).  The work is enqueued on `stream` (NULL = the index's stream) and
+ * the call returns without synchronising.  Scratch lives in a static device
+ * array of about 15.4 MiB that every GPU using the library holds until exit;
+ * batches that overlap on the GPU share it and race, so issue them on one
+ * stream or serialise them.  The first call on a device looks up that
+ * array's device address; make it before any stream capture.  The graph must
+ * already be mirrored on the GPU (any earlier allocating search does it).
+ * Limits: nq <= 65536, index size <= 2^20 nodes, max(ef, k) <= 512; larger
+ * requests return HG_EINVAL.  No counterpart in the reference. */
+int hg_index_search_batch_noalloc(const hg_index* idx, const float* queries, size_t nq, size_t k, size_t ef,
+                                  hg_neighbor* out, void* stream);
+
 /* Distance summation order for indexes created or loaded afterwards. */
 int hg_set_distance_order(int order);
 int hg_get_distance_order(void);
