@@ -57,6 +57,18 @@ def workload(rank: int):
     return base, queries, efs
 
 
+def launches_per_batch(ef_max: int) -> int:
+    """Kernels one batch enqueues: the ef-bucketing kernel, one query kernel per
+    ef bucket (16, 32, 64, ... up to ef_max) and the rerun pass."""
+    buckets, hi = 0, 16
+    while True:
+        buckets += 1
+        if hi >= ef_max or buckets == 12:
+            break
+        hi *= 2
+    return 2 + buckets
+
+
 def algorithmic_bytes(cnt: np.ndarray) -> float:
     """Bytes a query must move: query row, upper/level-0 lists, one row per
     distance, the tombstone bit word per level-0 candidate, the output row."""
@@ -237,7 +249,7 @@ def run_ours(args, rank, world, local):
                    "mean_l0_distances": round(float(cnt[:, 3].mean()), 2)},
         "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": int(NQ * DIM * 4 + NQ * 4),
                 "d2h_bytes_per_step": int(NQ * K * 16)},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches_per_batch(ef_max) * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(alg_bytes)},

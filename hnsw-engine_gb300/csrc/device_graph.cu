@@ -28,6 +28,8 @@ int slots_for(uint32_t pd);
 cudaError_t launch_inv_norm(const float* qs, uint32_t nq, uint32_t dim, float* out, cudaStream_t st);
 cudaError_t launch_search(const SearchParams& P, const float* inv, int blocks, int warps_per_block, cudaStream_t st);
 int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, uint32_t R, uint32_t C);
+cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, uint32_t ef_all, uint32_t ef_default,
+                          uint32_t k_all, const BucketSpec& spec, uint32_t* counts, uint32_t* lists, cudaStream_t st);
 cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bits, const uint64_t* labels, uint32_t n,
                                     uint32_t* out, cudaStream_t st);
 }  // namespace hg
@@ -126,7 +128,10 @@ struct hgd_graph {
   // per call
   DBuf q, efq, kq, fsel, fptrs, fbits, inv, out, nres, counters;
   DBuf work;  // [0] work counter, [1] overflow count, [2] rerun work counter
-  DBuf ovf_list, pool, bitmaps, pool_big, bitmaps_big;
+  DBuf ovf_list, pool, bitmaps, pool_big, bitmaps_big, owners, lists;
+  std::vector<cudaStream_t> aux;    // one per ef bucket
+  std::vector<cudaEvent_t> ev_join;
+  cudaEvent_t ev_fork = nullptr;
   PinnedBuf pin_in, pin_out;
   uint64_t pool_slots = 0, pool_cap = 0, big_slots = 0;
 };
@@ -267,8 +272,11 @@ void hgd_graph_free(hgd_graph* g) {
   cudaSetDevice(g->device);
   for (DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->q, &g->efq, &g->kq, &g->fsel,
                   &g->fptrs, &g->fbits, &g->inv, &g->out, &g->nres, &g->counters, &g->work, &g->ovf_list, &g->pool,
-                  &g->bitmaps, &g->pool_big, &g->bitmaps_big})
+                  &g->bitmaps, &g->pool_big, &g->bitmaps_big, &g->owners, &g->lists})
     d->release();
+  for (cudaStream_t s2 : g->aux) cudaStreamDestroy(s2);
+  for (cudaEvent_t e2 : g->ev_join) cudaEventDestroy(e2);
+  if (g->ev_fork) cudaEventDestroy(g->ev_fork);
   g->pin_in.release();
   g->pin_out.release();
   if (g->stream) cudaStreamDestroy(g->stream);
@@ -280,7 +288,8 @@ uint64_t hgd_graph_device_bytes(const hgd_graph* g) {
   uint64_t t = 0;
   for (const DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->q, &g->efq, &g->kq,
                         &g->fsel, &g->fptrs, &g->fbits, &g->inv, &g->out, &g->nres, &g->counters, &g->work,
-                        &g->ovf_list, &g->pool, &g->bitmaps, &g->pool_big, &g->bitmaps_big})
+                        &g->ovf_list, &g->pool, &g->bitmaps, &g->pool_big, &g->bitmaps_big, &g->owners,
+                        &g->lists})
     t += d->bytes;
   return t;
 }
@@ -447,66 +456,128 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   P.out = d_out;
   P.nres = d_nres;
   P.counters = d_cnt;
-  P.R = round_up(ef_max, 32);
-  P.C = std::max<uint32_t>(128, next_pow2(ef_max + 32));
-  P.H = ef_max <= 16 ? 2048 : 4096;
-  if (a->cand_cap) {
-    if (a->cand_cap < 128 || (a->cand_cap & (a->cand_cap - 1)))
-      return fail(HGD_EINVAL, "hgd_search: cand_cap must be a power of two >= 128");
-    P.C = a->cand_cap;
+  if (a->cand_cap && (a->cand_cap < 128 || a->cand_cap % 32))
+    return fail(HGD_EINVAL, "hgd_search: cand_cap must be a multiple of 32, >= 128");
+  if (a->hash_slots && (a->hash_slots < 256 || (a->hash_slots & (a->hash_slots - 1))))
+    return fail(HGD_EINVAL, "hgd_search: hash_slots must be a power of two >= 256");
+  if (a->warps_per_block > 4) return fail(HGD_EINVAL, "hgd_search: warps_per_block must be 1..4");
+
+  // ---- ef buckets: one launch shape per bucket, sized for its largest ef ----
+  hg::BucketSpec spec{};
+  for (uint32_t hi = 16;; hi *= 2) {
+    spec.hi[spec.n++] = std::min(hi, ef_max);
+    if (hi >= ef_max || spec.n == hg::kMaxBuckets) break;
   }
-  if (a->hash_slots) {
-    if (a->hash_slots < 256 || (a->hash_slots & (a->hash_slots - 1)))
-      return fail(HGD_EINVAL, "hgd_search: hash_slots must be a power of two >= 256");
-    P.H = a->hash_slots;
+  spec.hi[spec.n - 1] = ef_max;
+  struct Shape {
+    uint32_t H, R, C;
+    int wpb, blocks;
+    uint32_t slot_base;
+  };
+  std::vector<Shape> shapes(spec.n);
+  uint64_t slots_total = 0;
+  for (uint32_t b = 0; b < spec.n; ++b) {
+    Shape& sh = shapes[b];
+    const uint32_t E = spec.hi[b];
+    sh.R = round_up(E, 32);
+    sh.C = a->cand_cap ? a->cand_cap : std::max<uint32_t>(128, round_up(E + 32, 32));
+    sh.H = a->hash_slots ? a->hash_slots : (E <= 32 ? 1024u : (E <= 128 ? 2048u : 4096u));
+    const uint32_t wbytes = hg::warp_smem_bytes(sh.H, sh.R, sh.C);
+    sh.wpb = static_cast<int>(std::min<uint32_t>(4, (227u * 1024u) / wbytes));
+    if (a->warps_per_block) sh.wpb = std::min<int>(sh.wpb, static_cast<int>(a->warps_per_block));
+    if (sh.wpb < 1) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
+    const int occ = hg::search_occupancy(static_cast<uint32_t>(g->pd), g->metric, sh.wpb, sh.H, sh.R, sh.C);
+    if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the search kernel cannot be resident with this shape");
+    const uint64_t want = (nq + sh.wpb - 1) / sh.wpb;
+    sh.blocks = static_cast<int>(std::min<uint64_t>(want, static_cast<uint64_t>(g->sms) * occ));
+    sh.slot_base = static_cast<uint32_t>(slots_total);
+    slots_total += static_cast<uint64_t>(sh.blocks) * sh.wpb;
   }
-  const uint32_t wbytes = hg::warp_smem_bytes(P.H, P.R, P.C);
-  int wpb = static_cast<int>(std::min<uint32_t>(4, (227u * 1024u) / wbytes));
-  if (a->warps_per_block) {
-    if (a->warps_per_block > 4) return fail(HGD_EINVAL, "hgd_search: warps_per_block must be 1..4");
-    wpb = std::min<int>(wpb, static_cast<int>(a->warps_per_block));
-  }
-  if (wpb < 1) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
-  const int occ_blocks = hg::search_occupancy(P.pd, g->metric, wpb, P.H, P.R, P.C);
-  if (occ_blocks < 1) return fail(HGD_ECUDA, "hgd_search: the search kernel cannot be resident with this shape");
-  const uint64_t want_blocks = (nq + wpb - 1) / wpb;
-  const int blocks = static_cast<int>(std::min<uint64_t>(want_blocks, static_cast<uint64_t>(g->sms) * occ_blocks));
-  const uint64_t slots = static_cast<uint64_t>(blocks) * wpb;
+  // shared scratch: spill pools and visited bitmaps acquired per query
   const uint64_t bw = (g->n + 31) / 32 + 1;
-  uint64_t pool_cap = std::min<uint64_t>(std::max<uint64_t>(g->n, 1), 8192);
-  if (a->pool_cap) pool_cap = std::max<uint64_t>(a->pool_cap, 32);
-  HG_CUDA(g->pool.ensure(slots * pool_cap * 8));
-  HG_CUDA(g->bitmaps.ensure(slots * bw * 4));
-  HG_CUDA(g->work.ensure(64));
+  const uint64_t pool_cap = a->pool_cap ? std::max<uint64_t>(a->pool_cap, 32)
+                                        : std::min<uint64_t>(std::max<uint64_t>(g->n, 1), 16384);
+  const uint32_t pool_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 1024));
+  const uint32_t bm_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 512));
+  HG_CUDA(g->pool.ensure(pool_slots * pool_cap * 8));
+  HG_CUDA(g->bitmaps.ensure(bm_slots * bw * 4));
+  HG_CUDA(g->owners.ensure((pool_slots + bm_slots) * 4));
+  HG_CUDA(g->work.ensure(64 * 4));
   HG_CUDA(g->ovf_list.ensure(nq * 4));
-  HG_CUDA(cudaMemsetAsync(g->work.p, 0, 64, st));
+  HG_CUDA(g->lists.ensure(static_cast<uint64_t>(spec.n) * nq * 4));
+  HG_CUDA(cudaMemsetAsync(g->work.p, 0, 64 * 4, st));
+  HG_CUDA(cudaMemsetAsync(g->owners.p, 0, (pool_slots + bm_slots) * 4, st));
+  uint32_t* work = g->work.as<uint32_t>();  // [1] overflow count [2] rerun work [4] error
+                                            // [8+b] bucket work  [32+b] bucket size
   P.pool = g->pool.as<uint64_t>();
   P.pool_cap = pool_cap;
+  P.pool_owner = g->owners.as<uint32_t>();
+  P.pool_slots = pool_slots;
   P.bitmaps = g->bitmaps.as<uint32_t>();
   P.bitmap_words = bw;
-  P.work = g->work.as<uint32_t>();
-  P.ovf_count = g->work.as<uint32_t>() + 1;
+  P.bm_owner = g->owners.as<uint32_t>() + pool_slots;
+  P.bm_slots = bm_slots;
+  P.ovf_count = work + 1;
   P.ovf_list = g->ovf_list.as<uint32_t>();
-  P.err = g->work.as<uint32_t>() + 4;
+  P.err = work + 4;
   {
-    cudaError_t e = hg::launch_search(P, d_inv, blocks, wpb, st);
-    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("search kernel launch: ") + cudaGetErrorString(e));
+    cudaError_t e = hg::launch_bucket(d_ef, d_k, static_cast<uint32_t>(nq), a->ef, a->ef_default, a->k, spec,
+                                      work + 32, g->lists.as<uint32_t>(), st);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("bucket kernel launch: ") + cudaGetErrorString(e));
   }
-  // ---- rerun of queries whose spill pool overflowed: pool of n entries ----
+  // fork: each bucket on its own stream, largest ef first, joined back into st
+  if (g->aux.size() < spec.n) {
+    if (!g->ev_fork) HG_CUDA(cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming));
+    while (g->aux.size() < spec.n) {
+      cudaStream_t s2 = nullptr;
+      cudaEvent_t e2 = nullptr;
+      HG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+      HG_CUDA(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+      g->aux.push_back(s2);
+      g->ev_join.push_back(e2);
+    }
+  }
+  HG_CUDA(cudaEventRecord(g->ev_fork, st));
+  for (int b = static_cast<int>(spec.n) - 1; b >= 0; --b) {
+    const Shape& sh = shapes[b];
+    cudaStream_t sb = g->aux[b];
+    HG_CUDA(cudaStreamWaitEvent(sb, g->ev_fork, 0));
+    hg::SearchParams B = P;
+    B.H = sh.H;
+    B.R = sh.R;
+    B.C = sh.C;
+    B.nq_dev = work + 32 + b;
+    B.qidx = g->lists.as<uint32_t>() + static_cast<uint64_t>(b) * nq;
+    B.work = work + 8 + b;
+    B.slot_base = sh.slot_base;
+    cudaError_t e = hg::launch_search(B, d_inv, sh.blocks, sh.wpb, sb);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("search kernel launch: ") + cudaGetErrorString(e));
+    HG_CUDA(cudaEventRecord(g->ev_join[b], sb));
+  }
+  for (uint32_t b = 0; b < spec.n; ++b) HG_CUDA(cudaStreamWaitEvent(st, g->ev_join[b], 0));
+  // ---- rerun of queries that ran out of spill pool or bitmap: per-warp pool of n keys ----
   {
-    const uint64_t big_slots = static_cast<uint64_t>(g->sms);
+    const uint64_t big_slots = 32;
     const uint64_t big_cap = std::max<uint64_t>(g->n, 1);
     HG_CUDA(g->pool_big.ensure(big_slots * big_cap * 8));
     HG_CUDA(g->bitmaps_big.ensure(big_slots * bw * 4));
     hg::SearchParams B = P;
-    B.nq_dev = g->work.as<uint32_t>() + 1;
+    B.R = round_up(ef_max, 32);
+    B.C = std::max<uint32_t>(128, round_up(ef_max + 32, 32));
+    B.H = 4096;
+    B.nq_dev = work + 1;
     B.qidx = g->ovf_list.as<uint32_t>();
-    B.work = g->work.as<uint32_t>() + 2;
+    B.work = work + 2;
     B.pool = g->pool_big.as<uint64_t>();
     B.pool_cap = big_cap;
+    B.pool_owner = nullptr;
     B.bitmaps = g->bitmaps_big.as<uint32_t>();
-    B.ovf_count = g->work.as<uint32_t>() + 3;  // cannot overflow: cap = n
-    B.ovf_list = g->ovf_list.as<uint32_t>();
+    B.bm_owner = nullptr;
+    B.slot_base = 0;
+    B.ovf_count = work + 3;  // cannot overflow: cap = n, one bitmap per warp
+    B.rerun = 1;
+    const uint32_t wb = hg::warp_smem_bytes(B.H, B.R, B.C);
+    if (wb > 227u * 1024u) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
     cudaError_t e = hg::launch_search(B, d_inv, static_cast<int>(big_slots), 1, st);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("rerun kernel launch: ") + cudaGetErrorString(e));
   }

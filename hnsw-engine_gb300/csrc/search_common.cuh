@@ -40,16 +40,33 @@ struct SearchParams {
   uint32_t H;  // visited hash slots (power of two)
   uint32_t R;  // result capacity (>= every ef)
   uint32_t C;  // candidate head capacity (power of two, >= 64)
-  // ---- global scratch, per warp slot ----
-  uint64_t* pool;           // candidate spill pool
-  uint64_t pool_cap;        // entries per slot
-  uint32_t* bitmaps;        // visited bitmap tier
-  uint64_t bitmap_words;    // words per slot
+  // ---- global scratch ----
+  // Spill pools and visited bitmaps are either one per warp slot (owner
+  // arrays null: the rerun pass) or shared: a warp acquires one with a
+  // bounded CAS scan of the owner array when it first needs it and releases
+  // it when its query ends; if none is free the query goes to the rerun list.
+  uint64_t* pool;           // candidate spill pools, pool_cap keys each
+  uint64_t pool_cap;
+  uint32_t* pool_owner;     // [pool_slots] 0 = free
+  uint32_t pool_slots;
+  uint32_t* bitmaps;        // visited bitmaps, bitmap_words each
+  uint64_t bitmap_words;
+  uint32_t* bm_owner;       // [bm_slots] 0 = free
+  uint32_t bm_slots;
+  uint32_t slot_base;       // first warp slot of this launch (per-slot mode)
+  int32_t rerun;            // 1: this launch is the rerun pass (counter flag only)
   uint32_t* work;           // work-queue counter (zeroed before launch)
   uint32_t* ovf_list;       // queries whose pool overflowed
   uint32_t* ovf_count;
   unsigned long long* counters;  // nq x kCounters or null
   uint32_t* err;                 // set to 1 if a per-query ef / k exceeds this launch's capacity
+};
+
+// ef buckets of one batch: queries with effective ef <= hi[b] go to bucket b.
+constexpr int kMaxBuckets = 12;
+struct BucketSpec {
+  uint32_t n;
+  uint32_t hi[kMaxBuckets];
 };
 
 __host__ __device__ inline uint32_t warp_smem_bytes(uint32_t H, uint32_t R, uint32_t C) {

@@ -1,0 +1,17 @@
+// search_dot.cu -- instantiations of the query kernel for the inner-product / cosine metrics (1 - dot).
+#include "search_kernel.cuh"
+
+namespace hg {
+
+cudaError_t launch_search_dot(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st) {
+  const uint32_t pd = P.pd;
+  HG_SEARCH_DISPATCH(sk::launch_t, false, P, inv, blocks, wpb, st)
+  return cudaErrorInvalidValue;
+}
+
+int occupancy_dot(uint32_t pd, int wpb, size_t smem) {
+  HG_SEARCH_DISPATCH(sk::occupancy_t, false, wpb, smem)
+  return 0;
+}
+
+}  // namespace hg

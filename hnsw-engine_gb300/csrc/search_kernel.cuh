@@ -1,4 +1,5 @@
-// search_kernel.cu -- the batched HNSW query path on sm_103a.
+// search_kernel.cuh -- the batched HNSW query kernel (templates; instantiated
+// per metric in search_l2.cu / search_dot.cu).
 //
 // One warp answers one query at a time and pulls the next query from a
 // device work queue (a persistent grid).  Per query it runs exactly the
@@ -31,15 +32,16 @@
 //
 // Shared memory per warp: visited hash (4H B), results (8R B), candidate head
 // (8(C+32) B) and two 32-entry staging arrays.
+#pragma once
+
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "search_common.cuh"
 
 namespace hg {
-namespace {
+namespace sk {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr uint64_t kMaxKey = ~0ull;
@@ -81,7 +83,7 @@ __device__ __forceinline__ float warp_minf(float v) {
   return v;
 }
 
-// number of elements of sorted a[0..n) that are < x
+// number of elements of sorted a[0..n) that are < x (one lane)
 __device__ __forceinline__ int lower_bound(const uint64_t* a, int n, uint64_t x) {
   int lo = 0, hi = n;
   while (lo < hi) {
@@ -92,40 +94,68 @@ __device__ __forceinline__ int lower_bound(const uint64_t* a, int n, uint64_t x)
   return lo;
 }
 
+// The same count for a warp-uniform x, two shared loads and two ballots for
+// n <= 1024: sample every ceil(n/32)-th element, then scan inside the gap.
+__device__ __forceinline__ int warp_rank(const uint64_t* a, int n, uint64_t x, int lane) {
+  if (n <= 0) return 0;
+  if (n > 1024) {
+    int r = 0;
+    for (int base = 0; base < n; base += 32) {
+      const int i = base + lane;
+      const unsigned b = __ballot_sync(kFull, i < n && a[i] < x);
+      r += __popc(b);
+      if (b != kFull) break;
+    }
+    return r;
+  }
+  const int step = (n + 31) >> 5;
+  const int i = lane * step;
+  const int c = __popc(__ballot_sync(kFull, i < n && a[i] < x));
+  if (c == 0) return 0;
+  const int lo = (c - 1) * step;
+  const int j = lo + 1 + lane;
+  return lo + 1 + __popc(__ballot_sync(kFull, lane < step - 1 && j < n && a[j] < x));
+}
+
 // Merge sorted b[0..m) into sorted a[0..n) in place (keys unique), keeping
 // the smallest `cap`.  Returns the new size.  Whole warp, uniform arguments.
-__device__ int warp_merge(uint64_t* a, int n, int cap, const uint64_t* b, int m, int lane) {
+__device__ __forceinline__ int warp_merge(uint64_t* a, int n, int cap, const uint64_t* b, int m, int lane) {
   if (m == 0) return n;
+  // rb (lane j < m): insertion rank of b_j in a
   int rb = 0;
-  uint64_t bj = 0;
-  if (lane < m) {
-    bj = b[lane];
-    rb = lower_bound(a, n, bj);
+  if (m <= 4) {
+    for (int j = 0; j < m; ++j) {
+      const int r = warp_rank(a, n, b[j], lane);
+      if (lane == j) rb = r;
+    }
+  } else if (lane < m) {
+    rb = lower_bound(a, n, b[lane]);
   }
   const int p0 = __shfl_sync(kFull, rb, 0);
+  // a[i] moves up by #{j : rb_j <= i}; top chunks first so nothing unread is overwritten
   for (int top = n; top > p0; top -= 32) {
-    const int p = top - 32 + lane;
+    const int i = top - 32 + lane;
+    const bool live = i >= p0 && i < n;
     uint64_t x = 0;
-    int dst = -1;
-    if (p >= p0 && p < n) {
-      x = a[p];
-      dst = p + lower_bound(b, m, x);
+    if (live) x = a[i];
+    int sh = 0;
+    if (m <= 8) {
+      for (int j = 0; j < m; ++j) sh += __shfl_sync(kFull, rb, j) <= i ? 1 : 0;
+    } else if (live) {
+      sh = lower_bound(b, m, x);
     }
     __syncwarp();
-    if (dst >= 0 && dst < cap) a[dst] = x;
+    if (live && i + sh < cap) a[i + sh] = x;
     __syncwarp();
   }
-  if (lane < m) {
-    const int dst = lane + rb;
-    if (dst < cap) a[dst] = bj;
-  }
+  if (lane < m && rb + lane < cap) a[rb + lane] = b[lane];
   __syncwarp();
   const int t = n + m;
   return t < cap ? t : cap;
 }
 
 // Bitonic sort of a[0..p2) (p2 a power of two) by one warp.
-__device__ void warp_bitonic(uint64_t* a, int p2, int lane) {
+__device__ inline void warp_bitonic(uint64_t* a, int p2, int lane) {
   for (int k = 2; k <= p2; k <<= 1) {
     for (int j = k >> 1; j > 0; j >>= 1) {
       for (int i = lane; i < p2; i += 32) {
@@ -149,21 +179,28 @@ __device__ void warp_bitonic(uint64_t* a, int p2, int lane) {
 //   slot i < nb:        64 i + t        (chain A: acc0 lanes t<16 / acc1 t>=16)
 //   slot nb + i < 2nb:  64 i + 32 + t   (chain B: acc2 / acc3)
 //   slot 2nb + u < 2nb+nt, t < 16: 64 nb + 16 u + t  (16-float blocks -> acc0)
+// NB >= 0 fixes the layout at compile time; NB < 0 reads it from nb / nt.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int slot_elem(int i, int nb, int nt, int lane) {
-  if (i < nb) return 64 * i + lane;
-  if (i < 2 * nb) return 64 * (i - nb) + 32 + lane;
-  const int u = i - 2 * nb;
-  if (u < nt && lane < 16) return 64 * nb + 16 * u + lane;
-  return -1;
-}
+template <int NB, int NT, int S>
+struct Layout {
+  int nb_rt, nt_rt;
+  __device__ __forceinline__ int nb() const { return NB >= 0 ? NB : nb_rt; }
+  __device__ __forceinline__ int nt() const { return NB >= 0 ? NT : nt_rt; }
+  __device__ __forceinline__ int elem(int i, int lane) const {
+    if (i < nb()) return 64 * i + lane;
+    if (i < 2 * nb()) return 64 * (i - nb()) + 32 + lane;
+    const int u = i - 2 * nb();
+    if (u < nt() && lane < 16) return 64 * nb() + 16 * u + lane;
+    return -1;
+  }
+};
 
-template <int S, bool L2>
-__device__ __forceinline__ float combine(const float (&x)[S], const float (&qr)[S], int nb, int nt) {
+template <int NB, int NT, int S, bool L2>
+__device__ __forceinline__ float combine(const Layout<NB, NT, S>& L, const float (&x)[S], const float (&qr)[S]) {
   float a = 0.0f, b = 0.0f;
 #pragma unroll
   for (int i = 0; i < S; ++i) {
-    if (i < nb) {
+    if (i < L.nb()) {
       if (L2) {
         const float d = __fsub_rn(qr[i], x[i]);
         a = __fmaf_rn(d, d, a);
@@ -174,7 +211,7 @@ __device__ __forceinline__ float combine(const float (&x)[S], const float (&qr)[
   }
 #pragma unroll
   for (int i = 0; i < S; ++i) {
-    if (i >= nb && i < 2 * nb) {
+    if (i >= L.nb() && i < 2 * L.nb()) {
       if (L2) {
         const float d = __fsub_rn(qr[i], x[i]);
         b = __fmaf_rn(d, d, b);
@@ -185,7 +222,7 @@ __device__ __forceinline__ float combine(const float (&x)[S], const float (&qr)[
   }
 #pragma unroll
   for (int i = 0; i < S; ++i) {
-    if (i >= 2 * nb && i < 2 * nb + nt) {  // lanes >= 16 hold zeros here
+    if (i >= 2 * L.nb() && i < 2 * L.nb() + L.nt()) {  // lanes >= 16 hold zeros here
       if (L2) {
         const float d = __fsub_rn(qr[i], x[i]);
         a = __fmaf_rn(d, d, a);
@@ -205,50 +242,38 @@ __device__ __forceinline__ float combine(const float (&x)[S], const float (&qr)[
   return L2 ? s : __fsub_rn(1.0f, s);
 }
 
-// Distances from the query to up to G rows (ids; kNoId = unused), all lanes
-// get every result.  All loads are issued before any arithmetic.
-template <int S, int G, bool L2>
-__device__ __forceinline__ void group_dist(const float* __restrict__ vecs, uint32_t pd, const uint32_t (&ids)[G],
-                                           const float (&qr)[S], int nb, int nt, int lane, float (&out)[G]) {
-  float x[G][S];
-#pragma unroll
-  for (int g = 0; g < G; ++g) {
-    const float* row = vecs + static_cast<size_t>(ids[g] == kNoId ? 0u : ids[g]) * pd;
-#pragma unroll
-    for (int i = 0; i < S; ++i) {
-      const int e = slot_elem(i, nb, nt, lane);
-      x[g][i] = (ids[g] != kNoId && e >= 0) ? __ldg(row + e) : 0.0f;
-    }
-  }
-#pragma unroll
-  for (int g = 0; g < G; ++g) out[g] = combine<S, L2>(x[g], qr, nb, nt);
-}
-
-// Distances for the lanes in `mask`; lane j receives the distance of its id.
-template <int S, int G, bool L2>
-__device__ __forceinline__ float lane_dists(const float* __restrict__ vecs, uint32_t pd, uint32_t id, uint32_t mask,
-                                            const float (&qr)[S], int nb, int nt, int lane) {
+// Distances for the lanes in `mask`, G rows in flight; lane j receives the
+// distance of its own id.  All loads of a group are issued before any math.
+template <int NB, int NT, int S, int G, bool L2>
+__device__ __forceinline__ float lane_dists(const Layout<NB, NT, S>& L, const float* __restrict__ vecs, uint32_t pd,
+                                            uint32_t id, uint32_t mask, const float (&qr)[S], int lane) {
   float mine = 0.0f;
   while (mask) {
-    uint32_t gid[G];
     int gl[G];
+    const float* rows[G];
 #pragma unroll
     for (int g = 0; g < G; ++g) {
-      if (mask) {
-        const int l = __ffs(mask) - 1;
-        mask &= mask - 1;
-        gl[g] = l;
-      } else {
-        gl[g] = -1;
-      }
-      gid[g] = __shfl_sync(kFull, id, gl[g] < 0 ? 0 : gl[g]);
-      if (gl[g] < 0) gid[g] = kNoId;
+      gl[g] = mask ? __ffs(mask) - 1 : -1;
+      if (mask) mask &= mask - 1;
+      const uint32_t gid = __shfl_sync(kFull, id, gl[g] < 0 ? 0 : gl[g]);
+      rows[g] = gl[g] < 0 ? nullptr : vecs + static_cast<size_t>(gid) * pd;
     }
-    float gd[G];
-    group_dist<S, G, L2>(vecs, pd, gid, qr, nb, nt, lane, gd);
+    float x[G][S];
 #pragma unroll
-    for (int g = 0; g < G; ++g)
-      if (gl[g] == lane) mine = gd[g];
+    for (int g = 0; g < G; ++g) {
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        const int e = L.elem(i, lane);
+        x[g][i] = (rows[g] != nullptr && e >= 0) ? __ldg(rows[g] + e) : 0.0f;
+      }
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (gl[g] >= 0) {  // warp-uniform
+        const float d = combine<NB, NT, S, L2>(L, x[g], qr);
+        if (gl[g] == lane) mine = d;
+      }
+    }
   }
   return mine;
 }
@@ -262,14 +287,48 @@ struct Warp {
   uint64_t* cand;
   uint64_t* stA;
   uint64_t* stE;
-  uint64_t* pool;     // this slot's spill pool
-  uint32_t* bitmap;   // this slot's visited bitmap
+  uint64_t* pool;     // spill pool in use (null until the first spill)
+  uint32_t* bitmap;   // visited bitmap in use
+  uint64_t slot;      // global warp slot
+  int pool_idx;       // acquired shared pool (-1 none)
+  int bm_idx;         // acquired shared bitmap (-1 none)
   uint32_t hmask;
   int hshift;
   uint32_t tag;       // epoch << 24 (tagged mode)
   uint32_t vcount;    // visited entries in the hash
   bool bitmap_mode;
 };
+
+// Claim a free entry of a shared scratch array: one bounded pass over the
+// owner flags from a slot-dependent start (never waits).  -1 if all are taken.
+__device__ __forceinline__ int acquire(uint32_t* owner, uint32_t nslots, uint64_t slot, int lane) {
+  int got = -1;
+  if (lane == 0) {
+    const uint32_t start = static_cast<uint32_t>((slot * 2654435761ull) % nslots);
+    for (uint32_t t = 0; t < nslots; ++t) {
+      uint32_t i = start + t;
+      if (i >= nslots) i -= nslots;
+      if (atomicCAS(owner + i, 0u, 1u) == 0u) {
+        got = static_cast<int>(i);
+        break;
+      }
+    }
+  }
+  return __shfl_sync(kFull, got, 0);
+}
+
+// Give back the shared scratch a query held (its writes are complete first).
+__device__ __forceinline__ void release_scratch(Warp& w, const SearchParams& P, int lane) {
+  __syncwarp();
+  __threadfence();
+  if (lane == 0) {
+    if (w.pool_idx >= 0) atomicExch(P.pool_owner + w.pool_idx, 0u);
+    if (w.bm_idx >= 0) atomicExch(P.bm_owner + w.bm_idx, 0u);
+  }
+  w.pool_idx = -1;
+  w.bm_idx = -1;
+  w.pool = nullptr;
+}
 
 __device__ __forceinline__ bool hash_empty(uint32_t v, uint32_t tag, bool tagged) {
   return tagged ? ((v & 0xFF000000u) != tag) : (v == kNoId);
@@ -297,12 +356,19 @@ __device__ __forceinline__ bool visit(Warp& w, uint32_t id, bool tagged) {
   }
 }
 
-// Move the visited set from the hash to this slot's bitmap.
-__device__ void to_bitmap(Warp& w, const SearchParams& P, bool tagged, int lane) {
+// Move the visited set from the hash to a bitmap (false: none available).
+__device__ __forceinline__ bool to_bitmap(Warp& w, const SearchParams& P, bool tagged, int lane) {
   const uint64_t words = P.bitmap_words;
+  if (P.bm_owner) {
+    const int i = acquire(P.bm_owner, P.bm_slots, w.slot, lane);
+    if (i < 0) return false;
+    w.bm_idx = i;
+    w.bitmap = P.bitmaps + static_cast<uint64_t>(i) * words;
+  } else {
+    w.bitmap = P.bitmaps + w.slot * words;
+  }
   for (uint64_t i = lane; i < words; i += 32) w.bitmap[i] = 0u;
   __syncwarp();
-  __threadfence_block();
   for (uint32_t p = lane; p <= w.hmask; p += 32) {
     const uint32_t v = w.hash[p];
     if (!hash_empty(v, w.tag, tagged)) {
@@ -310,9 +376,9 @@ __device__ void to_bitmap(Warp& w, const SearchParams& P, bool tagged, int lane)
       atomicOr(&w.bitmap[id >> 5], 1u << (id & 31u));
     }
   }
-  __threadfence_block();
   __syncwarp();
   w.bitmap_mode = true;
+  return true;
 }
 
 __device__ __forceinline__ bool bit_of(const uint32_t* bits, uint32_t id) {
@@ -320,7 +386,7 @@ __device__ __forceinline__ bool bit_of(const uint32_t* bits, uint32_t id) {
 }
 
 // Radix select: the r-th smallest (1-based) of pool[0..pn).  hist: 256 u32 in smem.
-__device__ uint64_t radix_select(const uint64_t* pool, uint64_t pn, uint64_t r, uint32_t* hist, int lane) {
+__device__ inline uint64_t radix_select(const uint64_t* pool, uint64_t pn, uint64_t r, uint32_t* hist, int lane) {
   uint64_t prefix = 0, pmask = 0;
   for (int shift = 56; shift >= 0; shift -= 8) {
     for (int i = lane; i < 256; i += 32) hist[i] = 0u;
@@ -330,7 +396,6 @@ __device__ uint64_t radix_select(const uint64_t* pool, uint64_t pn, uint64_t r, 
       if ((x & pmask) == prefix) atomicAdd(&hist[(x >> shift) & 255u], 1u);
     }
     __syncwarp();
-    // lane l owns bins 8l..8l+7
     uint32_t c[8];
     uint32_t tot = 0;
 #pragma unroll
@@ -346,8 +411,7 @@ __device__ uint64_t radix_select(const uint64_t* pool, uint64_t pn, uint64_t r, 
     }
     const uint32_t excl = incl - tot;
     const bool here = excl < r && r <= incl;
-    const uint32_t owner_mask = __ballot_sync(kFull, here);
-    const int owner = __ffs(owner_mask) - 1;
+    const int owner = __ffs(__ballot_sync(kFull, here)) - 1;
     uint32_t bucket = 0, before = 0;
     if (lane == owner) {
       uint32_t cum = excl;
@@ -374,27 +438,41 @@ __device__ uint64_t radix_select(const uint64_t* pool, uint64_t pn, uint64_t r, 
 // Candidate queue: head = sorted cand[ch, ct) in smem, pool = unsorted spill.
 struct Cands {
   int ch, ct;
-  uint64_t pn;       // pool entries
-  uint64_t pmin;     // min key in pool (kMaxKey if empty)
-  uint64_t peak;     // largest head + pool size seen
+  uint64_t pn;    // pool entries
+  uint64_t pmin;  // min key in pool (kMaxKey if empty)
+  uint32_t peak;  // largest head + pool size seen
   bool overflow;
 };
 
-__device__ __forceinline__ bool pool_append(Warp& w, Cands& c, const uint64_t* src, int cnt, uint64_t cap, int lane) {
+__device__ __forceinline__ bool pool_append(Warp& w, Cands& c, const SearchParams& P, const uint64_t* src, int cnt,
+                                            int lane) {
   if (cnt <= 0) return true;
-  if (c.pn + static_cast<uint64_t>(cnt) > cap) {
+  if (c.pn + static_cast<uint64_t>(cnt) > P.pool_cap) {
     c.overflow = true;
     return false;
+  }
+  if (w.pool == nullptr) {
+    if (P.pool_owner) {
+      const int i = acquire(P.pool_owner, P.pool_slots, w.slot, lane);
+      if (i < 0) {
+        c.overflow = true;
+        return false;
+      }
+      w.pool_idx = i;
+      w.pool = P.pool + static_cast<uint64_t>(i) * P.pool_cap;
+    } else {
+      w.pool = P.pool + w.slot * P.pool_cap;
+    }
   }
   if (lane < cnt) w.pool[c.pn + lane] = src[lane];
   c.pn += cnt;
   return true;
 }
 
-// Refill an empty head from the pool with its smallest C/2 keys; when the
-// result set is full, first drop pool keys farther than the worst result.
-__device__ void refill(Warp& w, Cands& c, const SearchParams& P, bool res_full, float worst_d, int lane) {
-  __threadfence_block();
+// Refill an empty head from the pool with its smallest keys (at most C/2);
+// when the result set is full, first drop pool keys farther than the worst.
+__device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P, bool res_full, float worst_d, int lane) {
+  __syncwarp();
   if (res_full) {
     uint64_t wpos = 0;
     for (uint64_t base = 0; base < c.pn; base += 32) {
@@ -421,7 +499,6 @@ __device__ void refill(Warp& w, Cands& c, const SearchParams& P, bool res_full, 
   uint64_t T = kMaxKey;
   if (c.pn > take) T = radix_select(w.pool, c.pn, take, reinterpret_cast<uint32_t*>(w.cand), lane);
   __syncwarp();
-  // split: keys <= T to the head, the rest stay (compacted) in the pool
   uint64_t hpos = 0, wpos = 0, newmin = kMaxKey;
   for (uint64_t base = 0; base < c.pn; base += 32) {
     const uint64_t i = base + lane;
@@ -452,18 +529,17 @@ __device__ void refill(Warp& w, Cands& c, const SearchParams& P, bool res_full, 
   c.ct = static_cast<int>(hpos);
   c.pn = wpos;
   c.pmin = wpos ? newmin : kMaxKey;
-  __threadfence_block();
 }
 
 // Insert the sorted accepted batch stA[0..m) into the candidate queue.
-// res_full / worst_d: once the result set is full, head keys farther than the
-// worst result are dropped before anything would spill to the pool.
-__device__ void cand_insert(Warp& w, Cands& c, const SearchParams& P, int m, bool res_full, float worst_d,
+// Once the result set is full, head keys farther than the worst result are
+// dropped before anything would spill to the pool.
+__device__ __forceinline__ void cand_insert(Warp& w, Cands& c, const SearchParams& P, int m, bool res_full, float worst_d,
                             int lane) {
   if (m <= 0) return;
-  if (res_full && c.ct - c.ch + m > static_cast<int>(P.C) - c.ch) {
-    // first head index whose distance exceeds the worst result
-    int lo = c.ch, hi = c.ct;
+  const int C = static_cast<int>(P.C);
+  if (res_full && c.ct + m > C) {
+    int lo = c.ch, hi = c.ct;  // first head key farther than the worst result
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
       if (key_dist(w.cand[mid]) > worst_d) hi = mid;
@@ -473,15 +549,14 @@ __device__ void cand_insert(Warp& w, Cands& c, const SearchParams& P, int m, boo
   }
   int mh = m;
   if (c.pn > 0) {
-    const bool lt = lane < m && w.stA[lane] < c.pmin;
-    mh = __popc(__ballot_sync(kFull, lt));
-    if (m > mh && !pool_append(w, c, w.stA + mh, m - mh, P.pool_cap, lane)) return;
+    mh = __popc(__ballot_sync(kFull, lane < m && w.stA[lane] < c.pmin));
+    if (m > mh && !pool_append(w, c, P, w.stA + mh, m - mh, lane)) return;
   }
   if (mh > 0) {
     const int n = c.ct - c.ch;
-    const int nn = warp_merge(w.cand + c.ch, n, static_cast<int>(P.C) + 32 - c.ch, w.stA, mh, lane);
+    const int nn = warp_merge(w.cand + c.ch, n, C + 32 - c.ch, w.stA, mh, lane);
     c.ct = c.ch + nn;
-    if (c.ct > static_cast<int>(P.C)) {
+    if (c.ct > C) {
       if (c.ch > 0) {  // compact to the front
         const int len = c.ct - c.ch;
         for (int base = 0; base < len; base += 32) {
@@ -495,17 +570,17 @@ __device__ void cand_insert(Warp& w, Cands& c, const SearchParams& P, int m, boo
         c.ct = len;
         c.ch = 0;
       }
-      if (c.ct > static_cast<int>(P.C)) {  // spill the largest keys
-        const int cnt = c.ct - static_cast<int>(P.C);
-        const uint64_t first = w.cand[P.C];
-        if (!pool_append(w, c, w.cand + P.C, cnt, P.pool_cap, lane)) return;
+      if (c.ct > C) {  // spill the largest keys
+        const int cnt = c.ct - C;
+        const uint64_t first = w.cand[C];
+        if (!pool_append(w, c, P, w.cand + C, cnt, lane)) return;
         c.pmin = first < c.pmin ? first : c.pmin;
-        c.ct = static_cast<int>(P.C);
+        c.ct = C;
       }
     }
   }
   const uint64_t total = static_cast<uint64_t>(c.ct - c.ch) + c.pn;
-  c.peak = total > c.peak ? total : c.peak;
+  c.peak = total > c.peak ? static_cast<uint32_t>(total) : c.peak;
 }
 
 struct QueryOut {
@@ -517,23 +592,24 @@ struct QueryOut {
 // ---------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------
-template <int S, int G, bool L2>
+template <int NB, int NT, int S, int G, bool L2>
 __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float* __restrict__ inv_norm) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const uint32_t per_warp = warp_smem_bytes(P.H, P.R, P.C);
   unsigned char* base = smem + static_cast<size_t>(wib) * per_warp;
-  const uint64_t slot = static_cast<uint64_t>(blockIdx.x) * (blockDim.x >> 5) + wib;
-
   Warp w;
+  w.slot = P.slot_base + static_cast<uint64_t>(blockIdx.x) * (blockDim.x >> 5) + wib;
   w.hash = reinterpret_cast<uint32_t*>(base);
   w.res = reinterpret_cast<uint64_t*>(base + 4u * P.H);
   w.cand = w.res + P.R;
   w.stA = w.cand + P.C + 32;
   w.stE = w.stA + 32;
-  w.pool = P.pool + slot * P.pool_cap;
-  w.bitmap = P.bitmaps + slot * P.bitmap_words;
+  w.pool = nullptr;
+  w.bitmap = nullptr;
+  w.pool_idx = -1;
+  w.bm_idx = -1;
   w.hmask = P.H - 1;
   w.hshift = 32 - (31 - __clz(P.H));
   const bool tagged = P.tagged != 0;
@@ -541,9 +617,9 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
   for (uint32_t i = lane; i < P.H; i += 32) w.hash[i] = tagged ? 0u : kNoId;
   __syncwarp();
 
-  const int nb = static_cast<int>(P.pd / 64);
-  const int nt = static_cast<int>((P.pd % 64) / 16);
+  Layout<NB, NT, S> L{static_cast<int>(P.pd / 64), static_cast<int>((P.pd % 64) / 16)};
   const uint32_t nq = P.nq_dev ? *P.nq_dev : P.nq;
+  const bool single_chunk = P.M0 <= 32;
 
   for (;;) {
     uint32_t item = 0;
@@ -561,13 +637,14 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
       if (lane == 0) atomicExch(P.err, 1u);
       continue;
     }
+    const int efi = static_cast<int>(ef);
     const uint32_t* fb = nullptr;
     if (P.fsel) {
       const int32_t f = P.fsel[q];
       if (f >= 0) fb = P.fbits[f];
     }
     const bool filtered = fb != nullptr || P.deleted_any != 0;
-    unsigned long long cnt[kCounters] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t n_uplists = 0, n_updists = 0, n_lists = 0, n_dists = 0, n_visit = 0;
 
     int s = 0;  // result count
     Cands c{0, 0, 0, kMaxKey, 0, false};
@@ -578,7 +655,7 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
       float qr[S];
 #pragma unroll
       for (int i = 0; i < S; ++i) {
-        const int e = slot_elem(i, nb, nt, lane);
+        const int e = L.elem(i, lane);
         const float v = (e >= 0 && e < static_cast<int>(P.dim)) ? __ldg(raw + e) : 0.0f;
         qr[i] = inv_norm ? __fmul_rn(v, inv) : v;
       }
@@ -600,22 +677,22 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
 
       // ---- entry point + greedy descent (search_layer.cpp:29-56,156-157) ----
       uint32_t cur = P.entry;
-      float cur_d = lane_dists<S, G, L2>(P.vecs, P.pd, cur, 1u, qr, nb, nt, lane);
+      float cur_d = lane_dists<NB, NT, S, G, L2>(L, P.vecs, P.pd, cur, 1u, qr, lane);
       cur_d = __shfl_sync(kFull, cur_d, 0);
-      cnt[1]++;
+      n_updists = 1;
       for (int lc = P.max_level; lc > 0; --lc) {
         bool changed = true;
         while (changed) {
           changed = false;
-          const uint32_t* lst = P.up + static_cast<size_t>(P.up_blk[cur] + (lc - 1)) * P.up_stride;
-          cnt[0]++;
+          const uint32_t* lst = P.up + static_cast<size_t>(__ldg(P.up_blk + cur) + (lc - 1)) * P.up_stride;
+          ++n_uplists;
           for (uint32_t c0 = 0; c0 < P.M; c0 += 32) {
             const uint32_t j = c0 + lane;
             const uint32_t id = j < P.M ? __ldg(lst + j) : kNoId;
             const uint32_t vm = __ballot_sync(kFull, id != kNoId);
             if (!vm) break;
-            cnt[1] += __popc(vm);
-            const float d = lane_dists<S, G, L2>(P.vecs, P.pd, id, vm, qr, nb, nt, lane);
+            n_updists += __popc(vm);
+            const float d = lane_dists<NB, NT, S, G, L2>(L, P.vecs, P.pd, id, vm, qr, lane);
             const float m = warp_minf(id != kNoId ? d : __int_as_float(0x7f800000));
             if (m < cur_d) {
               const uint32_t hit = __ballot_sync(kFull, id != kNoId && d == m);
@@ -632,38 +709,52 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
       if (lane == 0) visit(w, cur, tagged);
       __syncwarp();
       w.vcount = 1;
-      cnt[4] = 1;
+      n_visit = 1;
       const uint64_t k0 = mkkey(cur_d, cur);
+      const bool e0 = !filtered || (bit_of(P.alive, cur) && (!fb || bit_of(fb, cur)));
       if (lane == 0) {
         w.cand[0] = k0;
-        if (!filtered || (bit_of(P.alive, cur) && (!fb || bit_of(fb, cur)))) w.res[0] = k0;
+        if (e0) w.res[0] = k0;
       }
       c.ct = 1;
       c.peak = 1;
-      if (!filtered || (bit_of(P.alive, cur) && (!fb || bit_of(fb, cur)))) s = 1;
+      s = e0 ? 1 : 0;
       __syncwarp();
 
       const uint32_t hlimit = (P.H * 5u) / 8u;
+      uint32_t pf_cid = kNoId, pf_id = kNoId;  // adjacency of the next head, loaded ahead
       for (;;) {
         if (c.ch == c.ct) {
           if (c.pn == 0) break;
-          const bool full = s >= static_cast<int>(ef);
+          const bool full = s >= efi;
           refill(w, c, P, full, full ? key_dist(w.res[s - 1]) : 0.0f, lane);
           if (c.ch == c.ct) break;
         }
         const uint64_t top = w.cand[c.ch];
-        if (s >= static_cast<int>(ef) && key_dist(top) > key_dist(w.res[s - 1])) break;
+        if (s >= efi && key_dist(top) > key_dist(w.res[s - 1])) break;
         c.ch++;
         const uint32_t cid = static_cast<uint32_t>(top);
         const uint32_t* lst = P.l0 + static_cast<size_t>(cid) * P.l0_stride;
-        cnt[2]++;
+        ++n_lists;
         for (uint32_t c0 = 0; c0 < P.M0; c0 += 32) {
           const uint32_t j = c0 + lane;
-          const uint32_t id = j < P.M0 ? __ldg(lst + j) : kNoId;
+          uint32_t id;
+          if (c0 == 0 && cid == pf_cid) id = pf_id;
+          else id = j < P.M0 ? __ldg(lst + j) : kNoId;
+          if (c0 == 0 && single_chunk) {
+            // load the list of the next head while this one is expanded
+            pf_cid = c.ch < c.ct ? static_cast<uint32_t>(w.cand[c.ch]) : kNoId;
+            if (pf_cid != kNoId) pf_id = lane < static_cast<int>(P.M0)
+                                             ? __ldg(P.l0 + static_cast<size_t>(pf_cid) * P.l0_stride + lane)
+                                             : kNoId;
+          }
           const bool valid = id != kNoId;
           const uint32_t vm = __ballot_sync(kFull, valid);
           if (!vm) break;
-          if (!w.bitmap_mode && w.vcount + __popc(vm) > hlimit) to_bitmap(w, P, tagged, lane);
+          if (!w.bitmap_mode && w.vcount + __popc(vm) > hlimit && !to_bitmap(w, P, tagged, lane)) {
+            c.overflow = true;  // no bitmap free: the rerun pass answers this query
+            break;
+          }
           bool first = valid;
           if (P.dedup && valid) {
             const uint32_t same = __match_any_sync(vm, id);
@@ -673,55 +764,49 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
           if (first) fresh = !visit(w, id, tagged);
           __syncwarp();
           uint32_t U = __ballot_sync(kFull, fresh);
-          w.vcount += __popc(U);
-          cnt[4] += __popc(U);
+          const int nu = __popc(U);
+          w.vcount += nu;
+          n_visit += nu;
           if (!U) continue;
-          cnt[3] += __popc(U);
-          const float d = lane_dists<S, G, L2>(P.vecs, P.pd, id, U, qr, nb, nt, lane);
+          n_dists += nu;
+          const float d = lane_dists<NB, NT, S, G, L2>(L, P.vecs, P.pd, id, U, qr, lane);
           bool elig = true;
           if (filtered && fresh) elig = bit_of(P.alive, id) && (!fb || bit_of(fb, id));
           const uint64_t key = mkkey(d, id);
 
-          // ---- in-order acceptance replay ----
-          const int s0 = s;
+          // ---- in-order acceptance replay (search_layer.cpp:112-132) ----
           uint32_t acc = 0, ins = 0, inres = 0;
-          int scur = s0, r = s0 - 1;
+          int scur = s, r = s - 1;  // r: largest original result not yet evicted
+          uint64_t maxI = 0;        // largest inserted key still in the results
           float worst_d = 0.0f;
-          if (s0 >= static_cast<int>(ef)) {
-            worst_d = key_dist(w.res[s0 - 1]);
-            U &= __ballot_sync(kFull, d < worst_d);
+          if (s >= efi) {
+            worst_d = key_dist(w.res[s - 1]);
+            U &= __ballot_sync(kFull, d < worst_d);  // worst only decreases
           }
           while (U) {
             const int jl = __ffs(U) - 1;
             U &= U - 1;
             const float dj = __shfl_sync(kFull, d, jl);
-            const bool ej = __shfl_sync(kFull, elig, jl);
-            const bool a = scur < static_cast<int>(ef) || dj < worst_d;
-            if (!a) continue;
+            if (!(scur < efi || dj < worst_d)) continue;
             acc |= 1u << jl;
-            if (!ej) continue;
+            if (!__shfl_sync(kFull, elig, jl)) continue;
+            const uint64_t kj = shfl64(key, jl);
             ins |= 1u << jl;
             inres |= 1u << jl;
-            if (scur < static_cast<int>(ef)) {
-              ++scur;
-              if (scur == static_cast<int>(ef)) {
-                const uint64_t mi = warp_max64((inres >> lane) & 1u ? key : 0ull);
-                const uint64_t rr = r >= 0 ? w.res[r] : 0ull;
-                worst_d = key_dist(rr > mi ? rr : mi);
-              }
-            } else {
-              uint64_t mi = warp_max64((inres >> lane) & 1u ? key : 0ull);
+            maxI = kj > maxI ? kj : maxI;
+            if (scur < efi) {
+              if (++scur < efi) continue;
+            } else {  // evict the largest of res[0..r] and the inserted keys
               const uint64_t rr = r >= 0 ? w.res[r] : 0ull;
-              if (rr > mi) {
+              if (rr > maxI) {
                 --r;
               } else {
-                const uint32_t who = __ballot_sync(kFull, ((inres >> lane) & 1u) && key == mi);
-                inres &= ~who;
+                inres &= ~__ballot_sync(kFull, ((inres >> lane) & 1u) && key == maxI);
+                maxI = warp_max64((inres >> lane) & 1u ? key : 0ull);
               }
-              mi = warp_max64((inres >> lane) & 1u ? key : 0ull);
-              const uint64_t r2 = r >= 0 ? w.res[r] : 0ull;
-              worst_d = key_dist(r2 > mi ? r2 : mi);
             }
+            const uint64_t rr = r >= 0 ? w.res[r] : 0ull;
+            worst_d = key_dist(rr > maxI ? rr : maxI);
           }
           if (!acc) continue;
 
@@ -732,8 +817,7 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
             while (it) {
               const int i = __ffs(it) - 1;
               it &= it - 1;
-              const uint64_t ki = shfl64(key, i);
-              const bool lt = ki < key;
+              const bool lt = shfl64(key, i) < key;
               rA += lt;
               rE += lt && ((ins >> i) & 1u);
             }
@@ -742,9 +826,9 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
             __syncwarp();
           }
           const int mA = __popc(acc), mE = __popc(ins);
-          s = warp_merge(w.res, s, static_cast<int>(ef), w.stE, mE, lane);
+          s = warp_merge(w.res, s, efi, w.stE, mE, lane);
           int mAk = mA;
-          const bool full = s >= static_cast<int>(ef);
+          const bool full = s >= efi;
           const float wd = full ? key_dist(w.res[s - 1]) : 0.0f;
           if (full) mAk = __popc(__ballot_sync(kFull, lane < mA && key_dist(w.stA[lane]) <= wd));
           cand_insert(w, c, P, mAk, full, wd, lane);
@@ -754,6 +838,8 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
       }
     }
 
+    const bool used_bitmap = w.bitmap_mode;
+    release_scratch(w, P, lane);
     if (c.overflow) {
       if (lane == 0) {
         const uint32_t o = atomicAdd(P.ovf_count, 1u);
@@ -780,227 +866,65 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
     }
     if (P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
     if (P.counters && lane == 0) {
-      cnt[5] = c.peak;
-      cnt[6] = static_cast<unsigned long long>(s);
-      cnt[7] = (w.bitmap_mode ? kTierBitmap : 0u) | (c.peak > P.C ? kTierPool : 0u) | (P.qidx ? kTierRerun : 0u);
-      for (int i = 0; i < kCounters; ++i) P.counters[static_cast<size_t>(q) * kCounters + i] = cnt[i];
+      unsigned long long* cp = P.counters + static_cast<size_t>(q) * kCounters;
+      cp[0] = n_uplists;
+      cp[1] = n_updists;
+      cp[2] = n_lists;
+      cp[3] = n_dists;
+      cp[4] = n_visit;
+      cp[5] = c.peak;
+      cp[6] = static_cast<unsigned long long>(s);
+      cp[7] = (used_bitmap ? kTierBitmap : 0u) | (c.peak > P.C ? kTierPool : 0u) | (P.rerun ? kTierRerun : 0u);
     }
     __syncwarp();
   }
 }
 
-// Cosine: inv_norm[q] = float(1 / sqrt(sum in double, in order)) (space.hpp:31-40).
-__global__ void inv_norm_kernel(const float* __restrict__ qs, uint32_t nq, uint32_t dim, float* __restrict__ out) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq) return;
-  const float* x = qs + static_cast<size_t>(q) * dim;
-  double norm = 0.0;
-  for (uint32_t i = 0; i < dim; ++i) {
-    const double v = static_cast<double>(x[i]);
-    norm = __dadd_rn(norm, __dmul_rn(v, v));
-  }
-  out[q] = norm > 0.0 ? __double2float_rn(1.0 / sqrt(norm)) : 1.0f;
-}
-
-template <int S, int G>
-cudaError_t launch_s(const SearchParams& P, const float* inv, int blocks, int threads, size_t smem, cudaStream_t st) {
-  if (P.metric == 0) {
-    auto* fn = search_kernel<S, G, true>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    fn<<<blocks, threads, smem, st>>>(P, inv);
-  } else {
-    auto* fn = search_kernel<S, G, false>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    fn<<<blocks, threads, smem, st>>>(P, inv);
-  }
+// Host-side launch / occupancy for one instantiation.
+template <int NB, int NT, int S, int G, bool L2>
+cudaError_t launch_t(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st) {
+  const size_t smem = static_cast<size_t>(wpb) * warp_smem_bytes(P.H, P.R, P.C);
+  auto* fn = search_kernel<NB, NT, S, G, L2>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  fn<<<blocks, 32 * wpb, smem, st>>>(P, inv);
   return cudaGetLastError();
 }
 
-// Label-space BitsetFilter words -> id-space bits: bit id set iff
-// labels[id] < num_bits and that label's bit is set (filter.hpp:39-41).
-__global__ void translate_filter_kernel(const uint64_t* __restrict__ words, uint64_t num_bits,
-                                        const uint64_t* __restrict__ labels, uint32_t n, uint32_t* __restrict__ out,
-                                        uint32_t out_words) {
-  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= out_words) return;
-  uint32_t bits = 0;
-  for (uint32_t b = 0; b < 32; ++b) {
-    const uint64_t id = static_cast<uint64_t>(w) * 32 + b;
-    if (id >= n) break;
-    const uint64_t l = labels[id];
-    if (l < num_bits && ((words[l >> 6] >> (l & 63)) & 1ull)) bits |= 1u << b;
-  }
-  out[w] = bits;
-}
-
-template <int S, int G>
-int occupancy_s(int metric, int threads, size_t smem) {
+template <int NB, int NT, int S, int G, bool L2>
+int occupancy_t(int wpb, size_t smem) {
   int blocks = 0;
-  if (metric == 0) {
-    auto* fn = search_kernel<S, G, true>;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
-      return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess) return 0;
-  } else {
-    auto* fn = search_kernel<S, G, false>;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
-      return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess) return 0;
-  }
+  auto* fn = search_kernel<NB, NT, S, G, L2>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 32 * wpb, smem) != cudaSuccess) return 0;
   return blocks;
 }
 
-}  // namespace
-
-// Query slots per lane for padded dim pd (AVX-512 layout).
-int slots_for(uint32_t pd) { return 2 * static_cast<int>(pd / 64) + static_cast<int>((pd % 64) / 16); }
-
-cudaError_t launch_inv_norm(const float* qs, uint32_t nq, uint32_t dim, float* out, cudaStream_t st) {
-  if (nq == 0) return cudaSuccess;
-  inv_norm_kernel<<<(nq + 127) / 128, 128, 0, st>>>(qs, nq, dim, out);
-  return cudaGetLastError();
-}
-
-// Returns cudaErrorInvalidValue for a padded dimension beyond the register layouts.
-cudaError_t launch_search(const SearchParams& P, const float* inv, int blocks, int warps_per_block,
-                          cudaStream_t st) {
-  const size_t smem = static_cast<size_t>(warps_per_block) * warp_smem_bytes(P.H, P.R, P.C);
-  const int threads = 32 * warps_per_block;
-  const int S = slots_for(P.pd);
-  if (S <= 5) return launch_s<5, 8>(P, inv, blocks, threads, smem, st);
-  if (S <= 9) return launch_s<9, 4>(P, inv, blocks, threads, smem, st);
-  if (S <= 17) return launch_s<17, 2>(P, inv, blocks, threads, smem, st);
-  if (S <= 33) return launch_s<33, 1>(P, inv, blocks, threads, smem, st);
-  return cudaErrorInvalidValue;
-}
-
-}  // namespace hg
-
-namespace hg {
-
-cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bits, const uint64_t* labels, uint32_t n,
-                                    uint32_t* out, cudaStream_t st) {
-  const uint32_t out_words = (n + 31) / 32 + 1;
-  translate_filter_kernel<<<(out_words + 255) / 256, 256, 0, st>>>(label_words, num_bits, labels, n, out, out_words);
-  return cudaGetLastError();
-}
-
-// Resident blocks per SM of the search kernel for this shape (0 on error).
-int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, uint32_t R, uint32_t C) {
-  const size_t smem = static_cast<size_t>(warps_per_block) * warp_smem_bytes(H, R, C);
-  const int threads = 32 * warps_per_block;
-  const int S = slots_for(pd);
-  if (S <= 5) return occupancy_s<5, 8>(metric, threads, smem);
-  if (S <= 9) return occupancy_s<9, 4>(metric, threads, smem);
-  if (S <= 17) return occupancy_s<17, 2>(metric, threads, smem);
-  if (S <= 33) return occupancy_s<33, 1>(metric, threads, smem);
-  return 0;
-}
-
-}  // namespace hg
-
-// ---------------------------------------------------------------------------
-// Batches that allocate nothing.
-//
-// Some callers cannot call cudaMalloc while they search: a serving process
-// that hands the GPU to other work under a fixed memory budget, code running
-// inside a region where allocation would synchronise the device or is
-// forbidden, or a host framework that owns every device allocation itself.
-// For them the search kernel also runs with its scratch (work counters, spill
-// pools, visited bitmaps, the rerun list and the cosine norms) placed in the
-// file-scope array below instead of buffers the library allocates.  Every
-// GPU that loads the library holds this array (about 15.4 MiB) until the
-// process exits.
-// ---------------------------------------------------------------------------
-namespace hg {
-namespace {
-
-constexpr uint32_t kNaMaxNodes = 1u << 20;    // largest graph
-constexpr uint32_t kNaMaxQueries = 1u << 16;  // largest batch
-constexpr uint32_t kNaMaxEf = 512;            // largest ef (after max(ef, k))
-constexpr int kNaWarpsPerBlock = 4;
-constexpr int kNaBlocks = 12;
-constexpr uint64_t kNaSlots = static_cast<uint64_t>(kNaWarpsPerBlock) * kNaBlocks;
-constexpr uint64_t kNaPoolCap = 2048;                    // spill keys per warp before the rerun pass
-constexpr uint64_t kNaBitmapWords = kNaMaxNodes / 32 + 1;
-
-// byte layout of the array
-constexpr size_t kNaOffCounters = 0;  // u32: [0] work, [1] overflow count, [2] rerun work, [3] spare, [4] error
-constexpr size_t kNaOffOvf = 256;
-constexpr size_t kNaOffInv = kNaOffOvf + 4ull * kNaMaxQueries;
-constexpr size_t kNaOffPool = kNaOffInv + 4ull * kNaMaxQueries;
-constexpr size_t kNaOffBitmaps = kNaOffPool + 8ull * kNaSlots * kNaPoolCap;
-constexpr size_t kNaOffBigPool = kNaOffBitmaps + 4ull * kNaSlots * kNaBitmapWords;
-constexpr size_t kNaOffBigBitmap = kNaOffBigPool + 8ull * kNaMaxNodes;
-constexpr size_t kNaBytes = kNaOffBigBitmap + 4ull * kNaBitmapWords;
-static_assert(kNaOffPool % 8 == 0 && kNaOffBigPool % 8 == 0, "8-byte keys need 8-byte alignment");
-
-static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
-
-std::mutex g_na_mutex;
-void* g_na_address[64] = {};
-
-// Device address of the array on the current device, looked up once per
-// device (host code cannot use the symbol itself as a device pointer).
-cudaError_t noalloc_scratch(int device, unsigned char** out) {
-  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (g_na_address[device] == nullptr) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_na_address[device] = p;
+// Dispatch on the padded dimension: fixed layouts for common dims, the
+// runtime layout (S slots max) otherwise.  G rows in flight per lane group.
+#define HG_SEARCH_DISPATCH(FN, L2, ...)                                               \
+  switch (pd) {                                                                      \
+    case 16: return FN<0, 1, 1, 8, L2>(__VA_ARGS__);                                 \
+    case 32: return FN<0, 2, 2, 8, L2>(__VA_ARGS__);                                 \
+    case 64: return FN<1, 0, 2, 8, L2>(__VA_ARGS__);                                 \
+    case 96: return FN<1, 2, 4, 4, L2>(__VA_ARGS__);                                 \
+    case 112: return FN<1, 3, 5, 4, L2>(__VA_ARGS__);                                \
+    case 128: return FN<2, 0, 4, 4, L2>(__VA_ARGS__);                                \
+    case 256: return FN<4, 0, 8, 2, L2>(__VA_ARGS__);                                \
+    case 512: return FN<8, 0, 16, 2, L2>(__VA_ARGS__);                               \
+    case 768: return FN<12, 0, 24, 1, L2>(__VA_ARGS__);                              \
+    case 960: return FN<15, 0, 30, 1, L2>(__VA_ARGS__);                              \
+    case 1024: return FN<16, 0, 32, 1, L2>(__VA_ARGS__);                             \
+    default: break;                                                                  \
+  }                                                                                  \
+  {                                                                                  \
+    const int S_ = 2 * static_cast<int>(pd / 64) + static_cast<int>((pd % 64) / 16); \
+    if (S_ <= 5) return FN<-1, 0, 5, 4, L2>(__VA_ARGS__);                            \
+    if (S_ <= 9) return FN<-1, 0, 9, 2, L2>(__VA_ARGS__);                            \
+    if (S_ <= 17) return FN<-1, 0, 17, 2, L2>(__VA_ARGS__);                          \
+    if (S_ <= 33) return FN<-1, 0, 33, 1, L2>(__VA_ARGS__);                          \
   }
-  *out = static_cast<unsigned char*>(g_na_address[device]);
-  return cudaSuccess;
-}
 
-}  // namespace
-
-uint32_t noalloc_max_nodes() { return kNaMaxNodes; }
-uint32_t noalloc_max_queries() { return kNaMaxQueries; }
-uint32_t noalloc_max_ef() { return kNaMaxEf; }
-
-// Enqueue one batch with scratch from the static array.  P carries the graph
-// and the batch (shape H/R/C included); its scratch fields are filled here.
-// The caller made `device` current.
-cudaError_t launch_search_noalloc(SearchParams P, int device, bool cosine, cudaStream_t st) {
-  unsigned char* base = nullptr;
-  cudaError_t e = noalloc_scratch(device, &base);
-  if (e != cudaSuccess) return e;
-  uint32_t* ctr = reinterpret_cast<uint32_t*>(base + kNaOffCounters);
-  e = cudaMemsetAsync(ctr, 0, 256, st);  // counters and flags must start at zero
-  if (e != cudaSuccess) return e;
-  float* inv = nullptr;
-  if (cosine) {
-    inv = reinterpret_cast<float*>(base + kNaOffInv);
-    e = launch_inv_norm(P.queries, P.nq, P.dim, inv, st);
-    if (e != cudaSuccess) return e;
-  }
-  P.pool = reinterpret_cast<uint64_t*>(base + kNaOffPool);
-  P.pool_cap = kNaPoolCap;
-  P.bitmaps = reinterpret_cast<uint32_t*>(base + kNaOffBitmaps);
-  P.bitmap_words = kNaBitmapWords;
-  P.work = ctr;
-  P.ovf_count = ctr + 1;
-  P.ovf_list = reinterpret_cast<uint32_t*>(base + kNaOffOvf);
-  P.err = ctr + 4;
-  P.nq_dev = nullptr;
-  P.qidx = nullptr;
-  e = launch_search(P, inv, kNaBlocks, kNaWarpsPerBlock, st);
-  if (e != cudaSuccess) return e;
-  // queries whose spill pool overflowed: one warp with a pool of n keys
-  SearchParams B = P;
-  B.nq_dev = ctr + 1;
-  B.qidx = P.ovf_list;
-  B.work = ctr + 2;
-  B.pool = reinterpret_cast<uint64_t*>(base + kNaOffBigPool);
-  B.pool_cap = kNaMaxNodes;
-  B.bitmaps = reinterpret_cast<uint32_t*>(base + kNaOffBigBitmap);
-  B.ovf_count = ctr + 3;
-  return launch_search(B, inv, 1, 1, st);
-}
-
+}  // namespace sk
 }  // namespace hg
