@@ -60,12 +60,15 @@ def workload(rank: int):
 def launches_per_batch(ef_max: int) -> int:
     """Kernels one batch enqueues: the ef-bucketing kernel, one query kernel per
     ef bucket (16, 32, 64, ... up to ef_max) and the rerun pass."""
-    buckets, hi = 0, 16
-    while True:
-        buckets += 1
-        if hi >= ef_max or buckets == 12:
+    buckets = 0
+    for hi in (16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024):
+        if buckets == 11:
             break
-        hi *= 2
+        buckets += 1
+        if hi >= ef_max:
+            break
+    else:
+        buckets += 1
     return 2 + buckets
 
 

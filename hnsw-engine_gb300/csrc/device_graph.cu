@@ -464,11 +464,16 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
 
   // ---- ef buckets: one launch shape per bucket, sized for its largest ef ----
   hg::BucketSpec spec{};
-  for (uint32_t hi = 16;; hi *= 2) {
-    spec.hi[spec.n++] = std::min(hi, ef_max);
-    if (hi >= ef_max || spec.n == hg::kMaxBuckets) break;
+  {
+    // bucket bounds 16, 32, 64, 96, 128, 192, 256, 384, 512, ... (x1.5 / x4/3 steps)
+    static const uint32_t kHi[] = {16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024};
+    for (uint32_t hi : kHi) {
+      if (spec.n == hg::kMaxBuckets - 1) break;
+      spec.hi[spec.n++] = std::min(hi, ef_max);
+      if (hi >= ef_max) break;
+    }
+    if (spec.hi[spec.n - 1] < ef_max) spec.hi[spec.n++] = ef_max;
   }
-  spec.hi[spec.n - 1] = ef_max;
   struct Shape {
     uint32_t H, R, C;
     int wpb, blocks;
@@ -481,7 +486,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     const uint32_t E = spec.hi[b];
     sh.R = round_up(E, 32);
     sh.C = a->cand_cap ? a->cand_cap : std::max<uint32_t>(128, round_up(E + 32, 32));
-    sh.H = a->hash_slots ? a->hash_slots : (E <= 32 ? 1024u : (E <= 128 ? 2048u : 4096u));
+    sh.H = a->hash_slots ? a->hash_slots : (E <= 32 ? 1024u : (E <= 512 ? 2048u : 4096u));
     const uint32_t wbytes = hg::warp_smem_bytes(sh.H, sh.R, sh.C);
     sh.wpb = static_cast<int>(std::min<uint32_t>(4, (227u * 1024u) / wbytes));
     if (a->warps_per_block) sh.wpb = std::min<int>(sh.wpb, static_cast<int>(a->warps_per_block));
@@ -498,7 +503,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   const uint64_t pool_cap = a->pool_cap ? std::max<uint64_t>(a->pool_cap, 32)
                                         : std::min<uint64_t>(std::max<uint64_t>(g->n, 1), 16384);
   const uint32_t pool_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 1024));
-  const uint32_t bm_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 512));
+  const uint32_t bm_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 2048));
   HG_CUDA(g->pool.ensure(pool_slots * pool_cap * 8));
   HG_CUDA(g->bitmaps.ensure(bm_slots * bw * 4));
   HG_CUDA(g->owners.ensure((pool_slots + bm_slots) * 4));

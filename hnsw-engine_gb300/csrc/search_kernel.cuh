@@ -83,6 +83,23 @@ __device__ __forceinline__ float warp_minf(float v) {
   return v;
 }
 
+// Sort one 64-bit key per lane ascending across the warp (bitonic network).
+__device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const uint32_t lo = __shfl_xor_sync(kFull, static_cast<uint32_t>(v), j);
+      const uint32_t hi = __shfl_xor_sync(kFull, static_cast<uint32_t>(v >> 32), j);
+      const uint64_t o = (static_cast<uint64_t>(hi) << 32) | lo;
+      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+      v = keep_min ? (o < v ? o : v) : (o > v ? o : v);
+    }
+  }
+  return v;
+}
+__device__ __forceinline__ uint64_t warp_min64(uint64_t v) { return ~warp_max64(~v); }
+
 // number of elements of sorted a[0..n) that are < x (one lane)
 __device__ __forceinline__ int lower_bound(const uint64_t* a, int n, uint64_t x) {
   int lo = 0, hi = n;
@@ -442,6 +459,7 @@ struct Cands {
   uint64_t pmin;  // min key in pool (kMaxKey if empty)
   uint32_t peak;  // largest head + pool size seen
   bool overflow;
+  bool spilled;   // the pool was used
 };
 
 __device__ __forceinline__ bool pool_append(Warp& w, Cands& c, const SearchParams& P, const uint64_t* src, int cnt,
@@ -466,6 +484,7 @@ __device__ __forceinline__ bool pool_append(Warp& w, Cands& c, const SearchParam
   }
   if (lane < cnt) w.pool[c.pn + lane] = src[lane];
   c.pn += cnt;
+  c.spilled = true;
   return true;
 }
 
@@ -593,7 +612,7 @@ struct QueryOut {
 // the kernel
 // ---------------------------------------------------------------------------
 template <int NB, int NT, int S, int G, bool L2>
-__global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float* __restrict__ inv_norm) {
+__global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchParams P, const float* __restrict__ inv_norm) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -647,7 +666,7 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
     uint32_t n_uplists = 0, n_updists = 0, n_lists = 0, n_dists = 0, n_visit = 0;
 
     int s = 0;  // result count
-    Cands c{0, 0, 0, kMaxKey, 0, false};
+    Cands c{0, 0, 0, kMaxKey, 0, false, false};
     if (P.n > 0) {
       // ---- query registers (prepare_vector: cosine scaled by 1/||q||) ----
       const float* raw = P.queries + static_cast<size_t>(q) * P.dim;
@@ -706,6 +725,11 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
       }
 
       // ---- layer 0 (search_layer.cpp:58-134) ----
+      // Results: sorted base res[0..rtop] in shared memory plus up to 32 newly
+      // inserted keys in a register buffer (one per lane: rk, live set rvalid,
+      // largest rmax).  Candidates: sorted head cand[ch..ct) (+ spill pool)
+      // plus a register buffer (ck, cvalid, smallest cmin).  Buffers are
+      // merged into the arrays when 32 keys have gathered.
       if (lane == 0) visit(w, cur, tagged);
       __syncwarp();
       w.vcount = 1;
@@ -718,21 +742,52 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
       }
       c.ct = 1;
       c.peak = 1;
-      s = e0 ? 1 : 0;
+      int rtop = e0 ? 0 : -1;
+      s = rtop + 1;
+      uint64_t rk = kMaxKey, ck = kMaxKey, rmax = 0, cmin = kMaxKey;
+      uint32_t rvalid = 0, cvalid = 0;
+      float worst_d = (e0 && efi <= 1) ? cur_d : 0.0f;  // distance of the worst result once s >= ef
       __syncwarp();
 
+      // merge the result buffer into the sorted base
+      auto flush_res = [&]() {
+        const uint64_t v = warp_sort32(((rvalid >> lane) & 1u) ? rk : kMaxKey, lane);
+        const int m = __popc(rvalid);
+        if (lane < m) w.stE[lane] = v;
+        __syncwarp();
+        rtop = warp_merge(w.res, rtop + 1, static_cast<int>(P.R), w.stE, m, lane) - 1;
+        rvalid = 0;
+        rk = kMaxKey;
+        rmax = 0;
+      };
+      // merge the candidate buffer into the head (dropping keys past the worst result)
+      auto flush_cand = [&]() {
+        const uint64_t v = warp_sort32(((cvalid >> lane) & 1u) ? ck : kMaxKey, lane);
+        const bool full = s >= efi;
+        int m = __popc(cvalid);
+        if (full) m = __popc(__ballot_sync(kFull, lane < m && key_dist(v) <= worst_d));
+        if (lane < m) w.stA[lane] = v;
+        __syncwarp();
+        cand_insert(w, c, P, m, full, worst_d, lane);
+        cvalid = 0;
+        ck = kMaxKey;
+        cmin = kMaxKey;
+      };
+
       const uint32_t hlimit = (P.H * 5u) / 8u;
-      uint32_t pf_cid = kNoId, pf_id = kNoId;  // adjacency of the next head, loaded ahead
+      uint32_t pf_cid = kNoId, pf_id = kNoId;  // adjacency of the next candidate, loaded ahead
       for (;;) {
-        if (c.ch == c.ct) {
-          if (c.pn == 0) break;
-          const bool full = s >= efi;
-          refill(w, c, P, full, full ? key_dist(w.res[s - 1]) : 0.0f, lane);
-          if (c.ch == c.ct) break;
+        if (c.ch == c.ct && c.pn > 0) refill(w, c, P, s >= efi, worst_d, lane);
+        const uint64_t bh = c.ch < c.ct ? w.cand[c.ch] : kMaxKey;
+        const uint64_t top = bh < cmin ? bh : cmin;
+        if (top == kMaxKey) break;
+        if (s >= efi && key_dist(top) > worst_d) break;
+        if (bh < cmin) {
+          c.ch++;
+        } else {  // the best candidate sits in the register buffer
+          cvalid &= ~__ballot_sync(kFull, ((cvalid >> lane) & 1u) && ck == cmin);
+          cmin = warp_min64(((cvalid >> lane) & 1u) ? ck : kMaxKey);
         }
-        const uint64_t top = w.cand[c.ch];
-        if (s >= efi && key_dist(top) > key_dist(w.res[s - 1])) break;
-        c.ch++;
         const uint32_t cid = static_cast<uint32_t>(top);
         const uint32_t* lst = P.l0 + static_cast<size_t>(cid) * P.l0_stride;
         ++n_lists;
@@ -742,8 +797,10 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
           if (c0 == 0 && cid == pf_cid) id = pf_id;
           else id = j < P.M0 ? __ldg(lst + j) : kNoId;
           if (c0 == 0 && single_chunk) {
-            // load the list of the next head while this one is expanded
-            pf_cid = c.ch < c.ct ? static_cast<uint32_t>(w.cand[c.ch]) : kNoId;
+            // load the list of the next candidate while this one is expanded
+            const uint64_t nb = c.ch < c.ct ? w.cand[c.ch] : kMaxKey;
+            const uint64_t nx = nb < cmin ? nb : cmin;
+            pf_cid = nx != kMaxKey ? static_cast<uint32_t>(nx) : kNoId;
             if (pf_cid != kNoId) pf_id = lane < static_cast<int>(P.M0)
                                              ? __ldg(P.l0 + static_cast<size_t>(pf_cid) * P.l0_stride + lane)
                                              : kNoId;
@@ -775,67 +832,54 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
           const uint64_t key = mkkey(d, id);
 
           // ---- in-order acceptance replay (search_layer.cpp:112-132) ----
-          uint32_t acc = 0, ins = 0, inres = 0;
-          int scur = s, r = s - 1;  // r: largest original result not yet evicted
-          uint64_t maxI = 0;        // largest inserted key still in the results
-          float worst_d = 0.0f;
-          if (s >= efi) {
-            worst_d = key_dist(w.res[s - 1]);
-            U &= __ballot_sync(kFull, d < worst_d);  // worst only decreases
-          }
+          if (s >= efi) U &= __ballot_sync(kFull, d < worst_d);  // the worst only decreases
           while (U) {
             const int jl = __ffs(U) - 1;
             U &= U - 1;
             const float dj = __shfl_sync(kFull, d, jl);
-            if (!(scur < efi || dj < worst_d)) continue;
-            acc |= 1u << jl;
-            if (!__shfl_sync(kFull, elig, jl)) continue;
+            if (!(s < efi || dj < worst_d)) continue;
             const uint64_t kj = shfl64(key, jl);
-            ins |= 1u << jl;
-            inres |= 1u << jl;
-            maxI = kj > maxI ? kj : maxI;
-            if (scur < efi) {
-              if (++scur < efi) continue;
-            } else {  // evict the largest of res[0..r] and the inserted keys
-              const uint64_t rr = r >= 0 ? w.res[r] : 0ull;
-              if (rr > maxI) {
-                --r;
+            // candidate
+            if (cvalid == kFull) {
+              flush_cand();
+              if (c.overflow) break;
+            }
+            {
+              const int slot = __ffs(~cvalid) - 1;
+              if (lane == slot) ck = kj;
+              cvalid |= 1u << slot;
+              cmin = kj < cmin ? kj : cmin;
+            }
+            if (!__shfl_sync(kFull, elig, jl)) continue;
+            // result
+            if (rvalid == kFull) flush_res();
+            {
+              const int slot = __ffs(~rvalid) - 1;
+              if (lane == slot) rk = kj;
+              rvalid |= 1u << slot;
+              rmax = kj > rmax ? kj : rmax;
+            }
+            if (s < efi) {
+              if (++s < efi) continue;
+            } else {  // evict the largest of res[rtop] and the buffer
+              const uint64_t bt = rtop >= 0 ? w.res[rtop] : 0ull;
+              if (bt > rmax) {
+                --rtop;
               } else {
-                inres &= ~__ballot_sync(kFull, ((inres >> lane) & 1u) && key == maxI);
-                maxI = warp_max64((inres >> lane) & 1u ? key : 0ull);
+                rvalid &= ~__ballot_sync(kFull, ((rvalid >> lane) & 1u) && rk == rmax);
+                rmax = warp_max64(((rvalid >> lane) & 1u) ? rk : 0ull);
               }
             }
-            const uint64_t rr = r >= 0 ? w.res[r] : 0ull;
-            worst_d = key_dist(rr > maxI ? rr : maxI);
+            const uint64_t bt = rtop >= 0 ? w.res[rtop] : 0ull;
+            worst_d = key_dist(bt > rmax ? bt : rmax);
           }
-          if (!acc) continue;
-
-          // ---- sorted batches: all accepted (cand), eligible accepted (res) ----
-          {
-            int rA = 0, rE = 0;
-            uint32_t it = acc;
-            while (it) {
-              const int i = __ffs(it) - 1;
-              it &= it - 1;
-              const bool lt = shfl64(key, i) < key;
-              rA += lt;
-              rE += lt && ((ins >> i) & 1u);
-            }
-            if ((acc >> lane) & 1u) w.stA[rA] = key;
-            if ((ins >> lane) & 1u) w.stE[rE] = key;
-            __syncwarp();
-          }
-          const int mA = __popc(acc), mE = __popc(ins);
-          s = warp_merge(w.res, s, efi, w.stE, mE, lane);
-          int mAk = mA;
-          const bool full = s >= efi;
-          const float wd = full ? key_dist(w.res[s - 1]) : 0.0f;
-          if (full) mAk = __popc(__ballot_sync(kFull, lane < mA && key_dist(w.stA[lane]) <= wd));
-          cand_insert(w, c, P, mAk, full, wd, lane);
           if (c.overflow) break;
+          const uint64_t live = static_cast<uint64_t>(c.ct - c.ch) + c.pn + __popc(cvalid);
+          c.peak = live > c.peak ? static_cast<uint32_t>(live) : c.peak;
         }
         if (c.overflow) break;
       }
+      if (!c.overflow) flush_res();  // res[0..s) sorted for the output
     }
 
     const bool used_bitmap = w.bitmap_mode;
@@ -874,7 +918,7 @@ __global__ void __launch_bounds__(128) search_kernel(SearchParams P, const float
       cp[4] = n_visit;
       cp[5] = c.peak;
       cp[6] = static_cast<unsigned long long>(s);
-      cp[7] = (used_bitmap ? kTierBitmap : 0u) | (c.peak > P.C ? kTierPool : 0u) | (P.rerun ? kTierRerun : 0u);
+      cp[7] = (used_bitmap ? kTierBitmap : 0u) | (c.spilled ? kTierPool : 0u) | (P.rerun ? kTierRerun : 0u);
     }
     __syncwarp();
   }
