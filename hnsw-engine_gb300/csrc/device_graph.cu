@@ -28,6 +28,11 @@ int slots_for(uint32_t pd);
 cudaError_t launch_inv_norm(const float* qs, uint32_t nq, uint32_t dim, float* out, cudaStream_t st);
 cudaError_t launch_search(const SearchParams& P, const float* inv, int blocks, int warps_per_block, cudaStream_t st);
 int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, uint32_t R, uint32_t C);
+cudaError_t launch_search_approx(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st);
+int occupancy_approx(uint32_t pdc, int metric, int prec, int wpb, size_t smem);
+cudaError_t launch_rerank(const SearchParams& P, const float* inv, int blocks, cudaStream_t st);
+cudaError_t launch_encode(const float* vecs, uint32_t n, uint32_t pd, uint32_t pdc, int prec, void* out,
+                          float* scale, cudaStream_t st);
 cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, uint32_t ef_all, uint32_t ef_default,
                           uint32_t k_all, const BucketSpec& spec, uint32_t* counts, uint32_t* lists, cudaStream_t st);
 cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bits, const uint64_t* labels, uint32_t n,
@@ -129,6 +134,9 @@ struct hgd_graph {
   DBuf q, efq, kq, fsel, fptrs, fbits, inv, out, nres, counters;
   DBuf work;  // [0] work counter, [1] overflow count, [2] rerun work counter
   DBuf ovf_list, pool, bitmaps, pool_big, bitmaps_big, owners, lists;
+  // compressed copies for FP16 / FP8 traversal (built on first use) and pools
+  DBuf v16, v8, vscale, pool_ids, pool_n;
+  bool has16 = false, has8 = false;
   std::vector<cudaStream_t> aux;    // one per ef bucket
   std::vector<cudaEvent_t> ev_join;
   cudaEvent_t ev_fork = nullptr;
@@ -272,7 +280,7 @@ void hgd_graph_free(hgd_graph* g) {
   cudaSetDevice(g->device);
   for (DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->q, &g->efq, &g->kq, &g->fsel,
                   &g->fptrs, &g->fbits, &g->inv, &g->out, &g->nres, &g->counters, &g->work, &g->ovf_list, &g->pool,
-                  &g->bitmaps, &g->pool_big, &g->bitmaps_big, &g->owners, &g->lists})
+                  &g->bitmaps, &g->pool_big, &g->bitmaps_big, &g->owners, &g->lists, &g->v16, &g->v8, &g->vscale, &g->pool_ids, &g->pool_n})
     d->release();
   for (cudaStream_t s2 : g->aux) cudaStreamDestroy(s2);
   for (cudaEvent_t e2 : g->ev_join) cudaEventDestroy(e2);
@@ -289,7 +297,7 @@ uint64_t hgd_graph_device_bytes(const hgd_graph* g) {
   for (const DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->q, &g->efq, &g->kq,
                         &g->fsel, &g->fptrs, &g->fbits, &g->inv, &g->out, &g->nres, &g->counters, &g->work,
                         &g->ovf_list, &g->pool, &g->bitmaps, &g->pool_big, &g->bitmaps_big, &g->owners,
-                        &g->lists})
+                        &g->lists, &g->v16, &g->v8, &g->vscale, &g->pool_ids, &g->pool_n})
     t += d->bytes;
   return t;
 }
@@ -300,7 +308,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   if (a->nq == 0) return HGD_OK;
   if (!a->queries || !a->out) return fail(HGD_EINVAL, "search_batch: null pointer");
   if (a->nq >= 0xFFFFFFFFull) return fail(HGD_EINVAL, "hgd_search: too many queries in one batch");
-  if (a->precision != HGD_PREC_FP32) return fail(HGD_EINVAL, "hgd_search: precision not available in this build");
+  if (a->precision > HGD_PREC_FP8) return fail(HGD_EINVAL, "hgd_search: unknown precision");
   if (a->num_filters && !a->filters) return fail(HGD_EINVAL, "hgd_search: null filter table");
   std::lock_guard<std::mutex> lock(g->mu);
   HG_CUDA(cudaSetDevice(g->device));
@@ -456,6 +464,36 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   P.out = d_out;
   P.nres = d_nres;
   P.counters = d_cnt;
+  // ---- compressed traversal: FP16 / FP8 copies (built once) and the rerank pools ----
+  const int prec = static_cast<int>(a->precision);
+  if (prec != HGD_PREC_FP32) {
+    const uint32_t pdc = round_up(static_cast<uint32_t>(g->dim), 128);
+    if (pdc != 128 && pdc != 256 && pdc != 512 && pdc != 1024)
+      return fail(HGD_EINVAL, "hgd_search: FP16/FP8 traversal supports dim <= 256, 257..512 and 513..1024 "
+                              "rounded to 128/256/512/1024");
+    DBuf& vb = prec == HGD_PREC_FP16 ? g->v16 : g->v8;
+    bool& have = prec == HGD_PREC_FP16 ? g->has16 : g->has8;
+    if (!have) {
+      HG_CUDA(vb.ensure(g->n * pdc * (prec == HGD_PREC_FP16 ? 2 : 1)));
+      if (prec == HGD_PREC_FP8) HG_CUDA(g->vscale.ensure(g->n * 4));
+      HG_CUDA(hg::launch_encode(g->vecs.as<float>(), static_cast<uint32_t>(g->n), static_cast<uint32_t>(g->pd), pdc,
+                                prec, vb.p, prec == HGD_PREC_FP8 ? g->vscale.as<float>() : nullptr, st));
+      have = true;
+    }
+    P.vq = vb.p;
+    P.vscale = prec == HGD_PREC_FP8 ? g->vscale.as<float>() : nullptr;
+    P.pdc = pdc;
+    P.pool_stride = round_up(ef_max, 32);
+    HG_CUDA(g->pool_ids.ensure(nq * P.pool_stride * 4));
+    HG_CUDA(g->pool_n.ensure(nq * 4));
+    P.pool_out = g->pool_ids.as<uint32_t>();
+    P.pool_n = g->pool_n.as<uint32_t>();
+  }
+  auto launch = [&](const hg::SearchParams& B, int blocks, int wpb, cudaStream_t sb) {
+    return prec == HGD_PREC_FP32 ? hg::launch_search(B, d_inv, blocks, wpb, sb)
+                                 : hg::launch_search_approx(B, d_inv, blocks, wpb, sb);
+  };
+
   if (a->cand_cap && (a->cand_cap < 128 || a->cand_cap % 32))
     return fail(HGD_EINVAL, "hgd_search: cand_cap must be a multiple of 32, >= 128");
   if (a->hash_slots && (a->hash_slots < 256 || (a->hash_slots & (a->hash_slots - 1))))
@@ -491,7 +529,10 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     sh.wpb = static_cast<int>(std::min<uint32_t>(4, (227u * 1024u) / wbytes));
     if (a->warps_per_block) sh.wpb = std::min<int>(sh.wpb, static_cast<int>(a->warps_per_block));
     if (sh.wpb < 1) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
-    const int occ = hg::search_occupancy(static_cast<uint32_t>(g->pd), g->metric, sh.wpb, sh.H, sh.R, sh.C);
+    const int occ = prec == HGD_PREC_FP32
+                        ? hg::search_occupancy(static_cast<uint32_t>(g->pd), g->metric, sh.wpb, sh.H, sh.R, sh.C)
+                        : hg::occupancy_approx(P.pdc, g->metric, prec, sh.wpb,
+                                               static_cast<size_t>(sh.wpb) * hg::warp_smem_bytes(sh.H, sh.R, sh.C));
     if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the search kernel cannot be resident with this shape");
     const uint64_t want = (nq + sh.wpb - 1) / sh.wpb;
     sh.blocks = static_cast<int>(std::min<uint64_t>(want, static_cast<uint64_t>(g->sms) * occ));
@@ -555,7 +596,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     B.qidx = g->lists.as<uint32_t>() + static_cast<uint64_t>(b) * nq;
     B.work = work + 8 + b;
     B.slot_base = sh.slot_base;
-    cudaError_t e = hg::launch_search(B, d_inv, sh.blocks, sh.wpb, sb);
+    cudaError_t e = launch(B, sh.blocks, sh.wpb, sb);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("search kernel launch: ") + cudaGetErrorString(e));
     HG_CUDA(cudaEventRecord(g->ev_join[b], sb));
   }
@@ -583,8 +624,16 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     B.rerun = 1;
     const uint32_t wb = hg::warp_smem_bytes(B.H, B.R, B.C);
     if (wb > 227u * 1024u) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
-    cudaError_t e = hg::launch_search(B, d_inv, static_cast<int>(big_slots), 1, st);
+    cudaError_t e = launch(B, static_cast<int>(big_slots), 1, st);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("rerun kernel launch: ") + cudaGetErrorString(e));
+  }
+  // ---- exact FP32 rerank of the traversal pools ----
+  if (prec != HGD_PREC_FP32) {
+    hg::SearchParams B = P;
+    B.R = next_pow2(P.pool_stride);  // per-warp sort buffer
+    const int blocks = static_cast<int>(std::min<uint64_t>((nq + 3) / 4, static_cast<uint64_t>(g->sms) * 8));
+    cudaError_t e = hg::launch_rerank(B, d_inv, blocks, st);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("rerank kernel launch: ") + cudaGetErrorString(e));
   }
   // ---- results back ----
   if (!a->out_on_device) {

@@ -1,0 +1,33 @@
+// search_approx.cu -- the query kernel on compressed rows (FP16 or per-row
+// scaled FP8 E4M3, FP32 accumulation) for padded row lengths 128 / 256 /
+// 512 / 1024, both metric families.  The exact FP32 rerank lives in
+// rerank.cu.
+#include "search_kernel.cuh"
+
+namespace hg {
+
+cudaError_t launch_search_approx(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st) {
+  const uint32_t pdc = P.pdc;
+  const int prec = static_cast<int>(P.vscale != nullptr) + 1;  // 1 fp16, 2 fp8
+  if (P.metric == 0) {
+    if (prec == 1) { HG_SEARCH_APPROX_DISPATCH(sk::launch_t, 1, true, P, inv, blocks, wpb, st) }
+    else { HG_SEARCH_APPROX_DISPATCH(sk::launch_t, 2, true, P, inv, blocks, wpb, st) }
+  } else {
+    if (prec == 1) { HG_SEARCH_APPROX_DISPATCH(sk::launch_t, 1, false, P, inv, blocks, wpb, st) }
+    else { HG_SEARCH_APPROX_DISPATCH(sk::launch_t, 2, false, P, inv, blocks, wpb, st) }
+  }
+  return cudaErrorInvalidValue;
+}
+
+int occupancy_approx(uint32_t pdc, int metric, int prec, int wpb, size_t smem) {
+  if (metric == 0) {
+    if (prec == 1) { HG_SEARCH_APPROX_DISPATCH(sk::occupancy_t, 1, true, wpb, smem) }
+    else { HG_SEARCH_APPROX_DISPATCH(sk::occupancy_t, 2, true, wpb, smem) }
+  } else {
+    if (prec == 1) { HG_SEARCH_APPROX_DISPATCH(sk::occupancy_t, 1, false, wpb, smem) }
+    else { HG_SEARCH_APPROX_DISPATCH(sk::occupancy_t, 2, false, wpb, smem) }
+  }
+  return 0;
+}
+
+}  // namespace hg

@@ -55,6 +55,13 @@ struct SearchParams {
   uint32_t bm_slots;
   uint32_t slot_base;       // first warp slot of this launch (per-slot mode)
   int32_t rerun;            // 1: this launch is the rerun pass (counter flag only)
+  // ---- compressed traversal (FP16 / FP8-E4M3 rows) ----
+  const void* vq;           // n x pdc compressed rows (halves or e4m3 bytes), zero padded
+  const float* vscale;      // FP8: per-row scale (row = scale x e4m3 values)
+  uint32_t pdc;             // compressed row length (dim rounded up to 128)
+  uint32_t* pool_out;       // nq x pool_stride: final traversal pool (ids, sorted by traversal distance)
+  uint32_t pool_stride;
+  uint32_t* pool_n;         // nq: pool size
   uint32_t* work;           // work-queue counter (zeroed before launch)
   uint32_t* ovf_list;       // queries whose pool overflowed
   uint32_t* ovf_count;

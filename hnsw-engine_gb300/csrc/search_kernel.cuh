@@ -34,6 +34,8 @@
 // (8(C+32) B) and two 32-entry staging arrays.
 #pragma once
 
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -294,6 +296,147 @@ __device__ __forceinline__ float lane_dists(const Layout<NB, NT, S>& L, const fl
   }
   return mine;
 }
+
+// ---------------------------------------------------------------------------
+// distance policies.  ExactDist: FP32 rows in the reference's AVX-512 order
+// (bit-identical distances).  ApproxDist: FP16 or per-row-scaled FP8 E4M3
+// rows, FP32 accumulation in any order; RPP rows per warp pass, each row
+// spread over 32/RPP lanes holding E consecutive elements (16-byte loads).
+// ---------------------------------------------------------------------------
+template <int NB, int NT, int S, int G>
+struct ExactDist {
+  static constexpr bool kApprox = false;
+  static constexpr int kMinBlocks = S >= 16 ? 4 : 5;
+  Layout<NB, NT, S> L;
+  float qr[S];
+  __device__ __forceinline__ void init(const SearchParams& P) {
+    L.nb_rt = static_cast<int>(P.pd / 64);
+    L.nt_rt = static_cast<int>((P.pd % 64) / 16);
+  }
+  __device__ __forceinline__ void load_query(const SearchParams& P, const float* raw, const float* inv_norm,
+                                             uint32_t q, int lane) {
+    const float inv = inv_norm ? inv_norm[q] : 1.0f;
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      const int e = L.elem(i, lane);
+      const float v = (e >= 0 && e < static_cast<int>(P.dim)) ? __ldg(raw + e) : 0.0f;
+      qr[i] = inv_norm ? __fmul_rn(v, inv) : v;
+    }
+  }
+  template <bool L2>
+  __device__ __forceinline__ float dists(const SearchParams& P, uint32_t id, uint32_t mask, int lane) const {
+    return lane_dists<NB, NT, S, G, L2>(L, P.vecs, P.pd, id, mask, qr, lane);
+  }
+};
+
+template <int PREC, bool L2, int E>
+__device__ __forceinline__ float approx_partial(const SearchParams& P, uint32_t id, int sub, const float (&qa)[E]) {
+  float acc = 0.0f;
+  if (PREC == 1) {
+    const uint4* p = reinterpret_cast<const uint4*>(static_cast<const __half*>(P.vq) +
+                                                    static_cast<size_t>(id) * P.pdc + sub * E);
+#pragma unroll
+    for (int c = 0; c < E / 8; ++c) {
+      const uint4 u = __ldg(p + c);
+      const uint32_t wds[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&wds[h]));
+        const float x0 = f.x, x1 = f.y;
+        const float q0 = qa[c * 8 + 2 * h], q1 = qa[c * 8 + 2 * h + 1];
+        if (L2) {
+          const float d0 = q0 - x0, d1 = q1 - x1;
+          acc = __fmaf_rn(d0, d0, acc);
+          acc = __fmaf_rn(d1, d1, acc);
+        } else {
+          acc = __fmaf_rn(q0, x0, acc);
+          acc = __fmaf_rn(q1, x1, acc);
+        }
+      }
+    }
+  } else {
+    const uint4* p = reinterpret_cast<const uint4*>(static_cast<const uint8_t*>(P.vq) +
+                                                    static_cast<size_t>(id) * P.pdc + sub * E);
+    const float sc = __ldg(P.vscale + id);
+#pragma unroll
+    for (int c = 0; c < E / 16; ++c) {
+      const uint4 u = __ldg(p + c);
+      const uint32_t wds[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+#pragma unroll
+        for (int pr = 0; pr < 2; ++pr) {
+          const __nv_fp8x2_storage_t two = static_cast<__nv_fp8x2_storage_t>((wds[h] >> (16 * pr)) & 0xFFFFu);
+          const __half2_raw hr = __nv_cvt_fp8x2_to_halfraw2(two, __NV_E4M3);
+          const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&hr));
+          const float x0 = f.x * sc, x1 = f.y * sc;
+          const float q0 = qa[c * 16 + 4 * h + 2 * pr], q1 = qa[c * 16 + 4 * h + 2 * pr + 1];
+          if (L2) {
+            const float d0 = q0 - x0, d1 = q1 - x1;
+            acc = __fmaf_rn(d0, d0, acc);
+            acc = __fmaf_rn(d1, d1, acc);
+          } else {
+            acc = __fmaf_rn(q0, x0, acc);
+            acc = __fmaf_rn(q1, x1, acc);
+          }
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+template <int RPP, int E, int PREC>
+struct ApproxDist {
+  static constexpr bool kApprox = true;
+  static constexpr int kMinBlocks = 5;
+  static constexpr int LPR = 32 / RPP;
+  float qa[E];
+  __device__ __forceinline__ void init(const SearchParams&) {}
+  __device__ __forceinline__ void load_query(const SearchParams& P, const float* raw, const float* inv_norm,
+                                             uint32_t q, int lane) {
+    const float inv = inv_norm ? inv_norm[q] : 1.0f;
+    const int base = (lane % LPR) * E;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int idx = base + e;
+      const float v = idx < static_cast<int>(P.dim) ? __ldg(raw + idx) : 0.0f;
+      qa[e] = inv_norm ? __fmul_rn(v, inv) : v;
+    }
+  }
+  template <bool L2>
+  __device__ __forceinline__ float dists(const SearchParams& P, uint32_t id, uint32_t mask, int lane) const {
+    const int qi = lane / LPR, sub = lane % LPR;
+    float mine = 0.0f;
+    while (mask) {
+      int ow[RPP];
+      uint32_t rid[RPP];
+#pragma unroll
+      for (int r = 0; r < RPP; ++r) {
+        ow[r] = mask ? __ffs(mask) - 1 : -1;
+        if (mask) mask &= mask - 1;
+        rid[r] = __shfl_sync(kFull, id, ow[r] < 0 ? 0 : ow[r]);
+      }
+      int myow = ow[0];
+      uint32_t myid = rid[0];
+#pragma unroll
+      for (int r = 1; r < RPP; ++r)
+        if (qi == r) {
+          myow = ow[r];
+          myid = rid[r];
+        }
+      float acc = myow >= 0 ? approx_partial<PREC, L2, E>(P, myid, sub, qa) : 0.0f;
+#pragma unroll
+      for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+#pragma unroll
+      for (int r = 0; r < RPP; ++r) {
+        const float v = __shfl_sync(kFull, acc, r * LPR);
+        if (ow[r] == lane) mine = L2 ? v : 1.0f - v;
+      }
+    }
+    return mine;
+  }
+};
 
 // ---------------------------------------------------------------------------
 // per-warp state
@@ -611,8 +754,8 @@ struct QueryOut {
 // ---------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------
-template <int NB, int NT, int S, int G, bool L2>
-__global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchParams P, const float* __restrict__ inv_norm) {
+template <class DP, bool L2>
+__global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParams P, const float* __restrict__ inv_norm) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -636,7 +779,8 @@ __global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchPa
   for (uint32_t i = lane; i < P.H; i += 32) w.hash[i] = tagged ? 0u : kNoId;
   __syncwarp();
 
-  Layout<NB, NT, S> L{static_cast<int>(P.pd / 64), static_cast<int>((P.pd % 64) / 16)};
+  DP dp;
+  dp.init(P);
   const uint32_t nq = P.nq_dev ? *P.nq_dev : P.nq;
   const bool single_chunk = P.M0 <= 32;
 
@@ -669,15 +813,7 @@ __global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchPa
     Cands c{0, 0, 0, kMaxKey, 0, false, false};
     if (P.n > 0) {
       // ---- query registers (prepare_vector: cosine scaled by 1/||q||) ----
-      const float* raw = P.queries + static_cast<size_t>(q) * P.dim;
-      const float inv = inv_norm ? inv_norm[q] : 1.0f;
-      float qr[S];
-#pragma unroll
-      for (int i = 0; i < S; ++i) {
-        const int e = L.elem(i, lane);
-        const float v = (e >= 0 && e < static_cast<int>(P.dim)) ? __ldg(raw + e) : 0.0f;
-        qr[i] = inv_norm ? __fmul_rn(v, inv) : v;
-      }
+      dp.load_query(P, P.queries + static_cast<size_t>(q) * P.dim, inv_norm, q, lane);
       // ---- visited set for this query ----
       w.bitmap_mode = false;
       w.vcount = 0;
@@ -696,7 +832,7 @@ __global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchPa
 
       // ---- entry point + greedy descent (search_layer.cpp:29-56,156-157) ----
       uint32_t cur = P.entry;
-      float cur_d = lane_dists<NB, NT, S, G, L2>(L, P.vecs, P.pd, cur, 1u, qr, lane);
+      float cur_d = dp.template dists<L2>(P, cur, 1u, lane);
       cur_d = __shfl_sync(kFull, cur_d, 0);
       n_updists = 1;
       for (int lc = P.max_level; lc > 0; --lc) {
@@ -711,7 +847,7 @@ __global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchPa
             const uint32_t vm = __ballot_sync(kFull, id != kNoId);
             if (!vm) break;
             n_updists += __popc(vm);
-            const float d = lane_dists<NB, NT, S, G, L2>(L, P.vecs, P.pd, id, vm, qr, lane);
+            const float d = dp.template dists<L2>(P, id, vm, lane);
             const float m = warp_minf(id != kNoId ? d : __int_as_float(0x7f800000));
             if (m < cur_d) {
               const uint32_t hit = __ballot_sync(kFull, id != kNoId && d == m);
@@ -826,7 +962,7 @@ __global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchPa
           n_visit += nu;
           if (!U) continue;
           n_dists += nu;
-          const float d = lane_dists<NB, NT, S, G, L2>(L, P.vecs, P.pd, id, U, qr, lane);
+          const float d = dp.template dists<L2>(P, id, U, lane);
           bool elig = true;
           if (filtered && fresh) elig = bit_of(P.alive, id) && (!fb || bit_of(fb, id));
           const uint64_t key = mkkey(d, id);
@@ -892,23 +1028,31 @@ __global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchPa
       continue;
     }
 
-    // ---- output (search_layer.cpp:166-169, 189-192) ----
-    const int m = s < static_cast<int>(k) ? s : static_cast<int>(k);
-    QueryOut* row = static_cast<QueryOut*>(P.out) + static_cast<size_t>(q) * P.k_stride;
-    for (uint32_t j = lane; j < P.k_stride; j += 32) {
-      QueryOut o;
-      if (static_cast<int>(j) < m) {
-        const uint64_t kk = w.res[j];
-        o.label = P.labels[static_cast<uint32_t>(kk)];
-        o.dist = key_dist(kk);
-      } else {
-        o.label = ~0ull;
-        o.dist = __int_as_float(0x7f800000);
-      }
-      o.zero = 0;
-      row[j] = o;
+    if (DP::kApprox) {
+      // traversal pool for the exact rerank (sorted by traversal distance)
+      uint32_t* prow = P.pool_out + static_cast<size_t>(q) * P.pool_stride;
+      for (int j = lane; j < s; j += 32) prow[j] = static_cast<uint32_t>(w.res[j]);
+      if (lane == 0) P.pool_n[q] = static_cast<uint32_t>(s);
     }
-    if (P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
+    // ---- output (search_layer.cpp:166-169, 189-192) ----
+    const int m = DP::kApprox ? 0 : (s < static_cast<int>(k) ? s : static_cast<int>(k));
+    if (!DP::kApprox) {
+      QueryOut* row = static_cast<QueryOut*>(P.out) + static_cast<size_t>(q) * P.k_stride;
+      for (uint32_t j = lane; j < P.k_stride; j += 32) {
+        QueryOut o;
+        if (static_cast<int>(j) < m) {
+          const uint64_t kk = w.res[j];
+          o.label = P.labels[static_cast<uint32_t>(kk)];
+          o.dist = key_dist(kk);
+        } else {
+          o.label = ~0ull;
+          o.dist = __int_as_float(0x7f800000);
+        }
+        o.zero = 0;
+        row[j] = o;
+      }
+    }
+    if (!DP::kApprox && P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
     if (P.counters && lane == 0) {
       unsigned long long* cp = P.counters + static_cast<size_t>(q) * kCounters;
       cp[0] = n_uplists;
@@ -925,20 +1069,20 @@ __global__ void __launch_bounds__(128, (S >= 16 ? 4 : 5)) search_kernel(SearchPa
 }
 
 // Host-side launch / occupancy for one instantiation.
-template <int NB, int NT, int S, int G, bool L2>
+template <class DP, bool L2>
 cudaError_t launch_t(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st) {
   const size_t smem = static_cast<size_t>(wpb) * warp_smem_bytes(P.H, P.R, P.C);
-  auto* fn = search_kernel<NB, NT, S, G, L2>;
+  auto* fn = search_kernel<DP, L2>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   fn<<<blocks, 32 * wpb, smem, st>>>(P, inv);
   return cudaGetLastError();
 }
 
-template <int NB, int NT, int S, int G, bool L2>
+template <class DP, bool L2>
 int occupancy_t(int wpb, size_t smem) {
   int blocks = 0;
-  auto* fn = search_kernel<NB, NT, S, G, L2>;
+  auto* fn = search_kernel<DP, L2>;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 32 * wpb, smem) != cudaSuccess) return 0;
@@ -949,25 +1093,96 @@ int occupancy_t(int wpb, size_t smem) {
 // runtime layout (S slots max) otherwise.  G rows in flight per lane group.
 #define HG_SEARCH_DISPATCH(FN, L2, ...)                                               \
   switch (pd) {                                                                      \
-    case 16: return FN<0, 1, 1, 8, L2>(__VA_ARGS__);                                 \
-    case 32: return FN<0, 2, 2, 8, L2>(__VA_ARGS__);                                 \
-    case 64: return FN<1, 0, 2, 8, L2>(__VA_ARGS__);                                 \
-    case 96: return FN<1, 2, 4, 4, L2>(__VA_ARGS__);                                 \
-    case 112: return FN<1, 3, 5, 4, L2>(__VA_ARGS__);                                \
-    case 128: return FN<2, 0, 4, 4, L2>(__VA_ARGS__);                                \
-    case 256: return FN<4, 0, 8, 2, L2>(__VA_ARGS__);                                \
-    case 512: return FN<8, 0, 16, 2, L2>(__VA_ARGS__);                               \
-    case 768: return FN<12, 0, 24, 1, L2>(__VA_ARGS__);                              \
-    case 960: return FN<15, 0, 30, 1, L2>(__VA_ARGS__);                              \
-    case 1024: return FN<16, 0, 32, 1, L2>(__VA_ARGS__);                             \
+    case 16: return FN<sk::ExactDist<0, 1, 1, 8>, L2>(__VA_ARGS__);                                 \
+    case 32: return FN<sk::ExactDist<0, 2, 2, 8>, L2>(__VA_ARGS__);                                 \
+    case 64: return FN<sk::ExactDist<1, 0, 2, 8>, L2>(__VA_ARGS__);                                 \
+    case 96: return FN<sk::ExactDist<1, 2, 4, 4>, L2>(__VA_ARGS__);                                 \
+    case 112: return FN<sk::ExactDist<1, 3, 5, 4>, L2>(__VA_ARGS__);                                \
+    case 128: return FN<sk::ExactDist<2, 0, 4, 4>, L2>(__VA_ARGS__);                                \
+    case 256: return FN<sk::ExactDist<4, 0, 8, 2>, L2>(__VA_ARGS__);                                \
+    case 512: return FN<sk::ExactDist<8, 0, 16, 2>, L2>(__VA_ARGS__);                               \
+    case 768: return FN<sk::ExactDist<12, 0, 24, 1>, L2>(__VA_ARGS__);                              \
+    case 960: return FN<sk::ExactDist<15, 0, 30, 1>, L2>(__VA_ARGS__);                              \
+    case 1024: return FN<sk::ExactDist<16, 0, 32, 1>, L2>(__VA_ARGS__);                             \
     default: break;                                                                  \
   }                                                                                  \
   {                                                                                  \
     const int S_ = 2 * static_cast<int>(pd / 64) + static_cast<int>((pd % 64) / 16); \
-    if (S_ <= 5) return FN<-1, 0, 5, 4, L2>(__VA_ARGS__);                            \
-    if (S_ <= 9) return FN<-1, 0, 9, 2, L2>(__VA_ARGS__);                            \
-    if (S_ <= 17) return FN<-1, 0, 17, 2, L2>(__VA_ARGS__);                          \
-    if (S_ <= 33) return FN<-1, 0, 33, 1, L2>(__VA_ARGS__);                          \
+    if (S_ <= 5) return FN<sk::ExactDist<-1, 0, 5, 4>, L2>(__VA_ARGS__);                            \
+    if (S_ <= 9) return FN<sk::ExactDist<-1, 0, 9, 2>, L2>(__VA_ARGS__);                            \
+    if (S_ <= 17) return FN<sk::ExactDist<-1, 0, 17, 2>, L2>(__VA_ARGS__);                          \
+    if (S_ <= 33) return FN<sk::ExactDist<-1, 0, 33, 1>, L2>(__VA_ARGS__);                          \
+  }
+
+// ---------------------------------------------------------------------------
+// Exact FP32 rerank of the traversal pools of a compressed-precision batch:
+// one warp per query recomputes the distances of its pool in the reference
+// order, sorts (distance, id) and writes the first k results.
+// Shared memory per warp: R keys.
+// ---------------------------------------------------------------------------
+template <class DP, bool L2>
+__global__ void __launch_bounds__(128) rerank_kernel(SearchParams P, const float* __restrict__ inv_norm) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smem) + static_cast<size_t>(wib) * P.R;
+  DP dp;
+  dp.init(P);
+  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + wib; q < P.nq; q += nw) {
+    const int s = static_cast<int>(P.pool_n[q]);
+    const uint32_t* prow = P.pool_out + static_cast<size_t>(q) * P.pool_stride;
+    dp.load_query(P, P.queries + static_cast<size_t>(q) * P.dim, inv_norm, q, lane);
+    for (int c0 = 0; c0 < s; c0 += 32) {
+      const bool live = c0 + lane < s;
+      const uint32_t id = live ? prow[c0 + lane] : kNoId;
+      const uint32_t mask = __ballot_sync(kFull, live);
+      const float d = dp.template dists<L2>(P, id, mask, lane);
+      if (live) keys[c0 + lane] = mkkey(d, id);
+    }
+    int p2 = 1;
+    while (p2 < s) p2 <<= 1;
+    for (int i = s + lane; i < p2; i += 32) keys[i] = kMaxKey;
+    __syncwarp();
+    warp_bitonic(keys, p2, lane);
+    uint32_t k = P.kq ? P.kq[q] : P.k_all;
+    const int m = s < static_cast<int>(k) ? s : static_cast<int>(k);
+    QueryOut* row = static_cast<QueryOut*>(P.out) + static_cast<size_t>(q) * P.k_stride;
+    for (uint32_t j = lane; j < P.k_stride; j += 32) {
+      QueryOut o;
+      if (static_cast<int>(j) < m) {
+        const uint64_t kk = keys[j];
+        o.label = P.labels[static_cast<uint32_t>(kk)];
+        o.dist = key_dist(kk);
+      } else {
+        o.label = ~0ull;
+        o.dist = __int_as_float(0x7f800000);
+      }
+      o.zero = 0;
+      row[j] = o;
+    }
+    if (P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
+    __syncwarp();
+  }
+}
+
+template <class DP, bool L2>
+cudaError_t rerank_t(const SearchParams& P, const float* inv, int blocks, cudaStream_t st) {
+  const size_t smem = 4u * P.R * 8u;
+  auto* fn = rerank_kernel<DP, L2>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  fn<<<blocks, 128, smem, st>>>(P, inv);
+  return cudaGetLastError();
+}
+
+#define HG_SEARCH_APPROX_DISPATCH(FN, PREC, L2, ...)                      \
+  switch (pdc) {                                                           \
+    case 128: return FN<sk::ApproxDist<4, 16, PREC>, L2>(__VA_ARGS__);    \
+    case 256: return FN<sk::ApproxDist<4, 32, PREC>, L2>(__VA_ARGS__);    \
+    case 512: return FN<sk::ApproxDist<2, 32, PREC>, L2>(__VA_ARGS__);    \
+    case 1024: return FN<sk::ApproxDist<1, 32, PREC>, L2>(__VA_ARGS__);   \
+    default: break;                                                        \
   }
 
 }  // namespace sk
