@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -115,6 +116,42 @@ namespace hg {
 void set_last_error(const std::string& msg) { g_err = msg; }
 }  // namespace hg
 
+// Scratch of one batch in flight.  A batch takes a free workspace and makes
+// its stream wait for the workspace's previous batch (event `done`), so
+// batches on different streams overlap on the GPU without sharing buffers.
+struct Workspace {
+  DBuf q, efq, kq, fsel, fptrs, fbits, inv, out, nres, counters;
+  DBuf work;  // [1] overflow count [2] rerun work [4] error [8+b] bucket work [32+b] bucket size
+  DBuf ovf_list, pool, bitmaps, pool_big, bitmaps_big, owners, lists, pool_ids, pool_n;
+  PinnedBuf pin_in, pin_out;
+  std::vector<cudaStream_t> aux;  // one per ef bucket
+  std::vector<cudaEvent_t> ev_join;
+  cudaEvent_t ev_fork = nullptr;
+  cudaEvent_t done = nullptr;  // recorded after the batch's last use of this workspace
+  bool busy = false;
+  void release_all() {
+    for (DBuf* d : {&q, &efq, &kq, &fsel, &fptrs, &fbits, &inv, &out, &nres, &counters, &work, &ovf_list, &pool,
+                    &bitmaps, &pool_big, &bitmaps_big, &owners, &lists, &pool_ids, &pool_n})
+      d->release();
+    pin_in.release();
+    pin_out.release();
+    for (cudaStream_t s2 : aux) cudaStreamDestroy(s2);
+    for (cudaEvent_t e2 : ev_join) cudaEventDestroy(e2);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (done) cudaEventDestroy(done);
+    aux.clear();
+    ev_join.clear();
+    ev_fork = done = nullptr;
+  }
+  uint64_t bytes() const {
+    uint64_t t = 0;
+    for (const DBuf* d : {&q, &efq, &kq, &fsel, &fptrs, &fbits, &inv, &out, &nres, &counters, &work, &ovf_list,
+                          &pool, &bitmaps, &pool_big, &bitmaps_big, &owners, &lists, &pool_ids, &pool_n})
+      t += d->bytes;
+    return t;
+  }
+};
+
 struct hgd_graph {
   int device = 0;
   int order = HGD_ORDER_AVX512;
@@ -130,19 +167,70 @@ struct hgd_graph {
   uint64_t num_deleted = 0;
   DBuf vecs, l0, up, up_blk, labels, alive;
   std::vector<uint32_t> alive_host;
-  // per call
-  DBuf q, efq, kq, fsel, fptrs, fbits, inv, out, nres, counters;
-  DBuf work;  // [0] work counter, [1] overflow count, [2] rerun work counter
-  DBuf ovf_list, pool, bitmaps, pool_big, bitmaps_big, owners, lists;
-  // compressed copies for FP16 / FP8 traversal (built on first use) and pools
-  DBuf v16, v8, vscale, pool_ids, pool_n;
+  // compressed copies for FP16 / FP8 traversal (built on first use)
+  DBuf v16, v8, vscale;
   bool has16 = false, has8 = false;
-  std::vector<cudaStream_t> aux;    // one per ef bucket
-  std::vector<cudaEvent_t> ev_join;
-  cudaEvent_t ev_fork = nullptr;
-  PinnedBuf pin_in, pin_out;
-  uint64_t pool_slots = 0, pool_cap = 0, big_slots = 0;
+  // batch scratch
+  std::mutex ws_mu;
+  std::vector<std::unique_ptr<Workspace>> ws;
+  PinnedBuf pin_patch;  // tombstone word staging
 };
+
+namespace {
+
+// Takes a workspace that no host thread is using (creating one if needed) and
+// gives it back when the call returns; GPU-side reuse is ordered by `done`.
+class WorkspaceLease {
+ public:
+  // Prefers a workspace whose previous batch has finished; otherwise opens a
+  // new one (up to kMaxWorkspaces batches in flight), else waits for the
+  // oldest.  Buffers may then be grown safely: nothing on the GPU uses them.
+  static constexpr size_t kMaxWorkspaces = 16;
+  explicit WorkspaceLease(hgd_graph* g) : g_(g) {
+    Workspace* wait_for = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(g->ws_mu);
+      for (auto& w : g->ws)
+        if (!w->busy && cudaEventQuery(w->done) == cudaSuccess) {
+          w_ = w.get();
+          break;
+        }
+      if (!w_ && g->ws.size() < kMaxWorkspaces) {
+        auto nw = std::make_unique<Workspace>();
+        if (cudaEventCreateWithFlags(&nw->done, cudaEventDisableTiming) != cudaSuccess) return;
+        w_ = nw.get();
+        g->ws.push_back(std::move(nw));
+      }
+      if (!w_)
+        for (auto& w : g->ws)
+          if (!w->busy) {
+            w_ = wait_for = w.get();
+            break;
+          }
+      if (w_) w_->busy = true;
+    }
+    if (wait_for) cudaEventSynchronize(wait_for->done);
+  }
+  ~WorkspaceLease() {
+    if (!w_) return;
+    if (st_set_) cudaEventRecord(w_->done, st_);  // after everything this call enqueued
+    std::lock_guard<std::mutex> lk(g_->ws_mu);
+    w_->busy = false;
+  }
+  Workspace* get() const { return w_; }
+  void on_stream(cudaStream_t st) {
+    st_ = st;
+    st_set_ = true;
+  }
+
+ private:
+  hgd_graph* g_;
+  Workspace* w_ = nullptr;
+  cudaStream_t st_ = nullptr;
+  bool st_set_ = false;
+};
+
+}  // namespace
 
 extern "C" {
 
@@ -270,7 +358,9 @@ int hgd_graph_set_deleted(hgd_graph* g, uint32_t id, int deleted) {
     return HGD_OK;
   }
   HG_CUDA(cudaSetDevice(g->device));
-  HG_CUDA(cudaMemcpyAsync(g->alive.as<uint32_t>() + (id >> 5), &word, 4, cudaMemcpyHostToDevice, g->stream));
+  HG_CUDA(g->pin_patch.ensure(8));
+  std::memcpy(g->pin_patch.p, &word, 4);
+  HG_CUDA(cudaMemcpyAsync(g->alive.as<uint32_t>() + (id >> 5), g->pin_patch.p, 4, cudaMemcpyHostToDevice, g->stream));
   HG_CUDA(cudaStreamSynchronize(g->stream));
   return HGD_OK;
 }
@@ -278,15 +368,15 @@ int hgd_graph_set_deleted(hgd_graph* g, uint32_t id, int deleted) {
 void hgd_graph_free(hgd_graph* g) {
   if (!g) return;
   cudaSetDevice(g->device);
-  for (DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->q, &g->efq, &g->kq, &g->fsel,
-                  &g->fptrs, &g->fbits, &g->inv, &g->out, &g->nres, &g->counters, &g->work, &g->ovf_list, &g->pool,
-                  &g->bitmaps, &g->pool_big, &g->bitmaps_big, &g->owners, &g->lists, &g->v16, &g->v8, &g->vscale, &g->pool_ids, &g->pool_n})
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  for (auto& w : g->ws) {
+    if (w->done) cudaEventSynchronize(w->done);
+    w->release_all();
+  }
+  g->ws.clear();
+  for (DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->v16, &g->v8, &g->vscale})
     d->release();
-  for (cudaStream_t s2 : g->aux) cudaStreamDestroy(s2);
-  for (cudaEvent_t e2 : g->ev_join) cudaEventDestroy(e2);
-  if (g->ev_fork) cudaEventDestroy(g->ev_fork);
-  g->pin_in.release();
-  g->pin_out.release();
+  g->pin_patch.release();
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
 }
@@ -294,11 +384,9 @@ void hgd_graph_free(hgd_graph* g) {
 uint64_t hgd_graph_device_bytes(const hgd_graph* g) {
   if (!g) return 0;
   uint64_t t = 0;
-  for (const DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->q, &g->efq, &g->kq,
-                        &g->fsel, &g->fptrs, &g->fbits, &g->inv, &g->out, &g->nres, &g->counters, &g->work,
-                        &g->ovf_list, &g->pool, &g->bitmaps, &g->pool_big, &g->bitmaps_big, &g->owners,
-                        &g->lists, &g->v16, &g->v8, &g->vscale, &g->pool_ids, &g->pool_n})
+  for (const DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->v16, &g->v8, &g->vscale})
     t += d->bytes;
+  for (const auto& w : g->ws) t += w->bytes();
   return t;
 }
 
@@ -310,9 +398,13 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   if (a->nq >= 0xFFFFFFFFull) return fail(HGD_EINVAL, "hgd_search: too many queries in one batch");
   if (a->precision > HGD_PREC_FP8) return fail(HGD_EINVAL, "hgd_search: unknown precision");
   if (a->num_filters && !a->filters) return fail(HGD_EINVAL, "hgd_search: null filter table");
-  std::lock_guard<std::mutex> lock(g->mu);
   HG_CUDA(cudaSetDevice(g->device));
   cudaStream_t st = a->stream ? static_cast<cudaStream_t>(a->stream) : g->stream;
+  WorkspaceLease lease(g);
+  Workspace* w = lease.get();
+  if (!w) return fail(HGD_ERUNTIME, "hgd_search: no workspace available (all held by calls in progress)");
+  HG_CUDA(cudaStreamWaitEvent(st, w->done, 0));  // its previous batch has finished with it
+  lease.on_stream(st);
   const uint64_t nq = a->nq;
   const uint32_t dim = static_cast<uint32_t>(g->dim);
 
@@ -337,18 +429,18 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   const uint32_t* d_ef = a->ef_per_query;
   const uint32_t* d_k = a->k_per_query;
   if (!a->queries_on_device) {
-    HG_CUDA(g->q.ensure(nq * dim * 4));
-    HG_CUDA(cudaMemcpyAsync(g->q.p, a->queries, nq * dim * 4, cudaMemcpyHostToDevice, st));
-    d_q = g->q.as<float>();
+    HG_CUDA(w->q.ensure(nq * dim * 4));
+    HG_CUDA(cudaMemcpyAsync(w->q.p, a->queries, nq * dim * 4, cudaMemcpyHostToDevice, st));
+    d_q = w->q.as<float>();
     if (a->ef_per_query) {
-      HG_CUDA(g->efq.ensure(nq * 4));
-      HG_CUDA(cudaMemcpyAsync(g->efq.p, a->ef_per_query, nq * 4, cudaMemcpyHostToDevice, st));
-      d_ef = g->efq.as<uint32_t>();
+      HG_CUDA(w->efq.ensure(nq * 4));
+      HG_CUDA(cudaMemcpyAsync(w->efq.p, a->ef_per_query, nq * 4, cudaMemcpyHostToDevice, st));
+      d_ef = w->efq.as<uint32_t>();
     }
     if (a->k_per_query) {
-      HG_CUDA(g->kq.ensure(nq * 4));
-      HG_CUDA(cudaMemcpyAsync(g->kq.p, a->k_per_query, nq * 4, cudaMemcpyHostToDevice, st));
-      d_k = g->kq.as<uint32_t>();
+      HG_CUDA(w->kq.ensure(nq * 4));
+      HG_CUDA(cudaMemcpyAsync(w->kq.p, a->k_per_query, nq * 4, cudaMemcpyHostToDevice, st));
+      d_k = w->kq.as<uint32_t>();
     }
   }
   // ---- filters -> id-space bitsets ----
@@ -359,8 +451,8 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     uint64_t label_words = 0;
     for (uint32_t f = 0; f < a->num_filters; ++f)
       if (a->filters[f].label_space) label_words += (a->filters[f].num_bits + 63) / 64;
-    HG_CUDA(g->fbits.ensure(static_cast<uint64_t>(a->num_filters) * nw * 4 + label_words * 8 + 64));
-    uint32_t* idbits = g->fbits.as<uint32_t>();
+    HG_CUDA(w->fbits.ensure(static_cast<uint64_t>(a->num_filters) * nw * 4 + label_words * 8 + 64));
+    uint32_t* idbits = w->fbits.as<uint32_t>();
     uint64_t* lw = reinterpret_cast<uint64_t*>(idbits + static_cast<uint64_t>(a->num_filters) * nw + 1);
     lw = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(lw) + 7) & ~uintptr_t(7));
     std::vector<const uint32_t*> ptrs(a->num_filters);
@@ -384,49 +476,49 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
         if (bits % 64) {
           uint64_t last = bs.words[full] & ((1ull << (bits % 64)) - 1);
           // staged through pinned memory: the source must outlive the async copy
-          HG_CUDA(g->pin_in.ensure(8));
-          std::memcpy(g->pin_in.p, &last, 8);
-          HG_CUDA(cudaMemcpyAsync(dst + 2 * full, g->pin_in.p, 8, cudaMemcpyHostToDevice, st));
+          HG_CUDA(w->pin_in.ensure(8));
+          std::memcpy(w->pin_in.p, &last, 8);
+          HG_CUDA(cudaMemcpyAsync(dst + 2 * full, w->pin_in.p, 8, cudaMemcpyHostToDevice, st));
           HG_CUDA(cudaStreamSynchronize(st));
         }
       }
     }
-    HG_CUDA(g->fptrs.ensure(a->num_filters * sizeof(void*)));
-    HG_CUDA(cudaMemcpyAsync(g->fptrs.p, ptrs.data(), a->num_filters * sizeof(void*), cudaMemcpyHostToDevice, st));
-    d_fptrs = g->fptrs.as<const uint32_t* const>();
-    HG_CUDA(g->fsel.ensure(nq * 4));
+    HG_CUDA(w->fptrs.ensure(a->num_filters * sizeof(void*)));
+    HG_CUDA(cudaMemcpyAsync(w->fptrs.p, ptrs.data(), a->num_filters * sizeof(void*), cudaMemcpyHostToDevice, st));
+    d_fptrs = w->fptrs.as<const uint32_t* const>();
+    HG_CUDA(w->fsel.ensure(nq * 4));
     if (a->filter_of_query) {
       for (uint64_t i = 0; i < nq; ++i)
         if (a->filter_of_query[i] >= static_cast<int32_t>(a->num_filters))
           return fail(HGD_EINVAL, "hgd_search: filter index out of range");
-      HG_CUDA(cudaMemcpyAsync(g->fsel.p, a->filter_of_query, nq * 4, cudaMemcpyHostToDevice, st));
+      HG_CUDA(cudaMemcpyAsync(w->fsel.p, a->filter_of_query, nq * 4, cudaMemcpyHostToDevice, st));
     } else {
-      HG_CUDA(cudaMemsetAsync(g->fsel.p, 0, nq * 4, st));
+      HG_CUDA(cudaMemsetAsync(w->fsel.p, 0, nq * 4, st));
     }
-    d_fsel = g->fsel.as<int32_t>();
+    d_fsel = w->fsel.as<int32_t>();
   }
   // ---- cosine: 1/||q|| per query ----
   const float* d_inv = nullptr;
   if (g->metric == HGD_METRIC_COSINE) {
-    HG_CUDA(g->inv.ensure(nq * 4));
-    HG_CUDA(hg::launch_inv_norm(d_q, static_cast<uint32_t>(nq), dim, g->inv.as<float>(), st));
-    d_inv = g->inv.as<float>();
+    HG_CUDA(w->inv.ensure(nq * 4));
+    HG_CUDA(hg::launch_inv_norm(d_q, static_cast<uint32_t>(nq), dim, w->inv.as<float>(), st));
+    d_inv = w->inv.as<float>();
   }
   // ---- outputs ----
   void* d_out = a->out;
   uint32_t* d_nres = a->nres;
   if (!a->out_on_device) {
-    HG_CUDA(g->out.ensure(nq * a->k * 16));
-    d_out = g->out.p;
+    HG_CUDA(w->out.ensure(nq * a->k * 16));
+    d_out = w->out.p;
     if (a->nres) {
-      HG_CUDA(g->nres.ensure(nq * 4));
-      d_nres = g->nres.as<uint32_t>();
+      HG_CUDA(w->nres.ensure(nq * 4));
+      d_nres = w->nres.as<uint32_t>();
     }
   }
   unsigned long long* d_cnt = nullptr;
   if (a->counters) {
-    HG_CUDA(g->counters.ensure(nq * hg::kCounters * 8));
-    d_cnt = g->counters.as<unsigned long long>();
+    HG_CUDA(w->counters.ensure(nq * hg::kCounters * 8));
+    d_cnt = w->counters.as<unsigned long long>();
   }
 
   // ---- launch shape ----
@@ -473,6 +565,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
                               "rounded to 128/256/512/1024");
     DBuf& vb = prec == HGD_PREC_FP16 ? g->v16 : g->v8;
     bool& have = prec == HGD_PREC_FP16 ? g->has16 : g->has8;
+    std::lock_guard<std::mutex> build_lock(g->mu);
     if (!have) {
       HG_CUDA(vb.ensure(g->n * pdc * (prec == HGD_PREC_FP16 ? 2 : 1)));
       if (prec == HGD_PREC_FP8) HG_CUDA(g->vscale.ensure(g->n * 4));
@@ -484,10 +577,10 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     P.vscale = prec == HGD_PREC_FP8 ? g->vscale.as<float>() : nullptr;
     P.pdc = pdc;
     P.pool_stride = round_up(ef_max, 32);
-    HG_CUDA(g->pool_ids.ensure(nq * P.pool_stride * 4));
-    HG_CUDA(g->pool_n.ensure(nq * 4));
-    P.pool_out = g->pool_ids.as<uint32_t>();
-    P.pool_n = g->pool_n.as<uint32_t>();
+    HG_CUDA(w->pool_ids.ensure(nq * P.pool_stride * 4));
+    HG_CUDA(w->pool_n.ensure(nq * 4));
+    P.pool_out = w->pool_ids.as<uint32_t>();
+    P.pool_n = w->pool_n.as<uint32_t>();
   }
   auto launch = [&](const hg::SearchParams& B, int blocks, int wpb, cudaStream_t sb) {
     return prec == HGD_PREC_FP32 ? hg::launch_search(B, d_inv, blocks, wpb, sb)
@@ -545,79 +638,79 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
                                         : std::min<uint64_t>(std::max<uint64_t>(g->n, 1), 16384);
   const uint32_t pool_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 1024));
   const uint32_t bm_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 2048));
-  HG_CUDA(g->pool.ensure(pool_slots * pool_cap * 8));
-  HG_CUDA(g->bitmaps.ensure(bm_slots * bw * 4));
-  HG_CUDA(g->owners.ensure((pool_slots + bm_slots) * 4));
-  HG_CUDA(g->work.ensure(64 * 4));
-  HG_CUDA(g->ovf_list.ensure(nq * 4));
-  HG_CUDA(g->lists.ensure(static_cast<uint64_t>(spec.n) * nq * 4));
-  HG_CUDA(cudaMemsetAsync(g->work.p, 0, 64 * 4, st));
-  HG_CUDA(cudaMemsetAsync(g->owners.p, 0, (pool_slots + bm_slots) * 4, st));
-  uint32_t* work = g->work.as<uint32_t>();  // [1] overflow count [2] rerun work [4] error
+  HG_CUDA(w->pool.ensure(pool_slots * pool_cap * 8));
+  HG_CUDA(w->bitmaps.ensure(bm_slots * bw * 4));
+  HG_CUDA(w->owners.ensure((pool_slots + bm_slots) * 4));
+  HG_CUDA(w->work.ensure(64 * 4));
+  HG_CUDA(w->ovf_list.ensure(nq * 4));
+  HG_CUDA(w->lists.ensure(static_cast<uint64_t>(spec.n) * nq * 4));
+  HG_CUDA(cudaMemsetAsync(w->work.p, 0, 64 * 4, st));
+  HG_CUDA(cudaMemsetAsync(w->owners.p, 0, (pool_slots + bm_slots) * 4, st));
+  uint32_t* work = w->work.as<uint32_t>();  // [1] overflow count [2] rerun work [4] error
                                             // [8+b] bucket work  [32+b] bucket size
-  P.pool = g->pool.as<uint64_t>();
+  P.pool = w->pool.as<uint64_t>();
   P.pool_cap = pool_cap;
-  P.pool_owner = g->owners.as<uint32_t>();
+  P.pool_owner = w->owners.as<uint32_t>();
   P.pool_slots = pool_slots;
-  P.bitmaps = g->bitmaps.as<uint32_t>();
+  P.bitmaps = w->bitmaps.as<uint32_t>();
   P.bitmap_words = bw;
-  P.bm_owner = g->owners.as<uint32_t>() + pool_slots;
+  P.bm_owner = w->owners.as<uint32_t>() + pool_slots;
   P.bm_slots = bm_slots;
   P.ovf_count = work + 1;
-  P.ovf_list = g->ovf_list.as<uint32_t>();
+  P.ovf_list = w->ovf_list.as<uint32_t>();
   P.err = work + 4;
   {
     cudaError_t e = hg::launch_bucket(d_ef, d_k, static_cast<uint32_t>(nq), a->ef, a->ef_default, a->k, spec,
-                                      work + 32, g->lists.as<uint32_t>(), st);
+                                      work + 32, w->lists.as<uint32_t>(), st);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("bucket kernel launch: ") + cudaGetErrorString(e));
   }
   // fork: each bucket on its own stream, largest ef first, joined back into st
-  if (g->aux.size() < spec.n) {
-    if (!g->ev_fork) HG_CUDA(cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming));
-    while (g->aux.size() < spec.n) {
+  if (w->aux.size() < spec.n) {
+    if (!w->ev_fork) HG_CUDA(cudaEventCreateWithFlags(&w->ev_fork, cudaEventDisableTiming));
+    while (w->aux.size() < spec.n) {
       cudaStream_t s2 = nullptr;
       cudaEvent_t e2 = nullptr;
       HG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
       HG_CUDA(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
-      g->aux.push_back(s2);
-      g->ev_join.push_back(e2);
+      w->aux.push_back(s2);
+      w->ev_join.push_back(e2);
     }
   }
-  HG_CUDA(cudaEventRecord(g->ev_fork, st));
+  HG_CUDA(cudaEventRecord(w->ev_fork, st));
   for (int b = static_cast<int>(spec.n) - 1; b >= 0; --b) {
     const Shape& sh = shapes[b];
-    cudaStream_t sb = g->aux[b];
-    HG_CUDA(cudaStreamWaitEvent(sb, g->ev_fork, 0));
+    cudaStream_t sb = w->aux[b];
+    HG_CUDA(cudaStreamWaitEvent(sb, w->ev_fork, 0));
     hg::SearchParams B = P;
     B.H = sh.H;
     B.R = sh.R;
     B.C = sh.C;
     B.nq_dev = work + 32 + b;
-    B.qidx = g->lists.as<uint32_t>() + static_cast<uint64_t>(b) * nq;
+    B.qidx = w->lists.as<uint32_t>() + static_cast<uint64_t>(b) * nq;
     B.work = work + 8 + b;
     B.slot_base = sh.slot_base;
     cudaError_t e = launch(B, sh.blocks, sh.wpb, sb);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("search kernel launch: ") + cudaGetErrorString(e));
-    HG_CUDA(cudaEventRecord(g->ev_join[b], sb));
+    HG_CUDA(cudaEventRecord(w->ev_join[b], sb));
   }
-  for (uint32_t b = 0; b < spec.n; ++b) HG_CUDA(cudaStreamWaitEvent(st, g->ev_join[b], 0));
+  for (uint32_t b = 0; b < spec.n; ++b) HG_CUDA(cudaStreamWaitEvent(st, w->ev_join[b], 0));
   // ---- rerun of queries that ran out of spill pool or bitmap: per-warp pool of n keys ----
   {
     const uint64_t big_slots = 32;
     const uint64_t big_cap = std::max<uint64_t>(g->n, 1);
-    HG_CUDA(g->pool_big.ensure(big_slots * big_cap * 8));
-    HG_CUDA(g->bitmaps_big.ensure(big_slots * bw * 4));
+    HG_CUDA(w->pool_big.ensure(big_slots * big_cap * 8));
+    HG_CUDA(w->bitmaps_big.ensure(big_slots * bw * 4));
     hg::SearchParams B = P;
     B.R = round_up(ef_max, 32);
     B.C = std::max<uint32_t>(128, round_up(ef_max + 32, 32));
     B.H = 4096;
     B.nq_dev = work + 1;
-    B.qidx = g->ovf_list.as<uint32_t>();
+    B.qidx = w->ovf_list.as<uint32_t>();
     B.work = work + 2;
-    B.pool = g->pool_big.as<uint64_t>();
+    B.pool = w->pool_big.as<uint64_t>();
     B.pool_cap = big_cap;
     B.pool_owner = nullptr;
-    B.bitmaps = g->bitmaps_big.as<uint32_t>();
+    B.bitmaps = w->bitmaps_big.as<uint32_t>();
     B.bm_owner = nullptr;
     B.slot_base = 0;
     B.ovf_count = work + 3;  // cannot overflow: cap = n, one bitmap per warp
@@ -642,11 +735,11 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   }
   if (a->counters)
     HG_CUDA(cudaMemcpyAsync(a->counters, d_cnt, nq * hg::kCounters * 8, cudaMemcpyDeviceToHost, st));
-  HG_CUDA(g->pin_out.ensure(8));
-  HG_CUDA(cudaMemcpyAsync(g->pin_out.p, g->work.as<uint32_t>() + 4, 4, cudaMemcpyDeviceToHost, st));
-  if (a->synchronize || !a->out_on_device || a->counters) {
+  HG_CUDA(w->pin_out.ensure(8));
+  HG_CUDA(cudaMemcpyAsync(w->pin_out.p, w->work.as<uint32_t>() + 4, 4, cudaMemcpyDeviceToHost, st));
+  if (a->synchronize || a->counters) {
     HG_CUDA(cudaStreamSynchronize(st));
-    if (*static_cast<uint32_t*>(g->pin_out.p) != 0)
+    if (*static_cast<uint32_t*>(w->pin_out.p) != 0)
       return fail(HGD_EINVAL, "hgd_search: a per-query ef or k exceeds the bound given for this batch");
   }
   return HGD_OK;

@@ -268,6 +268,53 @@ int hg_bruteforce_search_batch(const hg_bruteforce* bf, const float* qs, size_t 
 
 void hg_bruteforce_free(hg_bruteforce* bf) { delete bf; }
 
+struct hg_server {
+  hnsw::gb::Server* s;
+};
+
+int hg_server_create(const hg_index* idx, const hg_server_config* cfg, hg_server** out) {
+  return guarded([&] {
+    if (!idx || !out) throw std::invalid_argument("server: null argument");
+    hg_server_config c{};
+    if (cfg) c = *cfg;
+    *out = new hg_server{hnsw::gb::server_new(*idx->index.impl(), c)};
+  });
+}
+
+int hg_server_submit(hg_server* s, const hg_request* r, uint64_t* ticket) {
+  return guarded([&] {
+    if (!s || !r || !ticket) throw std::invalid_argument("server submit: null argument");
+    *ticket = hnsw::gb::server_submit(s->s, *r);
+  });
+}
+
+int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_ms) {
+  return guarded([&] {
+    if (!s) throw std::invalid_argument("server wait: null server");
+    hnsw::gb::server_wait(s->s, ticket, latency_ms);
+  });
+}
+
+int hg_server_replay(hg_server* s, const hg_request* reqs, const double* arrival_s, size_t n,
+                     hg_server_stats* stats) {
+  return guarded([&] {
+    if (!s || (n && (!reqs || !arrival_s)) || !stats) throw std::invalid_argument("server replay: null argument");
+    hnsw::gb::server_replay(s->s, reqs, arrival_s, n, stats);
+  });
+}
+
+int hg_server_stats_get(hg_server* s, hg_server_stats* out) {
+  return guarded([&] {
+    if (!s || !out) throw std::invalid_argument("server stats: null argument");
+    hnsw::gb::server_stats(s->s, out);
+  });
+}
+
+void hg_server_destroy(hg_server* s) {
+  if (s) hnsw::gb::server_delete(s->s);
+  delete s;
+}
+
 int hg_index_search_batch_noalloc(const hg_index* idx, const float* queries, size_t nq, size_t k, size_t ef,
                                   hg_neighbor* out, void* stream) {
   return guarded([&] {

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "hnsw/index.hpp"
+#include "hnswgpu.h"
 #include "hnswgpu_device.h"
 
 namespace hnsw::gb {
@@ -178,3 +179,44 @@ struct Index::Impl {
 };
 
 }  // namespace hnsw
+
+namespace hnsw::gb {
+
+/// Filter -> device bitset.  BitsetFilter ships its label-space words; any
+/// other filter is evaluated once per node on the host (it is a predicate on
+/// labels, so this is the same decision the reference makes lazily).
+struct FilterBits {
+  std::vector<uint64_t> owned;
+  hgd_bitset view{};
+};
+
+inline void to_bits(const Index::Impl& im, const Filter* f, FilterBits& out) {
+  if (const auto* bs = dynamic_cast<const BitsetFilter*>(f)) {
+    out.view.words = bs->words();
+    out.view.num_bits = bs->size();
+    out.view.label_space = 1;
+    return;
+  }
+  out.owned.assign((im.count + 63) / 64, 0);
+  for (std::size_t i = 0; i < im.count; ++i)
+    if (f->allowed(im.labels[i])) out.owned[i >> 6] |= 1ULL << (i & 63);
+  out.view.words = out.owned.data();
+  out.view.num_bits = im.count;
+  out.view.label_space = 0;
+}
+
+
+}  // namespace hnsw::gb
+
+namespace hnsw::gb {
+
+// continuous-batching server (server.cpp)
+class Server;
+Server* server_new(const Index::Impl& im, const hg_server_config& cfg);
+void server_delete(Server* s);
+uint64_t server_submit(Server* s, const hg_request& r);
+void server_wait(Server* s, uint64_t ticket, double* latency_ms);
+void server_replay(Server* s, const hg_request* reqs, const double* arrival_s, size_t n, hg_server_stats* out);
+void server_stats(Server* s, hg_server_stats* out);
+
+}  // namespace hnsw::gb

@@ -20,6 +20,9 @@ namespace hnsw {
 
 static_assert(sizeof(Neighbor) == 16, "device records are 16 bytes");
 
+using gb::FilterBits;
+using gb::to_bits;
+
 namespace {
 
 int order_of(simd::Isa isa) {
@@ -36,29 +39,6 @@ int order_of(simd::Isa isa) {
   const std::string msg = std::string(what) + ": " + hgd_last_error();
   if (rc == HGD_EINVAL) throw std::invalid_argument(msg);
   throw std::runtime_error(msg);
-}
-
-/// Filter -> device bitset.  BitsetFilter ships its label-space words; any
-/// other filter is evaluated once per node on the host (it is a predicate on
-/// labels, so this is the same decision the reference makes lazily).
-struct FilterBits {
-  std::vector<uint64_t> owned;
-  hgd_bitset view{};
-};
-
-void to_bits(const Index::Impl& im, const Filter* f, FilterBits& out) {
-  if (const auto* bs = dynamic_cast<const BitsetFilter*>(f)) {
-    out.view.words = bs->words();
-    out.view.num_bits = bs->size();
-    out.view.label_space = 1;
-    return;
-  }
-  out.owned.assign((im.count + 63) / 64, 0);
-  for (std::size_t i = 0; i < im.count; ++i)
-    if (f->allowed(im.labels[i])) out.owned[i >> 6] |= 1ULL << (i & 63);
-  out.view.words = out.owned.data();
-  out.view.num_bits = im.count;
-  out.view.label_space = 0;
 }
 
 }  // namespace

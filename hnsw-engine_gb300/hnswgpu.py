@@ -42,6 +42,23 @@ class _BatchOptions(C.Structure):
                 ("pool_cap", C.c_uint32), ("queries_on_device", C.c_int32), ("out_on_device", C.c_int32)]
 
 
+class _ServerConfig(C.Structure):
+    _fields_ = [("max_inflight", C.c_uint32), ("max_batch_queries", C.c_uint32), ("memory_budget", C.c_uint64),
+                ("precision", C.c_int32), ("reserved", C.c_int32)]
+
+
+class _Request(C.Structure):
+    _fields_ = [("queries", C.c_void_p), ("nq", C.c_uint32), ("k", C.c_uint32), ("ef", C.c_uint32),
+                ("reserved", C.c_uint32), ("filter", C.POINTER(_Filter)), ("out", C.c_void_p)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [("requests", C.c_uint64), ("queries", C.c_uint64), ("batches", C.c_uint64),
+                ("memory_waits", C.c_uint64), ("elapsed_s", C.c_double), ("qps", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("p999_ms", C.c_double), ("mean_ms", C.c_double),
+                ("max_ms", C.c_double), ("mean_batch_queries", C.c_double)]
+
+
 _lib = None
 
 
@@ -81,6 +98,12 @@ def lib():
         L.hg_bruteforce_search_batch.argtypes = [vp, vp, sz, sz, vp, C.POINTER(_Filter)]
         L.hg_bruteforce_free.argtypes = [vp]
         L.hg_index_search_batch_noalloc.argtypes = [vp, vp, sz, sz, sz, vp, vp]
+        L.hg_server_create.argtypes = [vp, C.POINTER(_ServerConfig), C.POINTER(vp)]
+        L.hg_server_submit.argtypes = [vp, C.POINTER(_Request), C.POINTER(C.c_uint64)]
+        L.hg_server_wait.argtypes = [vp, C.c_uint64, C.POINTER(C.c_double)]
+        L.hg_server_replay.argtypes = [vp, C.POINTER(_Request), vp, sz, C.POINTER(_ServerStats)]
+        L.hg_server_stats_get.argtypes = [vp, C.POINTER(_ServerStats)]
+        L.hg_server_destroy.argtypes = [vp]
         L.hg_set_distance_order.argtypes = [i32]
         L.hg_get_distance_order.restype = i32
         _lib = L
@@ -437,3 +460,68 @@ class BruteForceIndex:
         fh = _FilterHolder(filter)
         _check(lib().hg_bruteforce_search_batch(self._h, _ptr(q), q.shape[0], k, _ptr(out), fh.ref()))
         return out.reshape(q.shape[0], k)
+
+
+class Server:
+    """Continuous-batching server over an Index (hg_server_*): requests with their
+    own k / ef / filter are admitted into GPU batches as slots and memory free up."""
+
+    def __init__(self, index: Index, max_inflight: int = 4, max_batch_queries: int = 4096, memory_budget: int = 0,
+                 precision: int = 0):
+        self._h = None
+        self._index = index  # keep the index alive
+        cfg = _ServerConfig(max_inflight, max_batch_queries, memory_budget, precision, 0)
+        h = C.c_void_p()
+        _check(lib().hg_server_create(index._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._live = {}
+        self.dim = index.dim
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _request(self, queries, k, ef, filter, keep):
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self.dim)
+        out = np.empty(q.shape[0] * k, dtype=NEIGHBOR)
+        fh = _FilterHolder(filter)
+        keep.extend([q, out, fh])
+        r = _Request(q.ctypes.data, q.shape[0], k, ef, 0, C.pointer(fh.struct) if fh.struct is not None else None,
+                     out.ctypes.data)
+        return r, out
+
+    def submit(self, queries, k: int, ef: int = 0, filter=None) -> int:
+        keep = []
+        r, out = self._request(queries, k, ef, filter, keep)
+        t = C.c_uint64()
+        _check(lib().hg_server_submit(self._h, C.byref(r), C.byref(t)))
+        self._live[t.value] = (keep, out, k)
+        return t.value
+
+    def wait(self, ticket: int):
+        lat = C.c_double()
+        try:
+            _check(lib().hg_server_wait(self._h, ticket, C.byref(lat)))
+        finally:
+            keep, out, k = self._live.pop(ticket, (None, None, 1))
+        return out.reshape(-1, k), lat.value
+
+    def replay(self, requests, arrivals_s):
+        """requests: list of (queries, k, ef, filter); arrivals_s: seconds from the
+        call.  Returns (stats dict, list of result record arrays)."""
+        keep, outs = [], []
+        arr = (_Request * len(requests))()
+        for i, (q, k, ef, f) in enumerate(requests):
+            r, out = self._request(q, k, ef, f, keep)
+            arr[i] = r
+            outs.append((out, k))
+        at = np.ascontiguousarray(arrivals_s, dtype=np.float64)
+        st = _ServerStats()
+        _check(lib().hg_server_replay(self._h, arr, at.ctypes.data, len(requests), C.byref(st)))
+        stats = {f: getattr(st, f) for f, _ in _ServerStats._fields_}
+        return stats, [o.reshape(-1, k) for o, k in outs]
+

@@ -145,6 +145,47 @@ void hg_bruteforce_free(hg_bruteforce* bf);
 int hg_index_search_batch_noalloc(const hg_index* idx, const float* queries, size_t nq, size_t k, size_t ef,
                                   hg_neighbor* out, void* stream);
 
+/* Continuous-batching server over one index (an addition; the reference has
+ * no serving loop).  Requests -- a block of queries with their own k, ef and
+ * optional filter -- are queued and admitted into GPU batches as batch slots
+ * and the device-memory budget allow; batches in flight overlap on the GPU.
+ * A request's results do not depend on the requests it is batched with.
+ * The query, output and filter memory of a request must stay valid until
+ * hg_server_wait returns for it (or hg_server_replay returns). */
+typedef struct hg_server hg_server;
+typedef struct {
+  uint32_t max_inflight;       /* batches on the GPU at once (1..15, default 4) */
+  uint32_t max_batch_queries;  /* queries admitted into one batch (default 4096) */
+  uint64_t memory_budget;      /* device bytes for batches in flight; 0 = half the free memory */
+  int32_t precision;           /* 0 fp32; 1 fp16; 2 fp8 traversal + exact fp32 rerank */
+  int32_t reserved;
+} hg_server_config;
+typedef struct {
+  const float* queries;        /* nq x dim */
+  uint32_t nq;
+  uint32_t k;
+  uint32_t ef;                 /* 0 = the index's set_ef value */
+  uint32_t reserved;
+  const hg_filter* filter;     /* NULL = none */
+  hg_neighbor* out;            /* nq x k, padded like search_batch */
+} hg_request;
+typedef struct {
+  uint64_t requests, queries, batches, memory_waits;
+  double elapsed_s, qps;       /* first arrival to last completion */
+  double p50_ms, p99_ms, p999_ms, mean_ms, max_ms;  /* request latency, arrival to completion */
+  double mean_batch_queries;
+} hg_server_stats;
+
+int hg_server_create(const hg_index* idx, const hg_server_config* cfg, hg_server** out);
+int hg_server_submit(hg_server* s, const hg_request* r, uint64_t* ticket);
+int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_ms);
+/* Submits request i at arrival_s[i] seconds after the call (an open-loop
+ * load), waits for all and reports these requests' statistics. */
+int hg_server_replay(hg_server* s, const hg_request* reqs, const double* arrival_s, size_t n,
+                     hg_server_stats* stats);
+int hg_server_stats_get(hg_server* s, hg_server_stats* out);
+void hg_server_destroy(hg_server* s);
+
 /* Distance summation order for indexes created or loaded afterwards. */
 int hg_set_distance_order(int order);
 int hg_get_distance_order(void);

@@ -99,7 +99,8 @@ typedef struct {
   uint32_t* nres;                /* nullable: per-query result count (no padding) */
   void* stream;                  /* cudaStream_t; NULL = the graph's stream */
   uint64_t* counters;            /* nullable host array, nq x HGD_NCOUNTERS */
-  int32_t synchronize;           /* 1: return after the results are in `out` */
+  int32_t synchronize;           /* 1: return after the results are in `out`; 0: only enqueue on
+                                    `stream` (host buffers must then be pinned and stay alive) */
   int32_t reserved2;
   /* launch shape; 0 = chosen from ef (the autotuner's table) */
   uint32_t hash_slots;           /* visited hash per warp (power of two >= 256) */
