@@ -261,7 +261,122 @@ def run_ours(args, rank, world, local):
     }
     if rank == 0 and world == 1:
         result["cpu_baseline"] = cpu_baseline(gpath, queries, efs)
+        if not args.no_serving:
+            del ix
+            result["serving"] = run_serving(local)
     return result
+
+
+SERVE_N, SERVE_CLUSTERS, SERVE_REQUESTS = 1_000_000, 1024, 20_000
+SERVE_LOADS = (0.25, 0.5, 0.75, 1.0)
+SERVE_FILTERS = 16  # pool of distinct random 10%-density bitsets
+SERVE_RECALL_REQUESTS = 2000
+
+
+def serving_workload():
+    """Serving at 1M: 20,000 requests, log-uniform 1..256 queries each (seed 1
+    mixture), k in {1,10,100}, ef in {16,32,..,512}, 20% with a bitset filter."""
+    import workloads
+
+    r = np.random.default_rng(4)
+    nqs = np.minimum(np.floor(np.exp(r.uniform(0.0, np.log(257.0), SERVE_REQUESTS))), 256).astype(np.int64)
+    ks = r.choice(np.array([1, 10, 100]), SERVE_REQUESTS)
+    efs = r.choice(np.arange(16, 513, 16), SERVE_REQUESTS)
+    fsel = np.where(r.random(SERVE_REQUESTS) < 0.2, r.integers(0, SERVE_FILTERS, SERVE_REQUESTS), -1)
+    base, queries = workloads.int_mixture(SERVE_N, DIM, SERVE_CLUSTERS, int(nqs.sum()))
+    rf = np.random.default_rng(5)
+    masks = [rf.random(SERVE_N) < 0.1 for _ in range(SERVE_FILTERS)]
+    return base, queries, nqs, ks, efs, fsel, masks
+
+
+def run_serving(local):
+    """The served, batched search at 1M (FP8-E4M3 traversal + exact FP32 rerank,
+    and plain FP32) next to one plain FP32 search_batch over the same queries."""
+    import hnswgpu
+    import workloads
+
+    base, queries, nqs, ks, efs, fsel, masks = serving_workload()
+    t0 = time.time()
+    ix = hnswgpu.Index(DIM, "l2", M, EFC)
+    ix.add(base, num_threads=0)
+    build_s = time.time() - t0
+    ix.set_device(local)
+    bitsets = [hnswgpu.Bitset(workloads.mask_to_words(m), SERVE_N) for m in masks]
+    offs = np.concatenate([[0], np.cumsum(nqs)])
+    total_q = int(offs[-1])
+    req_rows = np.repeat(np.arange(SERVE_REQUESTS), nqs)
+    kq, efq, fq = ks[req_rows], efs[req_rows], fsel[req_rows]
+    requests = [(queries[offs[i]:offs[i + 1]], int(ks[i]), int(efs[i]), bitsets[fsel[i]] if fsel[i] >= 0 else None)
+                for i in range(SERVE_REQUESTS)]
+
+    # plain FP32 search_batch over all queries, per-query ef / k / filter, in
+    # 65,536-query calls (host buffers in and out)
+    chunk = 65536
+    plain = np.empty((total_q, 100), dtype=hnswgpu.NEIGHBOR)
+    for rep in range(2):  # the first pass mirrors the graph and warms up
+        t = time.perf_counter()
+        for s in range(0, total_q, chunk):
+            e = min(s + chunk, total_q)
+            plain[s:e] = ix.search_batch_ex(queries[s:e], 100, ef_per_query=efq[s:e], k_per_query=kq[s:e],
+                                            filters=bitsets, filter_of_query=fq[s:e]).reshape(e - s, 100)
+        plain_s = time.perf_counter() - t
+    plain_qps = total_q / plain_s
+
+    # recall against exact k-NN (brute force on the GPU, exact on integer data)
+    # over the first requests, per filter group
+    sample_q = int(offs[SERVE_RECALL_REQUESTS])
+    bf = hnswgpu.BruteForceIndex(DIM, "l2")
+    bf.add(base)
+    gt = np.empty((sample_q, 100), dtype=np.int64)
+    for f in range(-1, SERVE_FILTERS):
+        sel = np.nonzero(fq[:sample_q] == f)[0]
+        if sel.size:
+            gt[sel] = bf.search_raw(queries[sel], 100, filter=masks[f] if f >= 0 else None)["label"]
+    del bf
+
+    def recall(labels_of_query):
+        r_all, r10, n10 = 0.0, 0.0, 0
+        for q in range(sample_q):
+            k = int(kq[q])
+            got = labels_of_query(q, k)
+            r_all += len(np.intersect1d(got, gt[q, :k])) / k
+            if k >= 10:
+                r10 += len(np.intersect1d(got[:10], gt[q, :10])) / 10
+                n10 += 1
+        return round(r_all / sample_q, 4), round(r10 / max(n10, 1), 4)
+
+    plain_recall = recall(lambda q, k: plain[q, :k]["label"].astype(np.int64))
+    out = {"workload": f"serving-L2-1M: n={SERVE_N} d={DIM} M={M} efC={EFC}, {SERVE_REQUESTS} requests, "
+                       f"{total_q} queries, 1..256 queries/request log-uniform, k in {{1,10,100}}, "
+                       f"ef in {{16..512 step 16}}, 20% with a 10%-density bitset (pool of {SERVE_FILTERS})",
+           "build_s": round(build_s, 1), "queries": total_q,
+           "plain_fp32_search_batch": {"qps": round(plain_qps, 1), "recall_at_k": plain_recall[0],
+                                       "recall_at_10": plain_recall[1], "calls_of": chunk}}
+    for name, prec in (("fp32", 0), ("fp8_rerank", 2)):
+        srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, precision=prec)
+        srv.replay(requests[:2000], np.zeros(2000))  # warm-up: encodes the FP8 copy, sizes the staging
+        peak, outs = srv.replay(requests, np.zeros(SERVE_REQUESTS))
+        same = all(np.array_equal(outs[i]["label"], plain[offs[i]:offs[i + 1], :ks[i]]["label"])
+                   for i in range(SERVE_REQUESTS)) if prec == 0 else None
+        rec = recall(lambda q, k: outs[req_rows[q]][q - offs[req_rows[q]], :k]["label"].astype(np.int64))
+        form = {"peak_qps": round(peak["qps"], 1), "recall_at_k": rec[0], "recall_at_10": rec[1],
+                "peak_p50_ms": round(peak["p50_ms"], 3), "peak_mean_batch_queries": round(peak["mean_batch_queries"], 1),
+                "loads": []}
+        if same is not None:
+            form["identical_to_plain_search_batch"] = bool(same)
+        mean_q = total_q / SERVE_REQUESTS
+        for load in SERVE_LOADS:
+            rate = load * peak["qps"] / mean_q  # requests per second
+            arrivals = np.cumsum(np.random.default_rng(6).exponential(1.0 / rate, SERVE_REQUESTS))
+            st, _ = srv.replay(requests, arrivals)
+            form["loads"].append({"offered": load, "offered_qps": round(load * peak["qps"], 1),
+                                  "qps": round(st["qps"], 1), "p50_ms": round(st["p50_ms"], 3),
+                                  "p99_ms": round(st["p99_ms"], 3), "p999_ms": round(st["p999_ms"], 3),
+                                  "mean_batch_queries": round(st["mean_batch_queries"], 1)})
+        srv.close()
+        out[name] = form
+    out["served_fp8_over_plain_fp32"] = round(out["fp8_rerank"]["peak_qps"] / plain_qps, 3)
+    return out
 
 
 def cpu_baseline(gpath, queries, efs, sample=None):
@@ -319,6 +434,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-serving", action="store_true", help="skip the 1M serving measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

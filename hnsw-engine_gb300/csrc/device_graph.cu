@@ -122,7 +122,7 @@ void set_last_error(const std::string& msg) { g_err = msg; }
 struct Workspace {
   DBuf q, efq, kq, fsel, fptrs, fbits, inv, out, nres, counters;
   DBuf work;  // [1] overflow count [2] rerun work [4] error [8+b] bucket work [32+b] bucket size
-  DBuf ovf_list, pool, bitmaps, pool_big, bitmaps_big, owners, lists, pool_ids, pool_n;
+  DBuf ovf_list, pool, pool_t2, bitmaps, pool_big, bitmaps_big, owners, lists, pool_ids, pool_n;
   PinnedBuf pin_in, pin_out;
   std::vector<cudaStream_t> aux;  // one per ef bucket
   std::vector<cudaEvent_t> ev_join;
@@ -130,7 +130,7 @@ struct Workspace {
   cudaEvent_t done = nullptr;  // recorded after the batch's last use of this workspace
   bool busy = false;
   void release_all() {
-    for (DBuf* d : {&q, &efq, &kq, &fsel, &fptrs, &fbits, &inv, &out, &nres, &counters, &work, &ovf_list, &pool,
+    for (DBuf* d : {&q, &efq, &kq, &fsel, &fptrs, &fbits, &inv, &out, &nres, &counters, &work, &ovf_list, &pool, &pool_t2,
                     &bitmaps, &pool_big, &bitmaps_big, &owners, &lists, &pool_ids, &pool_n})
       d->release();
     pin_in.release();
@@ -146,7 +146,7 @@ struct Workspace {
   uint64_t bytes() const {
     uint64_t t = 0;
     for (const DBuf* d : {&q, &efq, &kq, &fsel, &fptrs, &fbits, &inv, &out, &nres, &counters, &work, &ovf_list,
-                          &pool, &bitmaps, &pool_big, &bitmaps_big, &owners, &lists, &pool_ids, &pool_n})
+                          &pool, &pool_t2, &bitmaps, &pool_big, &bitmaps_big, &owners, &lists, &pool_ids, &pool_n})
       t += d->bytes;
     return t;
   }
@@ -635,17 +635,31 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   // shared scratch: spill pools and visited bitmaps acquired per query
   const uint64_t bw = (g->n + 31) / 32 + 1;
   const uint64_t pool_cap = a->pool_cap ? std::max<uint64_t>(a->pool_cap, 32)
-                                        : std::min<uint64_t>(std::max<uint64_t>(g->n, 1), 16384);
-  const uint32_t pool_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 1024));
-  const uint32_t bm_slots = static_cast<uint32_t>(std::min<uint64_t>(slots_total, 2048));
+                                        : std::min<uint64_t>(std::max<uint64_t>(g->n, 1), 8192);
+  // Bitmaps and first-tier pools: one per warp that can be resident at once
+  // (every warp keeps at least the smallest shape's shared memory), so
+  // acquisition does not fail unless a memory cap binds.  The first tier
+  // holds 8K keys; queries whose candidate queue outgrows it (filtered
+  // searches: every visited node enters the queue until ef eligible results
+  // are found) move to a second tier of up to 2^18 keys.
+  const uint64_t resident = static_cast<uint64_t>(g->sms) * std::min<uint64_t>(64, (228u * 1024u) / hg::warp_smem_bytes(1024, 32, 128));
+  const uint32_t pool_slots = static_cast<uint32_t>(
+      std::max<uint64_t>(1, std::min<uint64_t>({slots_total, resident, hg::kPoolBytesCap / (pool_cap * 8)})));
+  const uint32_t bm_slots = static_cast<uint32_t>(
+      std::max<uint64_t>(1, std::min<uint64_t>({slots_total, resident, hg::kBitmapBytesCap / (bw * 4)})));
+  const uint64_t big_cap = a->pool_cap ? 0 : std::min<uint64_t>(std::max<uint64_t>(g->n, 1), uint64_t{1} << 18);
+  const uint32_t big_slots = big_cap <= pool_cap ? 0u
+                             : static_cast<uint32_t>(std::max<uint64_t>(
+                                   1, std::min<uint64_t>({slots_total, resident, hg::kBigPoolBytesCap / (big_cap * 8)})));
   HG_CUDA(w->pool.ensure(pool_slots * pool_cap * 8));
   HG_CUDA(w->bitmaps.ensure(bm_slots * bw * 4));
-  HG_CUDA(w->owners.ensure((pool_slots + bm_slots) * 4));
+  if (big_slots) HG_CUDA(w->pool_t2.ensure(big_slots * big_cap * 8));
+  HG_CUDA(w->owners.ensure((pool_slots + bm_slots + big_slots) * 4));
   HG_CUDA(w->work.ensure(64 * 4));
   HG_CUDA(w->ovf_list.ensure(nq * 4));
   HG_CUDA(w->lists.ensure(static_cast<uint64_t>(spec.n) * nq * 4));
   HG_CUDA(cudaMemsetAsync(w->work.p, 0, 64 * 4, st));
-  HG_CUDA(cudaMemsetAsync(w->owners.p, 0, (pool_slots + bm_slots) * 4, st));
+  HG_CUDA(cudaMemsetAsync(w->owners.p, 0, (pool_slots + bm_slots + big_slots) * 4, st));
   uint32_t* work = w->work.as<uint32_t>();  // [1] overflow count [2] rerun work [4] error
                                             // [8+b] bucket work  [32+b] bucket size
   P.pool = w->pool.as<uint64_t>();
@@ -656,6 +670,10 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   P.bitmap_words = bw;
   P.bm_owner = w->owners.as<uint32_t>() + pool_slots;
   P.bm_slots = bm_slots;
+  P.big_pool = big_slots ? w->pool_t2.as<uint64_t>() : nullptr;
+  P.big_cap = big_cap;
+  P.big_owner = big_slots ? w->owners.as<uint32_t>() + pool_slots + bm_slots : nullptr;
+  P.big_slots = big_slots;
   P.ovf_count = work + 1;
   P.ovf_list = w->ovf_list.as<uint32_t>();
   P.err = work + 4;
@@ -696,10 +714,10 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   for (uint32_t b = 0; b < spec.n; ++b) HG_CUDA(cudaStreamWaitEvent(st, w->ev_join[b], 0));
   // ---- rerun of queries that ran out of spill pool or bitmap: per-warp pool of n keys ----
   {
-    const uint64_t big_slots = 32;
-    const uint64_t big_cap = std::max<uint64_t>(g->n, 1);
-    HG_CUDA(w->pool_big.ensure(big_slots * big_cap * 8));
-    HG_CUDA(w->bitmaps_big.ensure(big_slots * bw * 4));
+    const uint64_t rerun_slots = 32;
+    const uint64_t rerun_cap = std::max<uint64_t>(g->n, 1);
+    HG_CUDA(w->pool_big.ensure(rerun_slots * rerun_cap * 8));
+    HG_CUDA(w->bitmaps_big.ensure(rerun_slots * bw * 4));
     hg::SearchParams B = P;
     B.R = round_up(ef_max, 32);
     B.C = std::max<uint32_t>(128, round_up(ef_max + 32, 32));
@@ -708,8 +726,11 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     B.qidx = w->ovf_list.as<uint32_t>();
     B.work = work + 2;
     B.pool = w->pool_big.as<uint64_t>();
-    B.pool_cap = big_cap;
+    B.pool_cap = rerun_cap;
     B.pool_owner = nullptr;
+    B.big_owner = nullptr;
+    B.big_pool = nullptr;
+    B.big_slots = 0;
     B.bitmaps = w->bitmaps_big.as<uint32_t>();
     B.bm_owner = nullptr;
     B.slot_base = 0;
@@ -717,7 +738,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     B.rerun = 1;
     const uint32_t wb = hg::warp_smem_bytes(B.H, B.R, B.C);
     if (wb > 227u * 1024u) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
-    cudaError_t e = launch(B, static_cast<int>(big_slots), 1, st);
+    cudaError_t e = launch(B, static_cast<int>(rerun_slots), 1, st);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("rerun kernel launch: ") + cudaGetErrorString(e));
   }
   // ---- exact FP32 rerank of the traversal pools ----

@@ -204,13 +204,14 @@ class Server {
   }
 
  private:
-  // Device bytes one batch needs beyond the resident graph: queries, per-query
-  // arrays and results, ef-bucket lists, rerank pools, spill pools and visited
-  // bitmaps (the workspace's shared scratch).
+  // Device bytes one batch needs beyond the resident graph (an upper bound):
+  // queries, per-query arrays and results, ef-bucket lists, rerank pools, the
+  // two spill-pool tiers, visited bitmaps and the rerun pass's scratch.
   uint64_t batch_bytes(uint64_t nq, uint32_t kstride, uint32_t ef_max) const {
     const uint64_t per_q = uint64_t{dim_} * 4 + uint64_t{kstride} * 16 + 64 + 12 * 4 + 4 * ((ef_max + 31) / 32 * 32);
-    const uint64_t pool = 1024ull * std::min<uint64_t>(std::max<uint64_t>(n_, 1), 16384) * 8;
-    const uint64_t bitmaps = 2048ull * ((n_ + 31) / 32 + 1) * 4;
+    const uint64_t pool = std::min<uint64_t>(1ull << 30, 152ull * 64 * std::min<uint64_t>(std::max<uint64_t>(n_, 1), 8192) * 8) +
+                          (2ull << 30);
+    const uint64_t bitmaps = std::min<uint64_t>(1ull << 30, 152ull * 64 * ((n_ + 31) / 32 + 1) * 4);
     const uint64_t rerun = 32ull * (std::max<uint64_t>(n_, 1) * 8 + ((n_ + 31) / 32 + 1) * 4);
     return per_q * nq + pool + bitmaps + rerun;
   }

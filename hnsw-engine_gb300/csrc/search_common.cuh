@@ -6,7 +6,11 @@ namespace hg {
 
 constexpr uint32_t kNoId = 0xFFFFFFFFu;
 constexpr int kCounters = 8;
-enum : uint32_t { kTierBitmap = 1u, kTierPool = 2u, kTierRerun = 4u };
+constexpr uint64_t kBitmapBytesCap = 1ull << 30;   // visited bitmaps per workspace
+constexpr uint64_t kPoolBytesCap = 1ull << 30;     // first-tier pools per workspace
+constexpr uint64_t kBigPoolBytesCap = 2ull << 30;  // second-tier pools per workspace
+constexpr uint32_t kBigPoolTries = 8192;  // bounded wait (~2 us steps) for a second-tier pool
+enum : uint32_t { kTierBitmap = 1u, kTierPool = 2u, kTierRerun = 4u, kTierPool2 = 8u };
 
 // Everything one launch of the query kernel reads.  Device pointers unless noted.
 struct SearchParams {
@@ -49,6 +53,10 @@ struct SearchParams {
   uint64_t pool_cap;
   uint32_t* pool_owner;     // [pool_slots] 0 = free
   uint32_t pool_slots;
+  uint64_t* big_pool;       // second pool tier: big_cap keys each (null: none)
+  uint64_t big_cap;
+  uint32_t* big_owner;      // [big_slots] 0 = free
+  uint32_t big_slots;
   uint32_t* bitmaps;        // visited bitmaps, bitmap_words each
   uint64_t bitmap_words;
   uint32_t* bm_owner;       // [bm_slots] 0 = free

@@ -451,6 +451,7 @@ struct Warp {
   uint32_t* bitmap;   // visited bitmap in use
   uint64_t slot;      // global warp slot
   int pool_idx;       // acquired shared pool (-1 none)
+  int big_idx;        // acquired second-tier pool (-1 none)
   int bm_idx;         // acquired shared bitmap (-1 none)
   uint32_t hmask;
   int hshift;
@@ -460,21 +461,25 @@ struct Warp {
 };
 
 // Claim a free entry of a shared scratch array: one bounded pass over the
-// owner flags from a slot-dependent start (never waits).  -1 if all are taken.
+// owner flags from a slot-dependent start, 32 flags per step (never waits).
+// -1 if all are taken.
 __device__ __forceinline__ int acquire(uint32_t* owner, uint32_t nslots, uint64_t slot, int lane) {
-  int got = -1;
-  if (lane == 0) {
-    const uint32_t start = static_cast<uint32_t>((slot * 2654435761ull) % nslots);
-    for (uint32_t t = 0; t < nslots; ++t) {
-      uint32_t i = start + t;
-      if (i >= nslots) i -= nslots;
-      if (atomicCAS(owner + i, 0u, 1u) == 0u) {
-        got = static_cast<int>(i);
-        break;
-      }
+  const uint32_t start = static_cast<uint32_t>((slot * 2654435761ull) % nslots);
+  for (uint32_t t = 0; t < nslots; t += 32) {
+    uint32_t i = start + t + static_cast<uint32_t>(lane);
+    if (i >= nslots) i -= nslots;
+    const bool open = t + static_cast<uint32_t>(lane) < nslots &&
+                      *reinterpret_cast<volatile const uint32_t*>(owner + i) == 0u;
+    uint32_t b = __ballot_sync(kFull, open);
+    while (b) {
+      const int l = __ffs(b) - 1;
+      b &= b - 1;
+      int got = 0;
+      if (lane == l) got = atomicCAS(owner + i, 0u, 1u) == 0u;
+      if (__shfl_sync(kFull, got, l)) return static_cast<int>(__shfl_sync(kFull, i, l));
     }
   }
-  return __shfl_sync(kFull, got, 0);
+  return -1;
 }
 
 // Give back the shared scratch a query held (its writes are complete first).
@@ -483,9 +488,11 @@ __device__ __forceinline__ void release_scratch(Warp& w, const SearchParams& P, 
   __threadfence();
   if (lane == 0) {
     if (w.pool_idx >= 0) atomicExch(P.pool_owner + w.pool_idx, 0u);
+    if (w.big_idx >= 0) atomicExch(P.big_owner + w.big_idx, 0u);
     if (w.bm_idx >= 0) atomicExch(P.bm_owner + w.bm_idx, 0u);
   }
   w.pool_idx = -1;
+  w.big_idx = -1;
   w.bm_idx = -1;
   w.pool = nullptr;
 }
@@ -605,12 +612,44 @@ struct Cands {
   bool spilled;   // the pool was used
 };
 
+// Move a pool of pn keys to the second tier (capacity big_cap); returns the
+// entry taken or -1.  Holders of second-tier entries wait on nothing, so the
+// bounded wait for a free entry ends; past the bound the query goes to the
+// rerun pass.  Plain arguments keep the caller's state in registers.
+static __device__ __noinline__ int promote_pool(uint64_t* big_pool, uint64_t big_cap, uint32_t* big_owner,
+                                                uint32_t big_slots, const uint64_t* src, uint64_t pn, uint64_t slot,
+                                                int lane) {
+  int i = -1;
+  for (uint32_t tries = 0; tries < kBigPoolTries; ++tries) {
+    i = acquire(big_owner, big_slots, slot, lane);
+    if (i >= 0) break;
+    __nanosleep(2000);
+  }
+  if (i < 0) return -1;
+  uint64_t* big = big_pool + static_cast<uint64_t>(i) * big_cap;
+  for (uint64_t j = lane; j < pn; j += 32) big[j] = src[j];
+  __syncwarp();
+  __threadfence();
+  return i;
+}
+
 __device__ __forceinline__ bool pool_append(Warp& w, Cands& c, const SearchParams& P, const uint64_t* src, int cnt,
                                             int lane) {
   if (cnt <= 0) return true;
-  if (c.pn + static_cast<uint64_t>(cnt) > P.pool_cap) {
-    c.overflow = true;
-    return false;
+  const uint64_t cap = w.big_idx >= 0 ? P.big_cap : P.pool_cap;
+  if (c.pn + static_cast<uint64_t>(cnt) > cap) {
+    const int i = (w.big_idx >= 0 || P.big_owner == nullptr || c.pn + static_cast<uint64_t>(cnt) > P.big_cap ||
+                   w.pool == nullptr)
+                      ? -1
+                      : promote_pool(P.big_pool, P.big_cap, P.big_owner, P.big_slots, w.pool, c.pn, w.slot, lane);
+    if (i < 0) {
+      c.overflow = true;
+      return false;
+    }
+    if (lane == 0 && w.pool_idx >= 0) atomicExch(P.pool_owner + w.pool_idx, 0u);
+    w.pool_idx = -1;
+    w.big_idx = i;
+    w.pool = P.big_pool + static_cast<uint64_t>(i) * P.big_cap;
   }
   if (w.pool == nullptr) {
     if (P.pool_owner) {
@@ -771,6 +810,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
   w.pool = nullptr;
   w.bitmap = nullptr;
   w.pool_idx = -1;
+  w.big_idx = -1;
   w.bm_idx = -1;
   w.hmask = P.H - 1;
   w.hshift = 32 - (31 - __clz(P.H));
@@ -962,9 +1002,15 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
           n_visit += nu;
           if (!U) continue;
           n_dists += nu;
+          // eligibility words load while the rows are gathered
+          uint32_t ew = ~0u;
+          if (filtered && fresh) {
+            const uint32_t aw = __ldg(P.alive + (id >> 5));
+            const uint32_t fw = fb ? __ldg(fb + (id >> 5)) : ~0u;
+            ew = aw & fw;
+          }
           const float d = dp.template dists<L2>(P, id, U, lane);
-          bool elig = true;
-          if (filtered && fresh) elig = bit_of(P.alive, id) && (!fb || bit_of(fb, id));
+          const bool elig = ((ew >> (id & 31u)) & 1u) != 0;
           const uint64_t key = mkkey(d, id);
 
           // ---- in-order acceptance replay (search_layer.cpp:112-132) ----
@@ -1019,6 +1065,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
     }
 
     const bool used_bitmap = w.bitmap_mode;
+    const bool used_pool2 = w.big_idx >= 0;
     release_scratch(w, P, lane);
     if (c.overflow) {
       if (lane == 0) {
@@ -1062,7 +1109,8 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       cp[4] = n_visit;
       cp[5] = c.peak;
       cp[6] = static_cast<unsigned long long>(s);
-      cp[7] = (used_bitmap ? kTierBitmap : 0u) | (c.spilled ? kTierPool : 0u) | (P.rerun ? kTierRerun : 0u);
+      cp[7] = (used_bitmap ? kTierBitmap : 0u) | (c.spilled ? kTierPool : 0u) | (P.rerun ? kTierRerun : 0u) |
+              (used_pool2 ? kTierPool2 : 0u);
     }
     __syncwarp();
   }

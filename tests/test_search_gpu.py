@@ -182,6 +182,32 @@ def test_tiers_keep_results_exact(hg, oracle, graphs):
             assert tiers & 2, "spill pool not reached"
 
 
+def test_second_pool_tier_keeps_results_exact(hg, oracle, tmp_path):
+    """A 0.5%-density filter at ef=300 on 100,000 nodes: until 300 eligible
+    results are found every visited node joins the candidate queue, which
+    outgrows the 8K-key first pool tier; the queries must move to the second
+    tier (not the rerun pass) and answer exactly as the oracle."""
+    import workloads
+
+    base, q = workloads.int_mixture(100_000, 16, 32, 48)
+    ix = hg.Index(16, "l2", 8, 64)
+    ix.add(base, num_threads=0)
+    p = tmp_path / "tier2.idx"
+    ix.save(p)
+    ix = hg.Index.load(p)
+    ox = oracle.OracleIndex(p)
+    fw = workloads.label_filter_bits(100_000, lambda l: l % 200 == 0)
+    fsel = np.zeros(q.shape[0], dtype=np.int32)
+    ol, od, ocnt = ox.search_batch(q, 10, 300, filters=[(fw, 100_000)], fsel=fsel, counters=True)
+    rec, cnt = ix.search_batch_ex(q, 10, 300, filters=[hg.Bitset(fw, 100_000)], filter_of_query=fsel, counters=True)
+    _eq_oracle(rec, ol, od, "second pool tier")
+    assert int(ocnt[:, 5].max()) > 8192, "workload too small to leave the first tier"
+    assert (cnt[:, 7] & 8).any(), "second pool tier not reached"
+    assert not (cnt[:, 7] & 4).any(), "rerun pass used"
+    for col in (2, 3, 4, 6):  # layer-0 lists, distances, visited, results
+        np.testing.assert_array_equal(cnt[:, col], ocnt[:, col], err_msg=f"counter {col}")
+
+
 def test_batch_equals_sequential(hg, graphs):
     _, q, *_ = graphs.data("c1")
     ix = hg.Index.load(graphs.path("c1"))
