@@ -271,6 +271,7 @@ SERVE_N, SERVE_CLUSTERS, SERVE_REQUESTS = 1_000_000, 1024, 20_000
 SERVE_LOADS = (0.25, 0.5, 0.75, 1.0)
 SERVE_FILTERS = 16  # pool of distinct random 10%-density bitsets
 SERVE_RECALL_REQUESTS = 2000
+SERVE_PLAIN_REQUESTS = 2000
 
 
 def serving_workload():
@@ -309,8 +310,18 @@ def run_serving(local):
     requests = [(queries[offs[i]:offs[i + 1]], int(ks[i]), int(efs[i]), bitsets[fsel[i]] if fsel[i] >= 0 else None)
                 for i in range(SERVE_REQUESTS)]
 
-    # plain FP32 search_batch over all queries, per-query ef / k / filter, in
-    # 65,536-query calls (host buffers in and out)
+    # plain FP32 search_batch, the reference's call: one call per request (its
+    # own k, ef and filter), one after another, on a sample of the requests
+    for i in range(200):
+        ix.search_raw(*requests[i])
+    t = time.perf_counter()
+    for i in range(SERVE_PLAIN_REQUESTS):
+        ix.search_raw(*requests[i])
+    per_request_s = time.perf_counter() - t
+    per_request_qps = int(offs[SERVE_PLAIN_REQUESTS]) / per_request_s
+
+    # batched FP32: all queries with per-query ef / k / filter in 65,536-query
+    # calls (host buffers in and out)
     chunk = 65536
     plain = np.empty((total_q, 100), dtype=hnswgpu.NEIGHBOR)
     for rep in range(2):  # the first pass mirrors the graph and warms up
@@ -350,8 +361,11 @@ def run_serving(local):
                        f"{total_q} queries, 1..256 queries/request log-uniform, k in {{1,10,100}}, "
                        f"ef in {{16..512 step 16}}, 20% with a 10%-density bitset (pool of {SERVE_FILTERS})",
            "build_s": round(build_s, 1), "queries": total_q,
-           "plain_fp32_search_batch": {"qps": round(plain_qps, 1), "recall_at_k": plain_recall[0],
-                                       "recall_at_10": plain_recall[1], "calls_of": chunk}}
+           "plain_fp32_search_batch_per_request": {
+               "qps": round(per_request_qps, 1), "requests": SERVE_PLAIN_REQUESTS,
+               "note": "one search_batch call per request (the reference API: one k / ef / filter per call)"},
+           "batched_fp32_search_batch_ex": {"qps": round(plain_qps, 1), "recall_at_k": plain_recall[0],
+                                            "recall_at_10": plain_recall[1], "queries_per_call": chunk}}
     for name, prec in (("fp32", 0), ("fp8_rerank", 2)):
         srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, precision=prec)
         srv.replay(requests[:2000], np.zeros(2000))  # warm-up: encodes the FP8 copy, sizes the staging
@@ -375,7 +389,8 @@ def run_serving(local):
                                   "mean_batch_queries": round(st["mean_batch_queries"], 1)})
         srv.close()
         out[name] = form
-    out["served_fp8_over_plain_fp32"] = round(out["fp8_rerank"]["peak_qps"] / plain_qps, 3)
+    out["served_fp8_over_plain_fp32"] = round(out["fp8_rerank"]["peak_qps"] / per_request_qps, 3)
+    out["served_fp8_over_batched_fp32"] = round(out["fp8_rerank"]["peak_qps"] / plain_qps, 3)
     return out
 
 
