@@ -1,0 +1,858 @@
+// bf_mma.cu -- exact brute-force k-NN on the 5th-generation tensor cores.
+//
+// The reference scans every row with its SIMD distance kernel and keeps the
+// k smallest (distance, label) pairs (src/brute_force.cpp:34-69).  Here the
+// scan is a GEMM: queries (M = 128 per tile) times rows (N = 256 per tile)
+// in FP16 with FP32 accumulation, tcgen05.mma issued by one thread, operands
+// staged by TMA (128-byte swizzle, 4-stage mbarrier pipeline), the
+// accumulator double-buffered in TMEM (2 x 256 columns) and read back by four
+// epilogue warps (tcgen05.ld) that keep each query's candidates.
+//
+// Exactness.  For a query q and row x the GEMM gives s = |x|^2 - 2 q.x (L2)
+// or -q.x (inner product / cosine), and the reference's distance d differs
+// from s + |q|^2 (resp. 1 + s) by at most E(q): FP16 rounding of both
+// operands (relative 2^-11, absolute 2^-25 below the FP16 normal range after
+// power-of-two scaling), FP32 accumulation (bounded as sequential with
+// truncation), the FP32 norm and the reference's own FP32 rounding.  Every
+// row with s <= T + 2E, where T is the k-th smallest s, is kept; the true k
+// nearest (ties included) are among them, and their exact distances are then
+// computed in the reference's summation order and sorted by (distance, row).
+// For integer data with |v| <= 2048 and dim * (max|q| + max|x|)^2 < 2^24
+// every step is exact and E = 0.  A query whose candidates do not fit the
+// buffers is reported, and the caller answers that batch with the
+// CUDA-core scan.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bf_common.cuh"
+#include "bf_mma.h"
+#include "hnswgpu_device.h"
+
+namespace hg::bfm {
+namespace {
+
+using namespace hg::bf;
+
+constexpr int BM = 128;  // queries per tile (TMEM lanes)
+constexpr int BN = 256;  // rows per tile (TMEM columns per accumulator)
+constexpr int BK = 64;   // FP16 elements per K chunk: one 128-byte swizzle atom
+constexpr int kStages = 4;
+constexpr uint32_t kABytes = BM * BK * 2;
+constexpr uint32_t kBBytes = BN * BK * 2;
+constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-5 epilogue
+constexpr uint32_t kTmemCols = 512;
+constexpr size_t kSmem = kStages * (kABytes + kBBytes) + 1024;
+constexpr uint32_t kOver = 0xFFFFFFFFu;
+constexpr uint32_t kMaxPool = 4096;
+constexpr uint32_t kMaxDim = 1024;
+constexpr uint32_t kMaxK = 256;
+constexpr uint64_t kWaitNs = 500ull * 1000 * 1000;  // bound of every pipeline wait
+
+// instruction descriptor: D f32, A/B f16, both K-major, N = 256, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | (static_cast<uint32_t>(BN >> 3) << 17) |
+                            (static_cast<uint32_t>(BM >> 4) << 24);
+
+struct MmaParams {
+  const float* xn;        // n_pad: |x|^2 (L2) or 0
+  const uint32_t* allow;  // bits over rows or null
+  const float* qc;        // nq_pad: s = xn + acc * qc
+  const float* qm;        // nq_pad: selection margin 2E
+  uint64_t* buf;          // splits x nq x cap candidate keys
+  uint32_t* cnt;          // splits x nq: candidates kept, or kOver
+  uint32_t* err;          // [0] pipeline wait expired
+  uint32_t n, nq, kchunks, cap, k, nbt, tiles_q, splits, tps;
+  int l2;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for the phase of parity `parity` to complete; false once the time bound
+// passes (the CTA's abort flag and the global error word are then set) or
+// another role of the CTA gave up.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile uint32_t* abort_flag, uint32_t* err) {
+  if (mbar_try(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try(bar, parity)) return true;
+    if ((i & 63u) == 0) {
+      if (*abort_flag) return false;
+      if (globaltimer() - t0 > kWaitNs) {
+        *abort_flag = 1u;
+        atomicExch(err, 1u);
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+  d |= static_cast<uint64_t>(1) << 16;            // leading byte offset (unused with this swizzle)
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;    // stride byte offset
+  d |= static_cast<uint64_t>(1) << 46;            // descriptor version
+  d |= static_cast<uint64_t>(2) << 61;            // 128-byte swizzle
+  return d;
+}
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ float dist_of_key_bits(uint32_t kb) {
+  const uint32_t u = (kb & 0x80000000u) ? (kb & 0x7FFFFFFFu) : ~kb;
+  return __uint_as_float(u);
+}
+
+// Keep the candidates of one query within T + margin, T the k-th smallest
+// distance among b[0..cnt) (cnt >= k).  Returns the count kept.
+__device__ __noinline__ uint32_t compact_keys(uint64_t* b, uint32_t cnt, uint32_t k, float margin, float* thr_out) {
+  uint32_t lo = 0u, hi = 0xFFFFFFFFu;
+  while (lo < hi) {
+    const uint32_t mid = lo + ((hi - lo) >> 1);
+    uint32_t c = 0;
+    for (uint32_t i = 0; i < cnt; ++i) c += static_cast<uint32_t>(b[i] >> 32) <= mid ? 1u : 0u;
+    if (c >= k) hi = mid;
+    else lo = mid + 1u;
+  }
+  const float thr = __fadd_ru(dist_of_key_bits(lo), margin);
+  uint32_t w = 0;
+  for (uint32_t i = 0; i < cnt; ++i) {
+    const uint64_t v = b[i];
+    if (key_dist(v) <= thr) b[w++] = v;
+  }
+  *thr_out = thr;
+  return w;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    bf_mma_kernel(const __grid_constant__ CUtensorMap map_q, const __grid_constant__ CUtensorMap map_x, MmaParams P) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[2 * kStages + 5];
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile uint32_t abort_flag;
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t{1023});
+  const uint32_t sbase = smem_u32(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto sA = [&](int s) { return sbase + static_cast<uint32_t>(s) * kABytes; };
+  auto sB = [&](int s) { return sbase + kStages * kABytes + static_cast<uint32_t>(s) * kBBytes; };
+  auto full = [&](int s) { return smem_u32(&bars[s]); };
+  auto empty = [&](int s) { return smem_u32(&bars[kStages + s]); };
+  auto tfull = [&](int b) { return smem_u32(&bars[2 * kStages + b]); };
+  auto tempty = [&](int b) { return smem_u32(&bars[2 * kStages + 2 + b]); };
+  const uint32_t mdone = smem_u32(&bars[2 * kStages + 4]);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(tfull(b), 1);
+      mbar_init(tempty(b), 4);
+    }
+    mbar_init(mdone, 1);
+    abort_flag = 0u;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t items = P.tiles_q * P.splits;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer: query chunk + row chunk per stage ----
+      uint32_t stage = 0, phase = 0;
+      uint32_t issued_mask = 0, parity_mask = 0;  // per stage: a load was issued, parity of the last one
+      bool ok = true;
+      for (uint32_t item = blockIdx.x; ok && item < items; item += gridDim.x) {
+        const uint32_t qt = item % P.tiles_q, sp = item / P.tiles_q;
+        const uint32_t b0 = sp * P.tps, b1 = min(P.nbt, b0 + P.tps);
+        for (uint32_t bt = b0; ok && bt < b1; ++bt) {
+          for (uint32_t kc = 0; kc < P.kchunks; ++kc) {
+            if (!mbar_wait(empty(stage), phase ^ 1u, &abort_flag, P.err)) {
+              ok = false;
+              break;
+            }
+            mbar_expect_tx(full(stage), kABytes + kBBytes);
+            tma_load_2d(sA(stage), &map_q, full(stage), static_cast<int>(kc * BK), static_cast<int>(qt * BM));
+            tma_load_2d(sB(stage), &map_x, full(stage), static_cast<int>(kc * BK), static_cast<int>(bt * BN));
+            issued_mask |= 1u << stage;
+            parity_mask = (parity_mask & ~(1u << stage)) | (phase << stage);
+            if (++stage == kStages) {
+              stage = 0;
+              phase ^= 1u;
+            }
+          }
+        }
+      }
+      // every copy issued has landed before the CTA exits (bounded)
+      for (int st = 0; st < kStages; ++st) {
+        if (!((issued_mask >> st) & 1u)) continue;
+        const uint64_t t0 = globaltimer();
+        while (!mbar_try(full(st), (parity_mask >> st) & 1u) && globaltimer() - t0 < kWaitNs) {
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      uint32_t stage = 0, phase = 0, acc_i = 0;
+      bool ok = true;
+      for (uint32_t item = blockIdx.x; ok && item < items; item += gridDim.x) {
+        const uint32_t sp = item / P.tiles_q;
+        const uint32_t b0 = sp * P.tps, b1 = min(P.nbt, b0 + P.tps);
+        for (uint32_t bt = b0; ok && bt < b1; ++bt, ++acc_i) {
+          const uint32_t ab = acc_i & 1u, aph = (acc_i >> 1) & 1u;
+          if (!mbar_wait(tempty(ab), aph ^ 1u, &abort_flag, P.err)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d = tmem + ab * BN;
+          for (uint32_t kc = 0; kc < P.kchunks; ++kc) {
+            if (!mbar_wait(full(stage), phase, &abort_flag, P.err)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint64_t a = sw128_desc(sA(stage)), b = sw128_desc(sB(stage));
+#pragma unroll
+            for (uint32_t kk = 0; kk < BK / 16; ++kk)  // K = 16 per MMA: +32 bytes in the swizzle atom
+              umma_f16(d, a + 2u * kk, b + 2u * kk, (kc | kk) != 0u ? 1u : 0u);
+            umma_commit(empty(stage));  // frees the stage once these MMAs have read it
+            if (++stage == kStages) {
+              stage = 0;
+              phase ^= 1u;
+            }
+          }
+          if (ok) umma_commit(tfull(ab));
+        }
+      }
+      // all MMAs of this thread have completed before TMEM is released (bounded)
+      umma_commit(mdone);
+      const uint64_t t0 = globaltimer();
+      while (!mbar_try(mdone, 0u) && globaltimer() - t0 < kWaitNs) {
+      }
+    }
+  } else {
+    // ---- epilogue: one query per thread (TMEM lane), 256 rows per tile ----
+    const uint32_t quarter = static_cast<uint32_t>(warp & 3);
+    const uint32_t row_in_tile = quarter * 32u + static_cast<uint32_t>(lane);
+    uint32_t acc_i = 0;
+    bool ok = true;
+    for (uint32_t item = blockIdx.x; ok && item < items; item += gridDim.x) {
+      const uint32_t qt = item % P.tiles_q, sp = item / P.tiles_q;
+      const uint32_t b0 = sp * P.tps, b1 = min(P.nbt, b0 + P.tps);
+      const uint32_t q = qt * BM + row_in_tile;
+      const bool live_q = q < P.nq;
+      const float cq = P.qc[q];
+      const float margin = P.qm[q];
+      uint64_t* bufp = P.buf + (static_cast<size_t>(sp) * P.nq + (live_q ? q : 0)) * P.cap;
+      uint32_t cnt = 0;
+      float thr = __int_as_float(0x7f800000);
+      bool over = false;
+      for (uint32_t bt = b0; bt < b1; ++bt, ++acc_i) {
+        const uint32_t ab = acc_i & 1u, aph = (acc_i >> 1) & 1u;
+        // one lane waits, the warp follows its answer (tcgen05.ld needs the whole warp)
+        int got = 0;
+        if (lane == 0) got = mbar_wait(tfull(ab), aph, &abort_flag, P.err) ? 1 : 0;
+        if (!__shfl_sync(kFull, got, 0)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t taddr = tmem + ((quarter * 32u) << 16) + ab * BN;
+#pragma unroll 1
+        for (uint32_t ch = 0; ch < BN / 32; ++ch) {
+          __syncwarp();
+          uint32_t r[32];
+          tmem_ld32(taddr + ch * 32u, r);
+          const uint32_t j0 = bt * BN + ch * 32u;
+          if (j0 >= P.n || !live_q || over) continue;
+          uint32_t valid = P.n - j0 >= 32u ? 0xFFFFFFFFu : ((1u << (P.n - j0)) - 1u);
+          if (P.allow) valid &= __ldg(P.allow + (j0 >> 5));
+          float xn[32];
+          const float4* x4 = reinterpret_cast<const float4*>(P.xn + j0);
+#pragma unroll
+          for (int v = 0; v < 8; ++v) {
+            const float4 t = __ldg(x4 + v);
+            xn[4 * v] = t.x;
+            xn[4 * v + 1] = t.y;
+            xn[4 * v + 2] = t.z;
+            xn[4 * v + 3] = t.w;
+          }
+#pragma unroll
+          for (int c = 0; c < 32; ++c) {
+            const float acc = __uint_as_float(r[c]);
+            const float s = P.l2 ? __fmaf_rn(acc, cq, xn[c]) : __fmul_rn(acc, cq);
+            if (((valid >> c) & 1u) && s <= thr) {
+              bufp[cnt] = (static_cast<uint64_t>(okey(s)) << 32) | (j0 + c);
+              if (++cnt == P.cap) {
+                cnt = compact_keys(bufp, cnt, P.k, margin, &thr);
+                if (cnt + 32u > P.cap) {  // the margin keeps too many rows: give this query up
+                  over = true;
+                  thr = -__int_as_float(0x7f800000);
+                }
+              }
+            }
+          }
+        }
+        __syncwarp();
+        tc_fence_before();
+        if (lane == 0) mbar_arrive(tempty(ab));
+      }
+      if (ok && live_q) P.cnt[static_cast<size_t>(sp) * P.nq + q] = over ? kOver : cnt;
+    }
+  }
+  __syncwarp();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// rows: bound constants, FP16 copy and squared norms
+// ---------------------------------------------------------------------------
+struct RowStats {
+  uint32_t max_abs_bits, max_l1_bits, max_l2_bits, all_int;
+};
+
+__global__ void row_stats_kernel(const float* __restrict__ rows, uint32_t n, uint32_t dim, uint32_t dp, RowStats* st) {
+  const uint64_t r = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  float mx = 0.0f;
+  double l1 = 0.0, l2 = 0.0;
+  bool isint = true;
+  for (uint32_t i = lane; i < dim; i += 32) {
+    const float v = rows[r * dp + i];
+    const float a = fabsf(v);
+    mx = fmaxf(mx, a);
+    l1 += a;
+    l2 += static_cast<double>(v) * v;
+    isint = isint && v == rintf(v) && a <= 2048.0f;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    l1 += __shfl_xor_sync(kFull, l1, o);
+    l2 += __shfl_xor_sync(kFull, l2, o);
+  }
+  isint = __all_sync(kFull, isint);
+  if (lane == 0) {
+    atomicMax(&st->max_abs_bits, __float_as_uint(mx));
+    atomicMax(&st->max_l1_bits, __float_as_uint(__double2float_ru(l1)));
+    atomicMax(&st->max_l2_bits, __float_as_uint(__double2float_ru(sqrt(l2))));
+    if (!isint) atomicAnd(&st->all_int, 0u);
+  }
+}
+
+__global__ void encode_rows_kernel(const float* __restrict__ rows, uint32_t n, uint32_t n_pad, uint32_t dim,
+                                   uint32_t dp, uint32_t kp, float sigma, int l2, __half* __restrict__ x16,
+                                   float* __restrict__ xn) {
+  const uint64_t r = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= n_pad) return;
+  float ss = 0.0f;
+  for (uint32_t i = lane; i < kp; i += 32) {
+    const float v = (r < n && i < dim) ? rows[r * dp + i] : 0.0f;
+    x16[r * kp + i] = __float2half_rn(__fmul_rn(v, sigma));
+    ss = __fmaf_rn(v, v, ss);
+  }
+  for (int o = 16; o > 0; o >>= 1) ss = __fadd_rn(ss, __shfl_xor_sync(kFull, ss, o));
+  if (lane == 0) xn[r] = (l2 && r < n) ? ss : 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// queries: FP16 copy, scale and selection margin
+// ---------------------------------------------------------------------------
+struct DataBound {
+  float sigma_x, x2, x1, xm;
+  int all_int;
+};
+
+__global__ void prep_queries_kernel(const float* __restrict__ raw, const float* __restrict__ inv, uint32_t nq,
+                                    uint32_t nq_pad, uint32_t dim, uint32_t kp, int l2, DataBound db,
+                                    __half* __restrict__ q16, float* __restrict__ qc, float* __restrict__ qm) {
+  const uint64_t q = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (q >= nq_pad) return;
+  const bool live = q < nq;
+  const float iv = (live && inv) ? inv[q] : 1.0f;
+  float mx = 0.0f;
+  double l1 = 0.0, l2s = 0.0;
+  bool isint = true;
+  for (uint32_t i = lane; i < dim; i += 32) {
+    float v = live ? raw[q * dim + i] : 0.0f;
+    if (inv) v = __fmul_rn(v, iv);
+    const float a = fabsf(v);
+    mx = fmaxf(mx, a);
+    l1 += a;
+    l2s += static_cast<double>(v) * v;
+    isint = isint && v == rintf(v) && a <= 2048.0f;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    l1 += __shfl_xor_sync(kFull, l1, o);
+    l2s += __shfl_xor_sync(kFull, l2s, o);
+  }
+  isint = __all_sync(kFull, isint);
+  const double d = static_cast<double>(dim);
+  const double qn = sqrt(l2s) * (1.0 + 1e-12);
+  const bool exact = db.all_int && isint &&
+                     d * (static_cast<double>(mx) + db.xm) * (static_cast<double>(mx) + db.xm) < 16777216.0;
+  float sigma_q = 1.0f;
+  if (!exact && mx > 0.0f) {
+    int e;
+    frexpf(mx, &e);                 // mx < 2^e
+    sigma_q = ldexpf(1.0f, 14 - e);  // mx * sigma_q in [2^13, 2^14)
+  }
+  for (uint32_t i = lane; i < kp; i += 32) {
+    float v = (live && i < dim) ? raw[q * dim + i] : 0.0f;
+    if (inv) v = __fmul_rn(v, iv);
+    q16[q * kp + i] = __float2half_rn(__fmul_rn(v, sigma_q));
+  }
+  if (lane != 0) return;
+  const float unscale = 1.0f / (sigma_q * db.sigma_x);  // a power of two
+  qc[q] = (l2 ? -2.0f : -1.0f) * unscale;
+  if (exact) {
+    qm[q] = 0.0f;
+    return;
+  }
+  // error bound E of s against the reference distance; the margin is 2 * (2E)
+  const double u = 1.0 / 2048.0, p23 = 1.0 / 8388608.0, p24 = p23 / 2.0;
+  const double c1 = 2.0 * u + u * u + (d + 2.0) * p23 * (1.0 + 2.0 * u + u * u);
+  const double sub = 1.01 * (1.0 / 33554432.0) * (l1 / db.sigma_x + db.x1 / sigma_q) + d * 1e-15;
+  const double edot = c1 * qn * db.x2 + sub;
+  const double gam = (d + 2.0) * p24 * 1.01;
+  double e;
+  if (l2) {
+    e = 2.0 * edot + gam * db.x2 * db.x2 + p23 * (db.x2 * db.x2 + 2.0 * qn * db.x2) +
+        (2.0 * p23 + gam) * (qn + db.x2) * (qn + db.x2) + gam * qn * qn;
+  } else {
+    e = edot + gam * qn * db.x2 + 2.0 * p23 * (1.0 + qn * db.x2);
+  }
+  qm[q] = __double2float_ru(4.0 * e);
+}
+
+// ---------------------------------------------------------------------------
+// per query: k-th smallest over the splits, survivors within the margin
+// ---------------------------------------------------------------------------
+__global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* __restrict__ cnt,
+                              const float* __restrict__ qm, uint32_t nq, uint32_t splits, uint32_t cap, uint32_t k,
+                              uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t* __restrict__ pool_n,
+                              uint32_t* __restrict__ err) {
+  const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  uint32_t total = 0;
+  bool over = false;
+  for (uint32_t s = 0; s < splits; ++s) {
+    const uint32_t c = cnt[static_cast<size_t>(s) * nq + q];
+    if (c == kOver) over = true;
+    else total += c;
+  }
+  if (over) {
+    if (lane == 0) {
+      pool_n[q] = 0;
+      atomicAdd(err + 1, 1u);
+    }
+    return;
+  }
+  auto count_le = [&](uint32_t bound) {
+    uint32_t c = 0;
+    for (uint32_t s = 0; s < splits; ++s) {
+      const uint32_t m = cnt[static_cast<size_t>(s) * nq + q];
+      const uint64_t* b = buf + (static_cast<size_t>(s) * nq + q) * cap;
+      for (uint32_t i = lane; i < m; i += 32) c += static_cast<uint32_t>(b[i] >> 32) <= bound ? 1u : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+    return c;
+  };
+  float thr = __int_as_float(0x7f800000);
+  if (total > k) {
+    uint32_t lo = 0u, hi = 0xFFFFFFFFu;
+    while (lo < hi) {
+      const uint32_t mid = lo + ((hi - lo) >> 1);
+      if (count_le(mid) >= k) hi = mid;
+      else lo = mid + 1u;
+    }
+    thr = __fadd_ru(dist_of_key_bits(lo), qm[q]);
+  }
+  uint32_t w = 0;
+  for (uint32_t s = 0; s < splits; ++s) {
+    const uint32_t m = cnt[static_cast<size_t>(s) * nq + q];
+    const uint64_t* b = buf + (static_cast<size_t>(s) * nq + q) * cap;
+    for (uint32_t base = 0; base < m; base += 32) {
+      const uint32_t i = base + lane;
+      const uint64_t v = i < m ? b[i] : 0ull;
+      const bool keep = i < m && key_dist(v) <= thr;
+      const uint32_t bal = __ballot_sync(kFull, keep);
+      const uint32_t pos = w + __popc(bal & ((1u << lane) - 1u));
+      if (keep && pos < pool_cap) pool[static_cast<size_t>(q) * pool_cap + pos] = static_cast<uint32_t>(v);
+      w += __popc(bal);
+    }
+  }
+  if (lane == 0) {
+    if (w > pool_cap) {
+      pool_n[q] = 0;
+      atomicAdd(err + 1, 1u);
+    } else {
+      pool_n[q] = w;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// exact distances of the survivors in the reference order, sorted, first k
+// ---------------------------------------------------------------------------
+template <int S, bool L2>
+__global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ rows, const uint64_t* __restrict__ labels,
+                                                     const float* __restrict__ queries, const float* __restrict__ inv,
+                                                     uint32_t nq, uint32_t dim, uint32_t dp, uint32_t k,
+                                                     const uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t p2max,
+                                                     const uint32_t* __restrict__ pool_n, Rec* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smem) + static_cast<size_t>(w) * p2max;
+  const uint32_t q = blockIdx.x * 4u + static_cast<uint32_t>(w);
+  if (q >= nq) return;
+  const int nb = static_cast<int>(dim / 64), nt = static_cast<int>((dim % 64) / 16), rem = static_cast<int>(dim % 16);
+  float qr[S];
+  const float iv = inv ? inv[q] : 1.0f;
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    const int e = bslot(i, nb, nt, rem, lane);
+    const float v = e >= 0 ? queries[static_cast<size_t>(q) * dim + e] : 0.0f;
+    qr[i] = inv ? __fmul_rn(v, iv) : v;
+  }
+  const uint32_t m = pool_n[q];
+  const uint32_t* ids = pool + static_cast<size_t>(q) * pool_cap;
+  for (uint32_t c = 0; c < m; ++c) {
+    const uint32_t r = ids[c];
+    float x[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      const int e = bslot(i, nb, nt, rem, lane);
+      x[i] = e >= 0 ? __ldg(rows + static_cast<size_t>(r) * dp + e) : 0.0f;
+    }
+    const float d = bdist<S, L2>(x, qr, nb, nt, rem, lane);
+    if (lane == 0) keys[c] = (static_cast<uint64_t>(okey(d)) << 32) | r;
+  }
+  int p2 = 1;
+  while (p2 < static_cast<int>(m)) p2 <<= 1;
+  for (int i = static_cast<int>(m) + lane; i < p2; i += 32) keys[i] = ~0ull;
+  __syncwarp();
+  warp_sort(keys, p2, lane);
+  Rec* row = out + static_cast<size_t>(q) * k;
+  for (uint32_t j = lane; j < k; j += 32) {
+    Rec o;
+    if (j < m) {
+      const uint64_t kk = keys[j];
+      o.label = labels[static_cast<uint32_t>(kk)];
+      o.dist = key_dist(kk);
+    } else {
+      o.label = ~0ull;
+      o.dist = __int_as_float(0x7f800000);
+    }
+    o.zero = 0;
+    row[j] = o;
+  }
+}
+
+int slots_of(uint32_t dim) {
+  return 2 * static_cast<int>(dim / 64) + static_cast<int>((dim % 64) / 16) + 1;
+}
+
+template <bool L2>
+cudaError_t launch_rerank(int S, dim3 grid, size_t smem, cudaStream_t st, const float* rows, const uint64_t* labels,
+                          const float* queries, const float* inv, uint32_t nq, uint32_t dim, uint32_t dp, uint32_t k,
+                          const uint32_t* pool, uint32_t pool_cap, uint32_t p2max, const uint32_t* pool_n, Rec* out) {
+  auto go = [&](auto fn) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    fn<<<grid, 128, smem, st>>>(rows, labels, queries, inv, nq, dim, dp, k, pool, pool_cap, p2max, pool_n, out);
+    return cudaGetLastError();
+  };
+  if (S <= 6) return go(rerank_kernel<6, L2>);
+  if (S <= 10) return go(rerank_kernel<10, L2>);
+  if (S <= 18) return go(rerank_kernel<18, L2>);
+  if (S <= 34) return go(rerank_kernel<34, L2>);
+  return cudaErrorInvalidValue;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// K-major FP16 matrix [rows][kp] with a (64 x box_rows) box and 128-byte swizzle
+bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint32_t kp, uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {kp, rows};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(kp) * 2};
+  const cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+uint32_t round_up(uint32_t v, uint32_t m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+
+struct Store {
+  __half* x16 = nullptr;
+  float* xn = nullptr;
+  uint32_t n_pad = 0, kp = 0;
+  DataBound db{};
+  CUtensorMap map_x{};
+  int sms = 0;
+};
+
+bool supported(uint32_t dim, uint32_t k) { return dim >= 1 && dim <= kMaxDim && k >= 1 && k <= kMaxK; }
+
+cudaError_t store_create(const Rows& r, cudaStream_t st, Store** out, std::string* err) {
+  auto* s = new Store();
+  s->kp = round_up(r.dim, BK);
+  s->n_pad = round_up(std::max<uint32_t>(r.n, 1), BN);
+  cudaError_t e = cudaSuccess;
+  RowStats* dstats = nullptr;
+  auto fail = [&](const char* what) {
+    *err = std::string("tensor brute force: ") + what + ": " + cudaGetErrorString(e);
+    if (dstats) cudaFree(dstats);
+    store_free(s);
+    return e;
+  };
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return fail("device");
+  if ((e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return fail("device");
+  if ((e = cudaMalloc(&s->x16, static_cast<size_t>(s->n_pad) * s->kp * 2)) != cudaSuccess) return fail("alloc");
+  if ((e = cudaMalloc(&s->xn, static_cast<size_t>(s->n_pad) * 4)) != cudaSuccess) return fail("alloc");
+  if ((e = cudaMalloc(&dstats, sizeof(RowStats))) != cudaSuccess) return fail("alloc");
+  RowStats init{0u, 0u, 0u, 1u};
+  if ((e = cudaMemcpyAsync(dstats, &init, sizeof(init), cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail("copy");
+  if (r.n) {
+    row_stats_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(r.n) * 32 + 255) / 256), 256, 0, st>>>(
+        r.rows, r.n, r.dim, r.dp, dstats);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail("stats kernel");
+  }
+  RowStats hs{};
+  if ((e = cudaMemcpyAsync(&hs, dstats, sizeof(hs), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return fail("copy");
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("stats");
+  cudaFree(dstats);
+  dstats = nullptr;
+  float xm, x1, x2;
+  std::memcpy(&xm, &hs.max_abs_bits, 4);
+  std::memcpy(&x1, &hs.max_l1_bits, 4);
+  std::memcpy(&x2, &hs.max_l2_bits, 4);
+  s->db.all_int = hs.all_int != 0u;
+  s->db.xm = xm;
+  s->db.x1 = x1;
+  s->db.x2 = x2;
+  s->db.sigma_x = 1.0f;
+  if (!s->db.all_int && xm > 0.0f) {
+    int ex;
+    std::frexp(xm, &ex);
+    s->db.sigma_x = std::ldexp(1.0f, 14 - ex);
+  }
+  encode_rows_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(s->n_pad) * 32 + 255) / 256), 256, 0, st>>>(
+      r.rows, r.n, s->n_pad, r.dim, r.dp, s->kp, s->db.sigma_x, r.metric == HGD_METRIC_L2 ? 1 : 0, s->x16, s->xn);
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail("encode kernel");
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("encode");
+  if (!make_map(&s->map_x, s->x16, s->n_pad, s->kp, BN)) {
+    e = cudaErrorInvalidValue;
+    return fail("tensor map");
+  }
+  *out = s;
+  return cudaSuccess;
+}
+
+void store_free(Store* s) {
+  if (!s) return;
+  if (s->x16) cudaFree(s->x16);
+  if (s->xn) cudaFree(s->xn);
+  delete s;
+}
+
+cudaError_t search(Store* s, const Rows& r, const float* queries, const float* inv, uint32_t nq, uint32_t k,
+                   const uint32_t* allow, void* out, cudaStream_t st, bool* redo, std::string* err) {
+  *redo = false;
+  if (nq == 0) return cudaSuccess;
+  const uint32_t nq_pad = round_up(nq, BM);
+  const uint32_t tiles_q = nq_pad / BM;
+  const uint32_t nbt = s->n_pad / BN;
+  uint32_t splits = 1;
+  if (tiles_q < static_cast<uint32_t>(s->sms))
+    splits = std::min<uint32_t>(nbt, (2u * static_cast<uint32_t>(s->sms) + tiles_q - 1) / tiles_q);
+  const uint32_t tps = (nbt + splits - 1) / splits;
+  splits = (nbt + tps - 1) / tps;
+  const uint32_t cap = std::max<uint32_t>(64, round_up(2 * k + 32, 32));
+  const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(splits * cap, 32), 32));
+  uint32_t p2max = 1;
+  while (p2max < pool_cap) p2max <<= 1;
+
+  __half* q16 = nullptr;
+  float *qc = nullptr, *qm = nullptr;
+  uint64_t* buf = nullptr;
+  uint32_t *cnt = nullptr, *pool = nullptr, *pool_n = nullptr, *derr = nullptr;
+  cudaError_t e = cudaSuccess;
+  const char* what = "";
+  do {
+    what = "alloc";
+    if ((e = cudaMalloc(&q16, static_cast<size_t>(nq_pad) * s->kp * 2)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&qc, nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&qm, nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&buf, static_cast<size_t>(splits) * nq * cap * 8)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&cnt, static_cast<size_t>(splits) * nq * 4)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&pool, static_cast<size_t>(nq) * pool_cap * 4)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&pool_n, nq * 4ull)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&derr, 16)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(derr, 0, 16, st)) != cudaSuccess) break;
+    what = "query kernel";
+    prep_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(nq_pad) * 32 + 255) / 256), 256, 0, st>>>(
+        queries, inv, nq, nq_pad, r.dim, s->kp, r.metric == HGD_METRIC_L2 ? 1 : 0, s->db, q16, qc, qm);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    CUtensorMap map_q;
+    what = "tensor map";
+    if (!make_map(&map_q, q16, nq_pad, s->kp, BM)) {
+      e = cudaErrorInvalidValue;
+      break;
+    }
+    MmaParams P{};
+    P.xn = s->xn;
+    P.allow = allow;
+    P.qc = qc;
+    P.qm = qm;
+    P.buf = buf;
+    P.cnt = cnt;
+    P.err = derr;
+    P.n = r.n;
+    P.nq = nq;
+    P.kchunks = s->kp / BK;
+    P.cap = cap;
+    P.k = k;
+    P.nbt = nbt;
+    P.tiles_q = tiles_q;
+    P.splits = splits;
+    P.tps = tps;
+    P.l2 = r.metric == HGD_METRIC_L2 ? 1 : 0;
+    what = "tensor kernel";
+    if ((e = cudaFuncSetAttribute(bf_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kSmem))) != cudaSuccess)
+      break;
+    const uint32_t items = tiles_q * splits;
+    const unsigned grid = std::min<uint32_t>(items, static_cast<uint32_t>(s->sms));
+    bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    what = "select kernel";
+    select_kernel<<<(nq * 32 + 255) / 256, 256, 0, st>>>(buf, cnt, qm, nq, splits, cap, k, pool, pool_cap, pool_n,
+                                                         derr);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    what = "rerank kernel";
+    const int S = slots_of(r.dim);
+    const dim3 rgrid((nq + 3) / 4);
+    const size_t rsmem = 4ull * p2max * 8;
+    e = r.metric == HGD_METRIC_L2
+            ? launch_rerank<true>(S, rgrid, rsmem, st, r.rows, r.labels, queries, inv, nq, r.dim, r.dp, k, pool,
+                                  pool_cap, p2max, pool_n, static_cast<Rec*>(out))
+            : launch_rerank<false>(S, rgrid, rsmem, st, r.rows, r.labels, queries, inv, nq, r.dim, r.dp, k, pool,
+                                   pool_cap, p2max, pool_n, static_cast<Rec*>(out));
+    if (e != cudaSuccess) break;
+    uint32_t herr[4] = {0, 0, 0, 0};
+    what = "status";
+    if ((e = cudaMemcpyAsync(herr, derr, 16, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
+    if (herr[0]) {
+      e = cudaErrorLaunchTimeout;
+      what = "tensor pipeline wait expired";
+      break;
+    }
+    *redo = herr[1] != 0;
+  } while (false);
+  if (e != cudaSuccess) *err = std::string("tensor brute force: ") + what + ": " + cudaGetErrorString(e);
+  cudaStreamSynchronize(st);
+  for (void* p : {static_cast<void*>(q16), static_cast<void*>(qc), static_cast<void*>(qm), static_cast<void*>(buf),
+                  static_cast<void*>(cnt), static_cast<void*>(pool), static_cast<void*>(pool_n),
+                  static_cast<void*>(derr)})
+    if (p) cudaFree(p);
+  return e;
+}
+
+}  // namespace hg::bfm

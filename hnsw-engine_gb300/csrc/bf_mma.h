@@ -1,0 +1,37 @@
+// bf_mma.h -- tensor-core brute force (tcgen05 / TMEM / TMA) behind
+// hgd_bruteforce: candidate selection by an FP16 GEMM with a proven error
+// margin, then the exact distances of the survivors in the reference order.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+namespace hg::bfm {
+
+struct Store;  // FP16 K-major copy of the rows, squared norms, bound constants, TMA map
+
+struct Rows {
+  const float* rows;       // n x dp float32 (device), sorted by label, zero tail
+  const uint64_t* labels;  // n (device), sorted
+  uint32_t n, dim, dp;
+  int metric;              // HGD_METRIC_*
+};
+
+// Whether the tensor path handles this shape (dim <= 1024, k <= 256).
+bool supported(uint32_t dim, uint32_t k);
+
+// Build the FP16 copy (once per store).  Synchronous.
+cudaError_t store_create(const Rows& r, cudaStream_t st, Store** out, std::string* err);
+void store_free(Store* s);
+
+// Exact k-NN of nq device queries (raw, nq x dim); `inv` = per-query 1/||q||
+// for cosine (else null), `allow` = bits over sorted rows or null.  Writes
+// nq x k records to `out` (device).  On return *redo is true when some query
+// could not be settled by the margin test (too many near-ties): the caller
+// then answers the batch with the CUDA-core scan.  Synchronises `st`.
+cudaError_t search(Store* s, const Rows& r, const float* queries, const float* inv, uint32_t nq, uint32_t k,
+                   const uint32_t* allow, void* out, cudaStream_t st, bool* redo, std::string* err);
+
+}  // namespace hg::bfm

@@ -18,6 +18,8 @@
 #include <string>
 #include <vector>
 
+#include "bf_common.cuh"
+#include "bf_mma.h"
 #include "hnswgpu_device.h"
 
 namespace hg {
@@ -26,64 +28,9 @@ void set_last_error(const std::string& msg);
 
 namespace {
 
-constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kWarps = 16;
 constexpr uint32_t kMaxK = 256;
-
-
-__device__ __forceinline__ uint32_t okey(float d) {
-  d = __fadd_rn(d, 0.0f);
-  const uint32_t u = __float_as_uint(d);
-  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float key_dist(uint64_t key) {
-  const uint32_t k = static_cast<uint32_t>(key >> 32);
-  const uint32_t u = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
-  return __uint_as_float(u);
-}
-
-// lane slots: A chain 64i+lane (i<nb); B chain 64i+32+lane; 16-blocks (lanes<16)
-// 64nb+16u+lane; masked remainder (lanes>=16) 64nb+16nt+(lane-16) < dim.
-__device__ __forceinline__ int bslot(int i, int nb, int nt, int rem, int lane) {
-  if (i < nb) return 64 * i + lane;
-  if (i < 2 * nb) return 64 * (i - nb) + 32 + lane;
-  const int u = i - 2 * nb;
-  if (u < nt) return lane < 16 ? 64 * nb + 16 * u + lane : -1;
-  if (u == nt && lane >= 16 && lane - 16 < rem) return 64 * nb + 16 * nt + (lane - 16);
-  return -1;
-}
-
-template <int S, bool L2>
-__device__ __forceinline__ float bdist(const float (&x)[S], const float (&q)[S], int nb, int nt, int rem, int lane) {
-  float a = 0.0f, b = 0.0f;
-#pragma unroll
-  for (int i = 0; i < S; ++i) {
-    const bool chainA = i < nb || (i >= 2 * nb && i < 2 * nb + nt) || (i == 2 * nb + nt && rem > 0);
-    const bool chainB = i >= nb && i < 2 * nb;
-    if (!chainA && !chainB) continue;
-    const int u = i - 2 * nb;
-    // 16-blocks touch lanes < 16 only, the masked block lanes >= 16 only
-    const bool live = chainB || i < nb || (u < nt ? lane < 16 : lane >= 16);
-    if (!live) continue;
-    float t;
-    if (L2) {
-      const float d = __fsub_rn(q[i], x[i]);
-      t = __fmaf_rn(d, d, chainA ? a : b);
-    } else {
-      t = __fmaf_rn(q[i], x[i], chainA ? a : b);
-    }
-    if (chainA) a = t;
-    else b = t;
-  }
-  const float xa = __fadd_rn(a, __shfl_xor_sync(kFull, a, 16));
-  const float xb = __fadd_rn(b, __shfl_xor_sync(kFull, b, 16));
-  float s = __fadd_rn(xa, xb);
-  s = __fadd_rn(s, __shfl_xor_sync(kFull, s, 8));
-  s = __fadd_rn(s, __shfl_xor_sync(kFull, s, 4));
-  s = __fadd_rn(s, __shfl_xor_sync(kFull, s, 2));
-  s = __fadd_rn(s, __shfl_xor_sync(kFull, s, 1));
-  return L2 ? s : __fsub_rn(1.0f, s);
-}
+using namespace hg::bf;
 
 struct BfParams {
   const float* rows;       // n x dp, sorted by label
@@ -93,12 +40,6 @@ struct BfParams {
   const float* inv;        // cosine: per query 1/||q|| or null
   uint32_t n, dim, dp, nq, k;
   void* out;
-};
-
-struct Rec {
-  uint64_t label;
-  float dist;
-  uint32_t zero;
 };
 
 template <int S, int QT, bool L2>
@@ -275,6 +216,9 @@ struct hgd_flat {
   uint64_t* labels = nullptr;
   std::vector<uint64_t> orig_of_sorted;  // sorted row -> insertion index
   cudaStream_t stream = nullptr;
+  hg::bfm::Store* tensor = nullptr;  // FP16 copy for the tensor-core path (built on first use)
+  int path = HGD_BF_AUTO;
+  int last_path = 0;
 };
 
 extern "C" {
@@ -324,15 +268,29 @@ void hgd_flat_free(hgd_flat* f) {
   cudaSetDevice(f->device);
   if (f->rows) cudaFree(f->rows);
   if (f->labels) cudaFree(f->labels);
+  hg::bfm::store_free(f->tensor);
   if (f->stream) cudaStreamDestroy(f->stream);
   delete f;
 }
+
+int hgd_flat_set_path(hgd_flat* f, int path) {
+  if (!f || path < HGD_BF_AUTO || path > HGD_BF_TENSOR)
+    return (hg::set_last_error("hgd_flat_set_path: bad argument"), HGD_EINVAL);
+  f->path = path;
+  return HGD_OK;
+}
+
+int hgd_flat_last_path(const hgd_flat* f) { return f ? f->last_path : 0; }
 
 int hgd_bruteforce(hgd_flat* f, const float* queries, uint64_t nq, uint32_t k, const hgd_bitset* filter, void* out,
                    void* stream) {
   if (!f || !queries || !out) return (hg::set_last_error("hgd_bruteforce: null argument"), HGD_EINVAL);
   if (k == 0) return (hg::set_last_error("search: k must be > 0"), HGD_EINVAL);
   if (k > kMaxK) return (hg::set_last_error("brute force: k above 256 is not supported"), HGD_EINVAL);
+  const bool tensor_ok = hg::bfm::supported(f->dim, k);
+  if (f->path == HGD_BF_TENSOR && !tensor_ok)
+    return (hg::set_last_error("brute force: the tensor path needs dim <= 1024 and k <= 256"), HGD_EINVAL);
+  const bool use_tensor = f->path != HGD_BF_SCAN && tensor_ok;
   if (nq == 0) return HGD_OK;
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : f->stream;
   float *dq = nullptr, *dinv = nullptr;
@@ -377,6 +335,30 @@ int hgd_bruteforce(hgd_flat* f, const float* queries, uint64_t nq, uint32_t k, c
         if (!check(cudaStreamSynchronize(st))) break;
       }
     }
+    if (use_tensor) {
+      hg::bfm::Rows R{f->rows, f->labels, f->n, f->dim, f->dp, f->metric};
+      std::string err;
+      if (!f->tensor && !check(hg::bfm::store_create(R, st, &f->tensor, &err))) {
+        hg::set_last_error(err);
+        break;
+      }
+      bool redo = false;
+      const cudaError_t e = hg::bfm::search(f->tensor, R, dq, dinv, static_cast<uint32_t>(nq), k, dallow, dout, st,
+                                            &redo, &err);
+      if (e != cudaSuccess) {
+        check(e);
+        hg::set_last_error(err);
+        break;
+      }
+      if (!redo) {
+        f->last_path = HGD_BF_TENSOR;
+        if (!check(cudaMemcpyAsync(out, dout, nq * k * 16, cudaMemcpyDeviceToHost, st))) break;
+        check(cudaStreamSynchronize(st));
+        break;
+      }
+      // some query kept more near-ties than the buffers hold: the scan answers the batch
+    }
+    f->last_path = HGD_BF_SCAN;
     BfParams P{};
     P.rows = f->rows;
     P.labels = f->labels;

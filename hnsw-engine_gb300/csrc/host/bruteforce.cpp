@@ -90,12 +90,19 @@ void BruteForceIndex::search_batch(const float* qs, std::size_t nq, std::size_t 
     if (view.words == nullptr && view.num_bits == 0) view.label_space = 1;
     if (dynamic_cast<const BitsetFilter*>(f)) view.label_space = 1;
   }
+  hgd_flat_set_path(dev_->flat, path_);
   const int rc = hgd_bruteforce(dev_->flat, qs, nq, static_cast<uint32_t>(k), f ? &view : nullptr, out, nullptr);
+  last_path_ = hgd_flat_last_path(dev_->flat);
   if (rc != HGD_OK) {
     const std::string msg = std::string("BruteForceIndex search: ") + hgd_last_error();
     if (rc == HGD_EINVAL) throw std::invalid_argument(msg);
     throw std::runtime_error(msg);
   }
+}
+
+void BruteForceIndex::set_gpu_path(int path) {
+  if (path < 0 || path > 2) throw std::invalid_argument("set_gpu_path: 0 (auto), 1 (scan) or 2 (tensor)");
+  path_ = path;
 }
 
 std::vector<Neighbor> BruteForceIndex::search(const float* q, std::size_t k, const Filter* f) const {

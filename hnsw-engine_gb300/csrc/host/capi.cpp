@@ -268,6 +268,15 @@ int hg_bruteforce_search_batch(const hg_bruteforce* bf, const float* qs, size_t 
 
 void hg_bruteforce_free(hg_bruteforce* bf) { delete bf; }
 
+int hg_bruteforce_set_path(hg_bruteforce* bf, int path) {
+  return guarded([&] {
+    if (!bf) throw std::invalid_argument("bruteforce: null index");
+    bf->bf.set_gpu_path(path);
+  });
+}
+
+int hg_bruteforce_last_path(const hg_bruteforce* bf) { return bf ? bf->bf.last_gpu_path() : 0; }
+
 struct hg_server {
   hnsw::gb::Server* s;
 };

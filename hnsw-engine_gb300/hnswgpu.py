@@ -98,6 +98,8 @@ def lib():
         L.hg_bruteforce_search_batch.argtypes = [vp, vp, sz, sz, vp, C.POINTER(_Filter)]
         L.hg_bruteforce_free.argtypes = [vp]
         L.hg_index_search_batch_noalloc.argtypes = [vp, vp, sz, sz, sz, vp, vp]
+        L.hg_bruteforce_set_path.argtypes = [vp, i32]
+        L.hg_bruteforce_last_path.argtypes = [vp]
         L.hg_server_create.argtypes = [vp, C.POINTER(_ServerConfig), C.POINTER(vp)]
         L.hg_server_submit.argtypes = [vp, C.POINTER(_Request), C.POINTER(C.c_uint64)]
         L.hg_server_wait.argtypes = [vp, C.c_uint64, C.POINTER(C.c_double)]
@@ -460,6 +462,16 @@ class BruteForceIndex:
         fh = _FilterHolder(filter)
         _check(lib().hg_bruteforce_search_batch(self._h, _ptr(q), q.shape[0], k, _ptr(out), fh.ref()))
         return out.reshape(q.shape[0], k)
+
+    PATH_AUTO, PATH_SCAN, PATH_TENSOR = 0, 1, 2
+
+    def set_path(self, path: int):
+        """GPU kernel: 0 auto, 1 CUDA-core scan, 2 tensor-core GEMM + exact rerank."""
+        _check(lib().hg_bruteforce_set_path(self._h, path))
+
+    @property
+    def last_path(self) -> int:
+        return int(lib().hg_bruteforce_last_path(self._h))
 
 
 class Server:

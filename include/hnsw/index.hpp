@@ -123,6 +123,11 @@ class BruteForceIndex {
                     const Filter* f = nullptr) const;
   std::size_t size() const noexcept { return labels_.size(); }
   std::size_t dim() const noexcept { return dim_; }
+  // GPU kernel choice (0 auto, 1 CUDA-core scan, 2 tensor-core GEMM + exact
+  // rerank) and the one that answered the last search; no counterpart in the
+  // reference.
+  void set_gpu_path(int path);
+  int last_gpu_path() const noexcept { return last_path_; }
 
   struct Dev;
 
@@ -132,6 +137,8 @@ class BruteForceIndex {
   std::vector<float> data_;
   std::vector<uint64_t> labels_;
   mutable std::unique_ptr<Dev> dev_;
+  int path_ = 0;
+  mutable int last_path_ = 0;
 };
 
 }  // namespace hnsw

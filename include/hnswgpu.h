@@ -125,6 +125,11 @@ int hg_bruteforce_add(hg_bruteforce* bf, const float* vecs, const uint64_t* labe
 int hg_bruteforce_search_batch(const hg_bruteforce* bf, const float* qs, size_t nq, size_t k, hg_neighbor* out,
                                const hg_filter* filter);
 void hg_bruteforce_free(hg_bruteforce* bf);
+/* GPU kernel choice for brute force: 0 auto, 1 CUDA-core scan, 2 tensor-core
+ * GEMM with exact rerank; and the kernel that answered the last search.  No
+ * counterpart in the reference. */
+int hg_bruteforce_set_path(hg_bruteforce* bf, int path);
+int hg_bruteforce_last_path(const hg_bruteforce* bf);
 
 /* A batch that allocates nothing on the device.  For callers that cannot
  * call cudaMalloc while they search -- a serving process that runs next to

@@ -123,6 +123,15 @@ typedef struct hgd_flat hgd_flat;
 int hgd_flat_upload(const float* prepared, const uint64_t* labels, uint64_t n, uint64_t dim, int metric, int device,
                     int order, hgd_flat** out);
 void hgd_flat_free(hgd_flat* f);
+/* Which kernel answers hgd_bruteforce: HGD_BF_AUTO (the tensor-core GEMM
+ * with exact rerank where the shape allows, else the CUDA-core scan),
+ * HGD_BF_SCAN, or HGD_BF_TENSOR (HGD_EINVAL where unsupported).  No
+ * counterpart in the reference, which has one CPU scan. */
+enum { HGD_BF_AUTO = 0, HGD_BF_SCAN = 1, HGD_BF_TENSOR = 2 };
+int hgd_flat_set_path(hgd_flat* f, int path);
+/* The kernel that produced the last hgd_bruteforce answer (HGD_BF_SCAN or
+ * HGD_BF_TENSOR; 0 before the first call). */
+int hgd_flat_last_path(const hgd_flat* f);
 int hgd_bruteforce(hgd_flat* f, const float* queries, uint64_t nq, uint32_t k, const hgd_bitset* filter, void* out,
                    void* stream);
 
