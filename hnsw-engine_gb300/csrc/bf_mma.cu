@@ -17,8 +17,11 @@
 // row with s <= T + 2E, where T is the k-th smallest s, is kept; the true k
 // nearest (ties included) are among them, and their exact distances are then
 // computed in the reference's summation order and sorted by (distance, row).
-// For integer data with |v| <= 2048 and dim * (max|q| + max|x|)^2 < 2^24
-// every step is exact and E = 0.  A query whose candidates do not fit the
+// For integer data with |v| <= 2048, dim * max|q| * max|x| < 2^24 and
+// dim * max(|q|, |x|)^2 < 2^24 the products, the GEMM sums and the norms are
+// exact; every row whose true distance is below 2^24 then has s + |q|^2
+// equal to the reference's distance, so E = 0 whenever the k-th smallest
+// s + |q|^2 is below 2^24 (checked per query).  A query whose candidates do not fit the
 // buffers is reported, and the caller answers that batch with the
 // CUDA-core scan.
 #include <cuda.h>
@@ -440,7 +443,8 @@ struct DataBound {
 
 __global__ void prep_queries_kernel(const float* __restrict__ raw, const float* __restrict__ inv, uint32_t nq,
                                     uint32_t nq_pad, uint32_t dim, uint32_t kp, int l2, DataBound db,
-                                    __half* __restrict__ q16, float* __restrict__ qc, float* __restrict__ qm) {
+                                    __half* __restrict__ q16, float* __restrict__ qc, float* __restrict__ qm,
+                                    float* __restrict__ qq) {
   const uint64_t q = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (q >= nq_pad) return;
@@ -466,8 +470,9 @@ __global__ void prep_queries_kernel(const float* __restrict__ raw, const float* 
   isint = __all_sync(kFull, isint);
   const double d = static_cast<double>(dim);
   const double qn = sqrt(l2s) * (1.0 + 1e-12);
-  const bool exact = db.all_int && isint &&
-                     d * (static_cast<double>(mx) + db.xm) * (static_cast<double>(mx) + db.xm) < 16777216.0;
+  const double mq = mx;
+  const bool exact = db.all_int && isint && d * mq * db.xm < 16777216.0 && d * mq * mq < 16777216.0 &&
+                     d * static_cast<double>(db.xm) * db.xm < 16777216.0;
   float sigma_q = 1.0f;
   if (!exact && mx > 0.0f) {
     int e;
@@ -482,6 +487,7 @@ __global__ void prep_queries_kernel(const float* __restrict__ raw, const float* 
   if (lane != 0) return;
   const float unscale = 1.0f / (sigma_q * db.sigma_x);  // a power of two
   qc[q] = (l2 ? -2.0f : -1.0f) * unscale;
+  qq[q] = exact ? static_cast<float>(l2 ? l2s : 1.0) : -1.0f;  // exact: |q|^2 (L2) or 1 (IP), else -1
   if (exact) {
     qm[q] = 0.0f;
     return;
@@ -506,7 +512,8 @@ __global__ void prep_queries_kernel(const float* __restrict__ raw, const float* 
 // per query: k-th smallest over the splits, survivors within the margin
 // ---------------------------------------------------------------------------
 __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* __restrict__ cnt,
-                              const float* __restrict__ qm, uint32_t nq, uint32_t splits, uint32_t cap, uint32_t k,
+                              const float* __restrict__ qm, const float* __restrict__ qq, uint32_t nq,
+                              uint32_t splits, uint32_t cap, uint32_t k,
                               uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t* __restrict__ pool_n,
                               uint32_t* __restrict__ err) {
   const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -544,7 +551,17 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
       if (count_le(mid) >= k) hi = mid;
       else lo = mid + 1u;
     }
-    thr = __fadd_ru(dist_of_key_bits(lo), qm[q]);
+    const float T = dist_of_key_bits(lo);
+    thr = __fadd_ru(T, qm[q]);
+    // exact mode holds while the k-th distance is below 2^24 (where the
+    // reference's own sum is still exact); past it the scan answers
+    if (qq[q] >= 0.0f && static_cast<double>(T) + qq[q] >= 16777216.0) {
+      if (lane == 0) {
+        pool_n[q] = 0;
+        atomicAdd(err + 1, 1u);
+      }
+      return;
+    }
   }
   uint32_t w = 0;
   for (uint32_t s = 0; s < splits; ++s) {
@@ -769,7 +786,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
   while (p2max < pool_cap) p2max <<= 1;
 
   __half* q16 = nullptr;
-  float *qc = nullptr, *qm = nullptr;
+  float *qc = nullptr, *qm = nullptr, *qq = nullptr;
   uint64_t* buf = nullptr;
   uint32_t *cnt = nullptr, *pool = nullptr, *pool_n = nullptr, *derr = nullptr;
   cudaError_t e = cudaSuccess;
@@ -779,6 +796,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     if ((e = cudaMalloc(&q16, static_cast<size_t>(nq_pad) * s->kp * 2)) != cudaSuccess) break;
     if ((e = cudaMalloc(&qc, nq_pad * 4ull)) != cudaSuccess) break;
     if ((e = cudaMalloc(&qm, nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&qq, nq_pad * 4ull)) != cudaSuccess) break;
     if ((e = cudaMalloc(&buf, static_cast<size_t>(splits) * nq * cap * 8)) != cudaSuccess) break;
     if ((e = cudaMalloc(&cnt, static_cast<size_t>(splits) * nq * 4)) != cudaSuccess) break;
     if ((e = cudaMalloc(&pool, static_cast<size_t>(nq) * pool_cap * 4)) != cudaSuccess) break;
@@ -787,7 +805,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     if ((e = cudaMemsetAsync(derr, 0, 16, st)) != cudaSuccess) break;
     what = "query kernel";
     prep_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(nq_pad) * 32 + 255) / 256), 256, 0, st>>>(
-        queries, inv, nq, nq_pad, r.dim, s->kp, r.metric == HGD_METRIC_L2 ? 1 : 0, s->db, q16, qc, qm);
+        queries, inv, nq, nq_pad, r.dim, s->kp, r.metric == HGD_METRIC_L2 ? 1 : 0, s->db, q16, qc, qm, qq);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     CUtensorMap map_q;
     what = "tensor map";
@@ -822,8 +840,8 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "select kernel";
-    select_kernel<<<(nq * 32 + 255) / 256, 256, 0, st>>>(buf, cnt, qm, nq, splits, cap, k, pool, pool_cap, pool_n,
-                                                         derr);
+    select_kernel<<<(nq * 32 + 255) / 256, 256, 0, st>>>(buf, cnt, qm, qq, nq, splits, cap, k, pool, pool_cap,
+                                                         pool_n, derr);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
     const int S = slots_of(r.dim);
@@ -848,7 +866,8 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
   } while (false);
   if (e != cudaSuccess) *err = std::string("tensor brute force: ") + what + ": " + cudaGetErrorString(e);
   cudaStreamSynchronize(st);
-  for (void* p : {static_cast<void*>(q16), static_cast<void*>(qc), static_cast<void*>(qm), static_cast<void*>(buf),
+  for (void* p : {static_cast<void*>(q16), static_cast<void*>(qc), static_cast<void*>(qm), static_cast<void*>(qq),
+                  static_cast<void*>(buf),
                   static_cast<void*>(cnt), static_cast<void*>(pool), static_cast<void*>(pool_n),
                   static_cast<void*>(derr)})
     if (p) cudaFree(p);
