@@ -164,22 +164,38 @@ __device__ __forceinline__ float dist_of_key_bits(uint32_t kb) {
   return __uint_as_float(u);
 }
 
-// Keep the candidates of one query within T + margin, T the k-th smallest
-// distance among b[0..cnt) (cnt >= k).  Returns the count kept.
-__device__ __noinline__ uint32_t compact_keys(uint64_t* b, uint32_t cnt, uint32_t k, float margin, float* thr_out) {
-  uint32_t lo = 0u, hi = 0xFFFFFFFFu;
+// The warp compacts the candidate buffer of one of its lanes: T = the k-th
+// smallest distance among b[0..cnt) (cnt >= k, found by bisection on the
+// order-preserving key bits), then the keys within T + margin are kept.
+__device__ __noinline__ uint32_t warp_compact(uint64_t* b, uint32_t cnt, uint32_t k, float margin, int lane,
+                                              float* thr_out) {
+  uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+  for (uint32_t i = lane; i < cnt; i += 32) {
+    const uint32_t v = static_cast<uint32_t>(b[i] >> 32);
+    lo = min(lo, v);
+    hi = max(hi, v);
+  }
+  lo = __reduce_min_sync(kFull, lo);
+  hi = __reduce_max_sync(kFull, hi);
   while (lo < hi) {
     const uint32_t mid = lo + ((hi - lo) >> 1);
     uint32_t c = 0;
-    for (uint32_t i = 0; i < cnt; ++i) c += static_cast<uint32_t>(b[i] >> 32) <= mid ? 1u : 0u;
+    for (uint32_t i = lane; i < cnt; i += 32) c += static_cast<uint32_t>(b[i] >> 32) <= mid ? 1u : 0u;
+    c = __reduce_add_sync(kFull, c);
     if (c >= k) hi = mid;
     else lo = mid + 1u;
   }
   const float thr = __fadd_ru(dist_of_key_bits(lo), margin);
   uint32_t w = 0;
-  for (uint32_t i = 0; i < cnt; ++i) {
-    const uint64_t v = b[i];
-    if (key_dist(v) <= thr) b[w++] = v;
+  for (uint32_t base = 0; base < cnt; base += 32) {
+    const uint32_t i = base + lane;
+    const uint64_t v = i < cnt ? b[i] : 0ull;
+    const bool keep = i < cnt && key_dist(v) <= thr;
+    const uint32_t bal = __ballot_sync(kFull, keep);
+    __syncwarp();
+    if (keep) b[w + __popc(bal & ((1u << lane) - 1u))] = v;
+    w += __popc(bal);
+    __syncwarp();
   }
   *thr_out = thr;
   return w;
@@ -336,31 +352,51 @@ __global__ void __launch_bounds__(kThreads, 1)
           uint32_t r[32];
           tmem_ld32(taddr + ch * 32u, r);
           const uint32_t j0 = bt * BN + ch * 32u;
-          if (j0 >= P.n || !live_q || over) continue;
+          if (j0 >= P.n) continue;  // warp-uniform: padding rows of the last tile
           uint32_t valid = P.n - j0 >= 32u ? 0xFFFFFFFFu : ((1u << (P.n - j0)) - 1u);
           if (P.allow) valid &= __ldg(P.allow + (j0 >> 5));
-          float xn[32];
+          if (!live_q || over) valid = 0u;
+          float sv[32];
           const float4* x4 = reinterpret_cast<const float4*>(P.xn + j0);
 #pragma unroll
           for (int v = 0; v < 8; ++v) {
             const float4 t = __ldg(x4 + v);
-            xn[4 * v] = t.x;
-            xn[4 * v + 1] = t.y;
-            xn[4 * v + 2] = t.z;
-            xn[4 * v + 3] = t.w;
-          }
+            const float xs[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const float acc = __uint_as_float(r[c]);
-            const float s = P.l2 ? __fmaf_rn(acc, cq, xn[c]) : __fmul_rn(acc, cq);
-            if (((valid >> c) & 1u) && s <= thr) {
-              bufp[cnt] = (static_cast<uint64_t>(okey(s)) << 32) | (j0 + c);
-              if (++cnt == P.cap) {
-                cnt = compact_keys(bufp, cnt, P.k, margin, &thr);
-                if (cnt + 32u > P.cap) {  // the margin keeps too many rows: give this query up
-                  over = true;
-                  thr = -__int_as_float(0x7f800000);
-                }
+            for (int u = 0; u < 4; ++u) {
+              const float acc = __uint_as_float(r[4 * v + u]);
+              sv[4 * v + u] = P.l2 ? __fmaf_rn(acc, cq, xs[u]) : __fmul_rn(acc, cq);
+            }
+          }
+          if (valid != 0xFFFFFFFFu) {  // masked rows become NaN: never <= thr, ignored by fminf
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+              if (!((valid >> c) & 1u)) sv[c] = __int_as_float(0x7fffffff);
+          }
+          float mn = sv[0];
+#pragma unroll
+          for (int c = 1; c < 32; ++c) mn = fminf(mn, sv[c]);
+          if (mn <= thr) {  // rare once the threshold has settled
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+              if (sv[c] <= thr) bufp[cnt++] = (static_cast<uint64_t>(okey(sv[c])) << 32) | (j0 + c);
+          }
+          // room for the next chunk: compact the lanes that are nearly full
+          uint32_t need = __ballot_sync(kFull, cnt + 32u > P.cap);
+          while (need) {
+            const int L = __ffs(need) - 1;
+            need &= need - 1;
+            uint64_t* lb = reinterpret_cast<uint64_t*>(__shfl_sync(kFull, reinterpret_cast<unsigned long long>(bufp), L));
+            const uint32_t lc = __shfl_sync(kFull, cnt, L);
+            const float lm = __shfl_sync(kFull, margin, L);
+            float lthr;
+            const uint32_t kept = warp_compact(lb, lc, P.k, lm, lane, &lthr);
+            if (lane == L) {
+              cnt = kept;
+              thr = lthr;
+              if (cnt + 32u > P.cap) {  // the margin keeps too many rows: give this query up
+                over = true;
+                thr = -__int_as_float(0x7f800000);
               }
             }
           }
@@ -780,7 +816,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     splits = std::min<uint32_t>(nbt, (2u * static_cast<uint32_t>(s->sms) + tiles_q - 1) / tiles_q);
   const uint32_t tps = (nbt + splits - 1) / splits;
   splits = (nbt + tps - 1) / tps;
-  const uint32_t cap = std::max<uint32_t>(64, round_up(2 * k + 32, 32));
+  const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
   const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(splits * cap, 32), 32));
   uint32_t p2max = 1;
   while (p2max < pool_cap) p2max <<= 1;
