@@ -261,9 +261,11 @@ def run_ours(args, rank, world, local):
     }
     if rank == 0 and world == 1:
         result["cpu_baseline"] = cpu_baseline(gpath, queries, efs)
+        del ix
         if not args.no_serving:
-            del ix
             result["serving"] = run_serving(local)
+        if not args.no_precision:
+            result["precision"] = run_precision(local)
     return result
 
 
@@ -394,6 +396,70 @@ def run_serving(local):
     return out
 
 
+PREC_N, PREC_DIM, PREC_NQ = 200_000, 960, 5_000
+PREC_EFS = (40, 64, 128, 256, 512)
+
+
+def run_precision(local):
+    """Precision path at d=960: |N(0,1)| x per-dimension scale U[0.05, 1],
+    200,000 rows, 5,000 queries.  For FP32, FP16 and FP8-E4M3 (per-row scale)
+    traversal, each followed by the exact FP32 rerank: QPS and recall@10 per
+    ef, the error of the returned distances against FP64, and the error of
+    the compressed copies' traversal distances against FP64."""
+    import torch
+
+    import hnswgpu
+    import workloads
+
+    base, queries = workloads.scaled_abs_normal(PREC_N, PREC_DIM, PREC_NQ)
+    t0 = time.time()
+    ix = hnswgpu.Index(PREC_DIM, "l2", M, EFC)
+    ix.add(base, num_threads=0)
+    build_s = time.time() - t0
+    ix.set_device(local)
+    bf = hnswgpu.BruteForceIndex(PREC_DIM, "l2")
+    bf.add(base)
+    gt = bf.search_raw(queries, K)["label"].astype(np.int64)
+    del bf
+    b64 = base.astype(np.float64)
+    q64 = queries.astype(np.float64)
+
+    def fp64_dist(qi, ids):
+        return ((b64[ids] - q64[qi][:, None, :]) ** 2).sum(-1)
+
+    # traversal distances of the compressed copies on a sample of (query, row) pairs
+    rs = np.random.default_rng(7)
+    pq = rs.integers(0, PREC_NQ, 20_000)
+    px = rs.integers(0, PREC_N, 20_000)
+    exact = ((b64[px] - q64[pq]) ** 2).sum(-1)
+    x16 = base[px].astype(np.float16).astype(np.float64)
+    xt = torch.from_numpy(base[px])
+    sc = xt.abs().amax(1, keepdim=True) / 448.0
+    sc = torch.where(sc > 0, sc, torch.ones_like(sc))
+    x8 = ((xt / sc).to(torch.float8_e4m3fn).to(torch.float32) * sc).double().numpy()
+    trav = {}
+    for name, xx in (("fp16", x16), ("fp8_e4m3", x8)):
+        rel = np.abs(((xx - q64[pq]) ** 2).sum(-1) - exact) / np.maximum(exact, 1e-30)
+        trav[name] = {"mean_rel": float(rel.mean()), "max_rel": float(rel.max())}
+
+    out = {"workload": f"precision-L2-960: n={PREC_N} d={PREC_DIM} M={M} efC={EFC}, {PREC_NQ} queries, k={K}",
+           "build_s": round(build_s, 1), "traversal_distance_error_vs_fp64": trav, "variants": {}}
+    for name, prec in (("fp32", 0), ("fp16_rerank", 1), ("fp8_rerank", 2)):
+        rows = []
+        for ef in PREC_EFS:
+            ix.search_batch_ex(queries[:256], K, ef, precision=prec)  # warm-up (builds the copy once)
+            t = time.perf_counter()
+            rec = ix.search_batch_ex(queries, K, ef, precision=prec)
+            el = time.perf_counter() - t
+            got = rec["label"].astype(np.int64)
+            d64 = fp64_dist(np.arange(PREC_NQ), got)
+            rel = np.abs(rec["distance"].astype(np.float64) - d64) / np.maximum(d64, 1e-30)
+            rows.append({"ef": ef, "qps": round(PREC_NQ / el, 1), "recall_at_10": round(workloads.recall_at_k(got, gt), 4),
+                         "dist_mean_rel_err_vs_fp64": float(rel.mean()), "dist_max_rel_err_vs_fp64": float(rel.max())})
+        out["variants"][name] = rows
+    return out
+
+
 def cpu_baseline(gpath, queries, efs, sample=None):
     """The reference algorithm (oracle restatement of search_batch) on the host
     cores, grouped per ef like one reference call per group."""
@@ -450,6 +516,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-serving", action="store_true", help="skip the 1M serving measurement")
+    ap.add_argument("--no-precision", action="store_true", help="skip the d=960 precision measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
