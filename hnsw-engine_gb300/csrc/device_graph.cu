@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -129,6 +130,10 @@ struct Workspace {
   cudaEvent_t ev_fork = nullptr;
   cudaEvent_t done = nullptr;  // recorded after the batch's last use of this workspace
   bool busy = false;
+  // CUDA graph of one device-resident batch shape: captured on the second call
+  // with the same key, replayed after that
+  std::string graph_seen, graph_key;
+  cudaGraphExec_t graph_exec = nullptr;
   void release_all() {
     for (DBuf* d : {&q, &efq, &kq, &fsel, &fptrs, &fbits, &inv, &out, &nres, &counters, &work, &ovf_list, &pool, &pool_t2,
                     &bitmaps, &pool_big, &bitmaps_big, &owners, &lists, &pool_ids, &pool_n})
@@ -139,6 +144,10 @@ struct Workspace {
     for (cudaEvent_t e2 : ev_join) cudaEventDestroy(e2);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (done) cudaEventDestroy(done);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+    graph_key.clear();
+    graph_seen.clear();
     aux.clear();
     ev_join.clear();
     ev_fork = done = nullptr;
@@ -174,6 +183,9 @@ struct hgd_graph {
   std::mutex ws_mu;
   std::vector<std::unique_ptr<Workspace>> ws;
   PinnedBuf pin_patch;  // tombstone word staging
+  // autotuned launch shapes (guarded by ws_mu); version enters graph keys
+  std::vector<hgd_tune_entry> tune;
+  uint64_t tune_version = 0;
 };
 
 namespace {
@@ -186,15 +198,23 @@ class WorkspaceLease {
   // new one (up to kMaxWorkspaces batches in flight), else waits for the
   // oldest.  Buffers may then be grown safely: nothing on the GPU uses them.
   static constexpr size_t kMaxWorkspaces = 16;
-  explicit WorkspaceLease(hgd_graph* g) : g_(g) {
+  explicit WorkspaceLease(hgd_graph* g, const std::string* graph_key = nullptr) : g_(g) {
     Workspace* wait_for = nullptr;
     {
       std::lock_guard<std::mutex> lk(g->ws_mu);
-      for (auto& w : g->ws)
-        if (!w->busy && cudaEventQuery(w->done) == cudaSuccess) {
-          w_ = w.get();
-          break;
-        }
+      if (graph_key)  // a workspace holding this batch's graph (or about to capture it) comes first
+        for (auto& w : g->ws)
+          if (!w->busy && (w->graph_key == *graph_key || w->graph_seen == *graph_key) &&
+              cudaEventQuery(w->done) == cudaSuccess) {
+            w_ = w.get();
+            break;
+          }
+      if (!w_)
+        for (auto& w : g->ws)
+          if (!w->busy && cudaEventQuery(w->done) == cudaSuccess) {
+            w_ = w.get();
+            break;
+          }
       if (!w_ && g->ws.size() < kMaxWorkspaces) {
         auto nw = std::make_unique<Workspace>();
         if (cudaEventCreateWithFlags(&nw->done, cudaEventDisableTiming) != cudaSuccess) return;
@@ -229,6 +249,20 @@ class WorkspaceLease {
   cudaStream_t st_ = nullptr;
   bool st_set_ = false;
 };
+
+// The inputs a captured batch depends on: pointers, sizes, shape fields, the
+// tombstone switch and the tuning table in force.
+std::string graph_key_of(const hgd_search_args* a, bool any_deleted, uint64_t tune_version) {
+  char buf[512];
+  std::snprintf(buf, sizeof buf, "%p/%llu/%u/%u/%u/%u/%p/%p/%p/%p/%u/%u/%u/%u/%d/%llu", static_cast<const void*>(a->queries),
+                static_cast<unsigned long long>(a->nq), a->k, a->ef, a->ef_default, a->precision,
+                static_cast<const void*>(a->ef_per_query), static_cast<const void*>(a->k_per_query), a->out,
+                static_cast<const void*>(a->nres), a->hash_slots, a->cand_cap, a->warps_per_block, a->pool_cap,
+                any_deleted ? 1 : 0, static_cast<unsigned long long>(tune_version));
+  return buf;
+}
+
+int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStream_t st);
 
 }  // namespace
 
@@ -400,11 +434,58 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   if (a->num_filters && !a->filters) return fail(HGD_EINVAL, "hgd_search: null filter table");
   HG_CUDA(cudaSetDevice(g->device));
   cudaStream_t st = a->stream ? static_cast<cudaStream_t>(a->stream) : g->stream;
-  WorkspaceLease lease(g);
+  const bool graphable = a->use_graph && a->queries_on_device && a->out_on_device && !a->counters &&
+                         a->num_filters == 0 && !a->synchronize;
+  std::string key;
+  if (graphable) {
+    std::lock_guard<std::mutex> lk(g->ws_mu);
+    key = graph_key_of(a, g->num_deleted > 0, g->tune_version);
+  }
+  WorkspaceLease lease(g, graphable ? &key : nullptr);
   Workspace* w = lease.get();
   if (!w) return fail(HGD_ERUNTIME, "hgd_search: no workspace available (all held by calls in progress)");
   HG_CUDA(cudaStreamWaitEvent(st, w->done, 0));  // its previous batch has finished with it
   lease.on_stream(st);
+  if (!graphable) return enqueue_batch(g, a, w, st);
+  if (w->graph_exec && w->graph_key == key) {
+    HG_CUDA(cudaGraphLaunch(w->graph_exec, st));
+    return HGD_OK;
+  }
+  if (w->graph_seen != key) {  // first call of this shape: run it (sizes every buffer)
+    w->graph_seen = key;
+    return enqueue_batch(g, a, w, st);
+  }
+  // second call: capture the batch, then launch the graph
+  if (w->graph_exec) {
+    HG_CUDA(cudaGraphExecDestroy(w->graph_exec));
+    w->graph_exec = nullptr;
+    w->graph_key.clear();
+  }
+  HG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int rc = enqueue_batch(g, a, w, st);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+  if (rc != HGD_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (ec != cudaSuccess) return fail(HGD_ECUDA, std::string("hgd_search: graph capture: ") + cudaGetErrorString(ec));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return fail(HGD_ECUDA, std::string("hgd_search: graph instantiate: ") + cudaGetErrorString(ei));
+  w->graph_exec = exec;
+  w->graph_key = key;
+  HG_CUDA(cudaGraphLaunch(exec, st));
+  return HGD_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Everything one batch enqueues on `st` (also the body a CUDA graph captures).
+int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStream_t st) {
   const uint64_t nq = a->nq;
   const uint32_t dim = static_cast<uint32_t>(g->dim);
 
@@ -610,17 +691,38 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     int wpb, blocks;
     uint32_t slot_base;
   };
+  std::vector<hgd_tune_entry> tune;
+  {
+    std::lock_guard<std::mutex> lk(g->ws_mu);
+    tune = g->tune;
+  }
+  auto tuned = [&](uint32_t E) -> const hgd_tune_entry* {
+    static const uint32_t kNominal[] = {16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024};
+    uint32_t nominal = 0;
+    for (uint32_t hi : kNominal)
+      if (hi >= E) {
+        nominal = hi;
+        break;
+      }
+    for (const auto& t : tune)
+      if (t.precision == a->precision && t.ef_hi == nominal) return &t;
+    return nullptr;
+  };
   std::vector<Shape> shapes(spec.n);
   uint64_t slots_total = 0;
   for (uint32_t b = 0; b < spec.n; ++b) {
     Shape& sh = shapes[b];
     const uint32_t E = spec.hi[b];
+    const hgd_tune_entry* t = tuned(E);
     sh.R = round_up(E, 32);
-    sh.C = a->cand_cap ? a->cand_cap : std::max<uint32_t>(128, round_up(E + 32, 32));
-    sh.H = a->hash_slots ? a->hash_slots : (E <= 32 ? 1024u : (E <= 512 ? 2048u : 4096u));
+    sh.C = a->cand_cap ? a->cand_cap
+                       : (t && t->cand_cap ? t->cand_cap : std::max<uint32_t>(128, round_up(E + 32, 32)));
+    sh.H = a->hash_slots ? a->hash_slots
+                         : (t && t->hash_slots ? t->hash_slots : (E <= 32 ? 1024u : (E <= 512 ? 2048u : 4096u)));
     const uint32_t wbytes = hg::warp_smem_bytes(sh.H, sh.R, sh.C);
     sh.wpb = static_cast<int>(std::min<uint32_t>(4, (227u * 1024u) / wbytes));
-    if (a->warps_per_block) sh.wpb = std::min<int>(sh.wpb, static_cast<int>(a->warps_per_block));
+    const uint32_t want_wpb = a->warps_per_block ? a->warps_per_block : (t ? t->warps_per_block : 0u);
+    if (want_wpb) sh.wpb = std::min<int>(sh.wpb, static_cast<int>(want_wpb));
     if (sh.wpb < 1) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
     const int occ = prec == HGD_PREC_FP32
                         ? hg::search_occupancy(static_cast<uint32_t>(g->pd), g->metric, sh.wpb, sh.H, sh.R, sh.C)
@@ -763,6 +865,40 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
     if (*static_cast<uint32_t*>(w->pin_out.p) != 0)
       return fail(HGD_EINVAL, "hgd_search: a per-query ef or k exceeds the bound given for this batch");
   }
+  return HGD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hgd_graph_set_tuning(hgd_graph* g, const hgd_tune_entry* entries, uint32_t n) {
+  if (!g || (n && !entries)) return fail(HGD_EINVAL, "hgd_graph_set_tuning: null argument");
+  for (uint32_t i = 0; i < n; ++i) {
+    const hgd_tune_entry& e = entries[i];
+    if (e.precision > HGD_PREC_FP8 || (e.hash_slots && (e.hash_slots < 256 || (e.hash_slots & (e.hash_slots - 1)))) ||
+        (e.cand_cap && (e.cand_cap < 128 || e.cand_cap % 32)) || e.warps_per_block > 4)
+      return fail(HGD_EINVAL, "hgd_graph_set_tuning: bad entry");
+  }
+  std::lock_guard<std::mutex> lk(g->ws_mu);
+  g->tune.assign(entries, entries + n);
+  ++g->tune_version;
+  return HGD_OK;
+}
+
+uint32_t hgd_shape_smem_bytes(uint32_t hash_slots, uint32_t ef_hi, uint32_t cand_cap) {
+  return hg::warp_smem_bytes(hash_slots, round_up(ef_hi, 32), cand_cap);
+}
+
+int hgd_graph_device_info(const hgd_graph* g, char* name, uint32_t name_cap, uint32_t* sms) {
+  if (!g) return fail(HGD_EINVAL, "hgd_graph_device_info: null graph");
+  cudaDeviceProp p{};
+  HG_CUDA(cudaGetDeviceProperties(&p, g->device));
+  if (name && name_cap) {
+    std::strncpy(name, p.name, name_cap - 1);
+    name[name_cap - 1] = 0;
+  }
+  if (sms) *sms = static_cast<uint32_t>(p.multiProcessorCount);
   return HGD_OK;
 }
 

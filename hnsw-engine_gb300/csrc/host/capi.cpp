@@ -183,8 +183,31 @@ int hg_index_search_batch_ex(const hg_index* idx, const float* qs, size_t nq, si
       opt.pool_cap = o->pool_cap;
       opt.queries_on_device = o->queries_on_device != 0;
       opt.out_on_device = o->out_on_device != 0;
+      opt.use_graph = o->use_graph != 0;
     }
     idx->index.search_batch_ex(qs, nq, k, ef, reinterpret_cast<hnsw::Neighbor*>(out), opt);
+  });
+}
+
+int hg_index_autotune(hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef_max, int precision, char* json,
+                      size_t json_cap, size_t* json_len) {
+  return guarded([&] {
+    if (!idx || !qs) throw std::invalid_argument("autotune: null pointer");
+    const std::string out = hnsw::gb::autotune(*idx->index.impl(), qs, nq, static_cast<uint32_t>(k),
+                                               static_cast<uint32_t>(std::min<size_t>(ef_max, 1024)), precision);
+    if (json_len) *json_len = out.size() + 1;
+    if (json && json_cap) {
+      const size_t m = std::min(json_cap - 1, out.size());
+      std::memcpy(json, out.data(), m);
+      json[m] = 0;
+    }
+  });
+}
+
+int hg_index_set_tuning(hg_index* idx, const char* json) {
+  return guarded([&] {
+    if (!idx || !json) throw std::invalid_argument("set_tuning: null pointer");
+    hnsw::gb::apply_tuning_json(*idx->index.impl(), json);
   });
 }
 

@@ -149,6 +149,7 @@ struct Index::Impl {
   mutable std::mutex dev_mutex;
   mutable hgd_graph* dev = nullptr;
   mutable bool dev_stale = true;
+  std::vector<hgd_tune_entry> tuning;  // launch shapes per ef bucket (autotuner), re-applied on upload
 
   explicit Impl(const Params& p);
   ~Impl();
@@ -209,6 +210,13 @@ inline void to_bits(const Index::Impl& im, const Filter* f, FilterBits& out) {
 }  // namespace hnsw::gb
 
 namespace hnsw::gb {
+
+// launch-shape autotuner (tune.cpp): times candidate shapes per ef bucket on
+// a sample of queries, installs the fastest and returns the table as JSON
+std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t k, uint32_t ef_max, int precision);
+// installs a table written by autotune (entries of other graphs' devices are
+// kept: the shape fields are valid on any GPU)
+void apply_tuning_json(Index::Impl& im, const std::string& json);
 
 // continuous-batching server (server.cpp)
 class Server;

@@ -69,6 +69,7 @@ hgd_graph* Index::Impl::device_graph() const {
   hgd_graph* out = nullptr;
   const int rc = hgd_graph_upload(&v, device, order_of(isa), &out);
   if (rc != HGD_OK) rethrow(rc, "upload to GPU");
+  if (!tuning.empty()) hgd_graph_set_tuning(out, tuning.data(), static_cast<uint32_t>(tuning.size()));
   dev = out;
   dev_stale = false;
   return dev;
@@ -123,6 +124,7 @@ void Index::search_batch_ex(const float* qs, std::size_t nq, std::size_t k, std:
   a.queries_on_device = opt.queries_on_device ? 1 : 0;
   a.out_on_device = opt.out_on_device ? 1 : 0;
   a.synchronize = opt.out_on_device ? 0 : 1;
+  a.use_graph = opt.use_graph ? 1 : 0;
   a.hash_slots = opt.hash_slots;
   a.cand_cap = opt.cand_cap;
   a.warps_per_block = opt.warps_per_block;

@@ -37,7 +37,7 @@ class _Filter(C.Structure):
 class _BatchOptions(C.Structure):
     _fields_ = [("ef_per_query", C.c_void_p), ("k_per_query", C.c_void_p), ("filters", C.POINTER(_Filter)),
                 ("num_filters", C.c_size_t), ("filter_of_query", C.c_void_p), ("stream", C.c_void_p),
-                ("precision", C.c_int32), ("reserved", C.c_int32), ("counters", C.c_void_p),
+                ("precision", C.c_int32), ("use_graph", C.c_int32), ("counters", C.c_void_p),
                 ("hash_slots", C.c_uint32), ("cand_cap", C.c_uint32), ("warps_per_block", C.c_uint32),
                 ("pool_cap", C.c_uint32), ("queries_on_device", C.c_int32), ("out_on_device", C.c_int32)]
 
@@ -98,6 +98,8 @@ def lib():
         L.hg_bruteforce_search_batch.argtypes = [vp, vp, sz, sz, vp, C.POINTER(_Filter)]
         L.hg_bruteforce_free.argtypes = [vp]
         L.hg_index_search_batch_noalloc.argtypes = [vp, vp, sz, sz, sz, vp, vp]
+        L.hg_index_autotune.argtypes = [vp, vp, sz, sz, sz, i32, C.c_char_p, sz, C.POINTER(sz)]
+        L.hg_index_set_tuning.argtypes = [vp, C.c_char_p]
         L.hg_bruteforce_set_path.argtypes = [vp, i32]
         L.hg_bruteforce_last_path.argtypes = [vp]
         L.hg_server_create.argtypes = [vp, C.POINTER(_ServerConfig), C.POINTER(vp)]
@@ -332,17 +334,49 @@ class Index:
         return (out, cnt) if counters else out
 
     def search_device(self, q_ptr: int, nq: int, k: int, ef: int, out_ptr: int, stream: int = 0,
-                      ef_ptr: int = 0, k_ptr: int = 0):
+                      ef_ptr: int = 0, k_ptr: int = 0, graph: bool = False, precision: int = 0):
         """Enqueue a batch whose queries (nq x dim float32), optional per-query
         ef / k (uint32) and output records (nq x k x 16 bytes) live in device
-        memory; returns once the work is on `stream` (a cudaStream_t handle)."""
+        memory; returns once the work is on `stream` (a cudaStream_t handle).
+        graph=True: the launch sequence is captured into a CUDA graph on the
+        second call with the same pointers and shape and replayed after."""
         opt = _BatchOptions()
         opt.queries_on_device, opt.out_on_device = 1, 1
+        opt.use_graph = 1 if graph else 0
+        opt.precision = precision
         opt.ef_per_query = ef_ptr or None
         opt.k_per_query = k_ptr or None
         opt.stream = stream or None
         _check(lib().hg_index_search_batch_ex(self._h, C.c_void_p(q_ptr), nq, k, ef, C.c_void_p(out_ptr),
                                               C.byref(opt)))
+
+    def autotune(self, queries, k: int = 10, ef_max: int = 512, precision: int = 0, path=None) -> dict:
+        """Time the query kernel's launch shapes per ef bucket on these sample
+        queries, install the fastest and return the table (also written to
+        `path` as JSON when given)."""
+        import json
+
+        q, _ = self._queries(queries)
+        need = C.c_size_t(0)
+        buf = C.create_string_buffer(1 << 16)
+        _check(lib().hg_index_autotune(self._h, _ptr(q), q.shape[0], k, ef_max, precision, buf, len(buf),
+                                       C.byref(need)))
+        text = buf.value.decode()
+        if path is not None:
+            Path(path).write_text(text)
+        return json.loads(text)
+
+    def set_tuning(self, table):
+        """Install a table from autotune (a dict, a JSON string or a file path)."""
+        import json
+
+        if isinstance(table, dict):
+            text = json.dumps(table)
+        elif isinstance(table, (str, Path)) and Path(str(table)).exists():
+            text = Path(str(table)).read_text()
+        else:
+            text = str(table)
+        _check(lib().hg_index_set_tuning(self._h, text.encode()))
 
     def search_noalloc(self, q_ptr: int, nq: int, k: int, ef: int, out_ptr: int, stream: int = 0):
         """hg_index_search_batch_noalloc: a batch that allocates no device memory.

@@ -51,6 +51,9 @@ struct SearchOptions {
   /// device-resident batches: queries / ef / k (and out) are device pointers;
   /// with out_on_device the call only enqueues work on `stream`.
   bool queries_on_device = false, out_on_device = false;
+  /// device-resident batches without filters or counters: capture the launch
+  /// sequence into a CUDA graph (second call of a shape) and replay it
+  bool use_graph = false;
 };
 
 class Index {

@@ -74,7 +74,9 @@ typedef struct {
   const int32_t* filter_of_query;  /* nq entries, -1 = none; NULL = filter 0 for all */
   void* stream;                    /* cudaStream_t, NULL = the index's own */
   int32_t precision;               /* 0 fp32; 1 fp16; 2 fp8 traversal with exact fp32 rerank */
-  int32_t reserved;
+  int32_t use_graph;               /* 1 with device-resident queries and out (no filters or
+                                      counters): the batch is captured into a CUDA graph on its
+                                      second call with the same pointers and shape, then replayed */
   uint64_t* counters;              /* nq x 8 traversal counters or NULL */
   uint32_t hash_slots;             /* launch shape, 0 = automatic: visited-hash slots per warp */
   uint32_t cand_cap;               /* candidate head capacity per warp */
@@ -101,6 +103,15 @@ int hg_index_search_batch(const hg_index* idx, const float* qs, size_t nq, size_
                           size_t num_threads, const hg_filter* filter);
 int hg_index_search_batch_ex(const hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef,
                              hg_neighbor* out, const hg_batch_options* opt);
+
+/* Launch-shape autotuner (no counterpart in the reference): times the query
+ * kernel's candidate shapes per ef bucket (up to ef_max) on `qs` (nq sample
+ * queries, host memory), installs the fastest for `precision` and writes the
+ * table as JSON into json (capacity json_cap; *json_len = bytes needed).
+ * hg_index_set_tuning installs a table written earlier. */
+int hg_index_autotune(hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef_max, int precision, char* json,
+                      size_t json_cap, size_t* json_len);
+int hg_index_set_tuning(hg_index* idx, const char* json);
 
 int hg_index_mark_deleted(hg_index* idx, uint64_t label);
 int hg_index_is_deleted(const hg_index* idx, uint64_t label, int* out);

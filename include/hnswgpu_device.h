@@ -101,7 +101,10 @@ typedef struct {
   uint64_t* counters;            /* nullable host array, nq x HGD_NCOUNTERS */
   int32_t synchronize;           /* 1: return after the results are in `out`; 0: only enqueue on
                                     `stream` (host buffers must then be pinned and stay alive) */
-  int32_t reserved2;
+  int32_t use_graph;             /* 1 (device-resident queries and out, no filters or counters,
+                                    synchronize 0): the second call with the same pointers and
+                                    shape captures the batch into a CUDA graph, later calls
+                                    replay it */
   /* launch shape; 0 = chosen from ef (the autotuner's table) */
   uint32_t hash_slots;           /* visited hash per warp (power of two >= 256) */
   uint32_t cand_cap;             /* candidate head per warp (power of two >= 128) */
@@ -117,6 +120,24 @@ void hgd_graph_free(hgd_graph* g);
 uint64_t hgd_graph_device_bytes(const hgd_graph* g);
 
 int hgd_search(hgd_graph* g, const hgd_search_args* a);
+
+/* Launch shape of one ef bucket (bounds 16, 32, 64, 96, 128, 192, 256, 384,
+ * 512, 768, 1024) for one precision, as chosen by the autotuner; a batch
+ * without explicit shape fields uses the entry of each of its buckets.  No
+ * counterpart in the reference. */
+typedef struct {
+  uint32_t precision;
+  uint32_t ef_hi;
+  uint32_t hash_slots;
+  uint32_t cand_cap;
+  uint32_t warps_per_block;
+  uint32_t reserved;
+} hgd_tune_entry;
+int hgd_graph_set_tuning(hgd_graph* g, const hgd_tune_entry* entries, uint32_t n);
+/* Bytes of per-warp shared memory of a shape (validation for tuners). */
+uint32_t hgd_shape_smem_bytes(uint32_t hash_slots, uint32_t ef_hi, uint32_t cand_cap);
+/* Device name and SM count of the graph's GPU. */
+int hgd_graph_device_info(const hgd_graph* g, char* name, uint32_t name_cap, uint32_t* sms);
 
 /* Exact k-NN over n prepared vectors (dim, unpadded), labels per row. */
 typedef struct hgd_flat hgd_flat;
