@@ -172,21 +172,33 @@ def run_ours(args, rank, world, local):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
     ef_max = int(efs.max())
 
-    def step_device():
-        ix.search_device(q_d.data_ptr(), NQ, K, ef_max, out_d.data_ptr(), stream.cuda_stream, ef_ptr=ef_d.data_ptr())
+    # launch shapes per ef bucket: autotuned on separate sample queries (seed 2)
+    import workloads
+
+    _, sample = workloads.int_mixture(N_BASE, DIM, CLUSTERS, 4096, qseed=2)
+    sample_efs = np.random.default_rng(4).choice(np.array(EF_CHOICES, dtype=np.uint32), 4096)
+    t0 = time.time()
+    tuning = ix.autotune(sample, k=K, ef_max=int(efs.max()), precision=0, ef_per_query=sample_efs)
+    tune_s = time.time() - t0
+
+    def step_device(graph=False):
+        ix.search_device(q_d.data_ptr(), NQ, K, ef_max, out_d.data_ptr(), stream.cuda_stream, ef_ptr=ef_d.data_ptr(),
+                         graph=graph)
 
     # recall and traversal counters of this batch (untimed)
     rec, cnt = ix.search_batch_ex(queries, K, ef_per_query=efs, counters=True)
     got = rec["label"].astype(np.int64)
-    import workloads
 
     recall = workloads.recall_at_k(got, gt)
     alg_bytes = algorithmic_bytes(cnt)
 
+    # timed path: the batch's launch sequence replayed as one CUDA graph
+    # (captured on the second warm-up step); the plain-stream path is timed
+    # after it for comparison
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.zero_()
-            step_device()
+            step_device(graph=True)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -198,7 +210,7 @@ def run_ours(args, rank, world, local):
             for i in range(args.steps):
                 flush.zero_()
                 ev[i][0].record(stream)
-                step_device()
+                step_device(graph=True)
                 ev[i][1].record(stream)
             torch.cuda.synchronize()
             wall = time.perf_counter() - wall0
@@ -206,6 +218,18 @@ def run_ours(args, rank, world, local):
             torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     dev_ms = sum(step_ms)
+    # the same step launched kernel by kernel on forked streams
+    stream_ms = []
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup + args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step_device(graph=False)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                stream_ms.append(a.elapsed_time(b))
     # device output equals the host-path output
     dev_rec = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(NQ, K)
     if not np.array_equal(dev_rec["label"], rec["label"]):
@@ -248,6 +272,15 @@ def run_ours(args, rank, world, local):
         "config": {"workload": WORKLOAD, "global_batch": world * NQ, "recall_at_10": round(recall, 4),
                    "ef_mix": list(EF_CHOICES), "l2_flush": "256 MiB write before every timed step",
                    "parallelism": f"replicas x{world} (queries per replica fixed)", "build_s": round(build_s, 2),
+                   "launch": "one CUDA-graph replay per step (bucket kernel, per-ef-bucket persistent kernels on "
+                             "prioritised forked streams, rerun pass)",
+                   "streams_ms_per_step": round(statistics.median(stream_ms), 4),
+                   "autotune": {"seconds": round(tune_s, 2),
+                                "sample": "4096 seed-2 queries of the same mixture, ef from the same set (seed 4)",
+                                "buckets": {str(e["ef_hi"]): [e["hash_slots"], e["cand_cap"], e["warps_per_block"],
+                                                              round(e["default_us_per_query"] / max(e["us_per_query"], 1e-9), 3)]
+                                            for e in tuning["entries"]},
+                                "fields": "hash_slots, cand_cap, warps_per_block (0 = default), speed-up over default"},
                    "mean_l0_expansions": round(float(cnt[:, 2].mean()), 2),
                    "mean_l0_distances": round(float(cnt[:, 3].mean()), 2)},
         "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": int(NQ * DIM * 4 + NQ * 4),
@@ -305,6 +338,14 @@ def run_serving(local):
     build_s = time.time() - t0
     ix.set_device(local)
     bitsets = [hnswgpu.Bitset(workloads.mask_to_words(m), SERVE_N) for m in masks]
+    # launch shapes for both forms, tuned on separate queries (seed 2, same
+    # cluster centres) with the serving ef mix
+    _, sample = workloads.int_mixture(1, DIM, SERVE_CLUSTERS, 4096, qseed=2)
+    sample_efs = np.random.default_rng(8).choice(np.arange(16, 513, 16), 4096).astype(np.uint32)
+    t0 = time.time()
+    for prec in (0, 2):
+        ix.autotune(sample, k=10, ef_max=512, precision=prec, ef_per_query=sample_efs)
+    tune_s = time.time() - t0
     offs = np.concatenate([[0], np.cumsum(nqs)])
     total_q = int(offs[-1])
     req_rows = np.repeat(np.arange(SERVE_REQUESTS), nqs)
@@ -362,7 +403,7 @@ def run_serving(local):
     out = {"workload": f"serving-L2-1M: n={SERVE_N} d={DIM} M={M} efC={EFC}, {SERVE_REQUESTS} requests, "
                        f"{total_q} queries, 1..256 queries/request log-uniform, k in {{1,10,100}}, "
                        f"ef in {{16..512 step 16}}, 20% with a 10%-density bitset (pool of {SERVE_FILTERS})",
-           "build_s": round(build_s, 1), "queries": total_q,
+           "build_s": round(build_s, 1), "autotune_s": round(tune_s, 1), "queries": total_q,
            "plain_fp32_search_batch_per_request": {
                "qps": round(per_request_qps, 1), "requests": SERVE_PLAIN_REQUESTS,
                "note": "one search_batch call per request (the reference API: one k / ef / filter per call)"},

@@ -471,7 +471,7 @@ int hgd_search(hgd_graph* g, const hgd_search_args* a) {
   }
   if (ec != cudaSuccess) return fail(HGD_ECUDA, std::string("hgd_search: graph capture: ") + cudaGetErrorString(ec));
   cudaGraphExec_t exec = nullptr;
-  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  const cudaError_t ei = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(graph);
   if (ei != cudaSuccess) return fail(HGD_ECUDA, std::string("hgd_search: graph instantiate: ") + cudaGetErrorString(ei));
   w->graph_exec = exec;
@@ -787,10 +787,16 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   // fork: each bucket on its own stream, largest ef first, joined back into st
   if (w->aux.size() < spec.n) {
     if (!w->ev_fork) HG_CUDA(cudaEventCreateWithFlags(&w->ev_fork, cudaEventDisableTiming));
+    int least = 0, greatest = 0;
+    HG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     while (w->aux.size() < spec.n) {
       cudaStream_t s2 = nullptr;
       cudaEvent_t e2 = nullptr;
-      HG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+      // larger-ef buckets get higher priority: their blocks take the SMs first
+      // and the short queries fill in (also inside a captured graph)
+      const int b = static_cast<int>(w->aux.size());
+      const int prio = std::max(greatest, least - b / 2);
+      HG_CUDA(cudaStreamCreateWithPriority(&s2, cudaStreamNonBlocking, prio));
       HG_CUDA(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
       w->aux.push_back(s2);
       w->ev_join.push_back(e2);

@@ -189,12 +189,13 @@ int hg_index_search_batch_ex(const hg_index* idx, const float* qs, size_t nq, si
   });
 }
 
-int hg_index_autotune(hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef_max, int precision, char* json,
-                      size_t json_cap, size_t* json_len) {
+int hg_index_autotune(hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef_max, int precision,
+                      const uint32_t* ef_per_query, char* json, size_t json_cap, size_t* json_len) {
   return guarded([&] {
     if (!idx || !qs) throw std::invalid_argument("autotune: null pointer");
-    const std::string out = hnsw::gb::autotune(*idx->index.impl(), qs, nq, static_cast<uint32_t>(k),
-                                               static_cast<uint32_t>(std::min<size_t>(ef_max, 1024)), precision);
+    const std::string out =
+        hnsw::gb::autotune(*idx->index.impl(), qs, nq, static_cast<uint32_t>(k),
+                           static_cast<uint32_t>(std::min<size_t>(ef_max, 1024)), precision, ef_per_query);
     if (json_len) *json_len = out.size() + 1;
     if (json && json_cap) {
       const size_t m = std::min(json_cap - 1, out.size());

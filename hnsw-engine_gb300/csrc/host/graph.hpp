@@ -213,7 +213,8 @@ namespace hnsw::gb {
 
 // launch-shape autotuner (tune.cpp): times candidate shapes per ef bucket on
 // a sample of queries, installs the fastest and returns the table as JSON
-std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t k, uint32_t ef_max, int precision);
+std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t k, uint32_t ef_max, int precision,
+                     const uint32_t* ef_per_query);
 // installs a table written by autotune (entries of other graphs' devices are
 // kept: the shape fields are valid on any GPU)
 void apply_tuning_json(Index::Impl& im, const std::string& json);

@@ -7,7 +7,10 @@
 // (n, degree, dimension), the precision and the GPU, so it is measured: for
 // each bucket up to ef_max, every feasible shape of a small grid runs a
 // sample batch whose queries all carry the bucket's ef, timed with CUDA
-// events after a warm-up, and the fastest shape is kept.  The table goes to
+// events after a warm-up, and the fastest shape is kept.  Given per-query ef
+// for the sample, the buckets run concurrently as in a real mixed batch, so
+// the table is found on the whole batch's time instead: first one shape for
+// every bucket, then one bucket at a time, largest first.  The table goes to
 // the device mirror (hgd_graph_set_tuning) and to JSON for reuse.  No
 // counterpart in the reference (its search runs one query per CPU thread).
 #include <cuda_runtime.h>
@@ -45,7 +48,8 @@ uint32_t round_up32(uint32_t v) { return (v + 31u) / 32u * 32u; }
 
 }  // namespace
 
-std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t k, uint32_t ef_max, int precision) {
+std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t k, uint32_t ef_max, int precision,
+                     const uint32_t* ef_per_query) {
   if (!queries || nq == 0) throw std::invalid_argument("autotune: no sample queries");
   if (k == 0) throw std::invalid_argument("autotune: k must be > 0");
   if (precision < 0 || precision > 2) throw std::invalid_argument("autotune: precision must be 0, 1 or 2");
@@ -54,9 +58,16 @@ std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t 
   hgd_graph* g = im.device_graph();
   cuda_ok(cudaSetDevice(im.device), "device");
   const size_t dim = im.dim;
-  DevMem dq, dout;
+  DevMem dq, dout, def;
   cuda_ok(cudaMalloc(&dq.p, nq * dim * 4), "alloc");
   cuda_ok(cudaMemcpy(dq.p, queries, nq * dim * 4, cudaMemcpyHostToDevice), "copy");
+  uint32_t mix_max = 0;
+  if (ef_per_query) {
+    for (size_t i = 0; i < nq; ++i) mix_max = std::max(mix_max, std::max(ef_per_query[i], k));
+    if (mix_max == 0 || mix_max > 1024) throw std::invalid_argument("autotune: per-query ef must be in 1..1024");
+    cuda_ok(cudaMalloc(&def.p, nq * 4), "alloc");
+    cuda_ok(cudaMemcpy(def.p, ef_per_query, nq * 4, cudaMemcpyHostToDevice), "copy");
+  }
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
@@ -75,6 +86,7 @@ std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t 
   // time one shape (0 fields = the default rule): microseconds per query
   auto time_shape = [&](uint32_t ef, uint32_t kk, uint32_t H, uint32_t C, uint32_t wpb) -> double {
     hgd_search_args a{};
+    if (def.p) a.ef_per_query = static_cast<const uint32_t*>(def.p);
     a.queries = static_cast<const float*>(dq.p);
     a.queries_on_device = 1;
     a.out_on_device = 1;
@@ -111,7 +123,94 @@ std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t 
     std::vector<hgd_tune_entry> others = table;
     hgd_graph_set_tuning(g, others.data(), static_cast<uint32_t>(others.size()));
   }
+  if (ef_per_query) {
+    // ---- mixed batch: coordinate descent over the buckets present ----
+    std::vector<uint32_t> present;
+    for (size_t bi = 0; bi < sizeof(kBuckets) / sizeof(kBuckets[0]); ++bi) {
+      const uint32_t E = kBuckets[bi];
+      const uint32_t lo = bi == 0 ? 0u : kBuckets[bi - 1];
+      bool any = false;
+      for (size_t i = 0; i < nq && !any; ++i) {
+        const uint32_t e = std::max(ef_per_query[i], k);
+        any = e > lo && e <= E;
+      }
+      if (any) present.push_back(E);
+    }
+    std::vector<hgd_tune_entry> mine;
+    for (uint32_t E : present) mine.push_back(hgd_tune_entry{static_cast<uint32_t>(precision), E, 0, 0, 0, 0});
+    auto install = [&]() {
+      std::vector<hgd_tune_entry> all = table;
+      all.insert(all.end(), mine.begin(), mine.end());
+      if (hgd_graph_set_tuning(g, all.data(), static_cast<uint32_t>(all.size())) != HGD_OK)
+        throw std::runtime_error(std::string("autotune: ") + hgd_last_error());
+    };
+    cuda_ok(cudaMalloc(&dout.p, nq * k * 16), "alloc");
+    install();
+    const double t_default = time_shape(mix_max, k, 0, 0, 0);
+    double best = t_default;
+    // phase 1: one shape for every bucket (the buckets share the SMs, so
+    // shrinking all of them together is what frees room for more warps)
+    {
+      std::vector<hgd_tune_entry> keep = mine;
+      for (uint32_t H : {512u, 1024u, 2048u, 4096u})
+        for (int half = 0; half < 2; ++half)
+          for (uint32_t wpb : {1u, 2u, 4u}) {
+            for (size_t bi = 0; bi < present.size(); ++bi) {
+              const uint32_t E = present[bi];
+              const uint32_t C = std::max<uint32_t>(128, round_up32((half ? E / 2 : E) + 32));
+              mine[bi] = static_cast<uint64_t>(wpb) * hgd_shape_smem_bytes(H, E, C) <= kSmemPerBlock
+                             ? hgd_tune_entry{static_cast<uint32_t>(precision), E, H, C, wpb, 0}
+                             : hgd_tune_entry{static_cast<uint32_t>(precision), E, 0, 0, 0, 0};
+            }
+            install();
+            const double t = time_shape(mix_max, k, 0, 0, 0);
+            if (t < best * 0.995) {
+              best = t;
+              keep = mine;
+            }
+          }
+      mine = keep;
+      install();
+    }
+    // phase 2: one bucket at a time
+    for (int pass = 0; pass < 1; ++pass) {
+      for (size_t bi = present.size(); bi-- > 0;) {
+        const uint32_t E = present[bi];
+        const uint32_t c_full = std::max<uint32_t>(128, round_up32(E + 32));
+        const uint32_t c_half = std::max<uint32_t>(128, round_up32(E / 2 + 32));
+        hgd_tune_entry keep = mine[bi];
+        for (uint32_t H : {512u, 1024u, 2048u, 4096u})
+          for (uint32_t C : {c_full, c_half}) {
+            if (C == c_half && c_half == c_full) continue;
+            for (uint32_t wpb : {1u, 2u, 4u}) {
+              if (static_cast<uint64_t>(wpb) * hgd_shape_smem_bytes(H, E, C) > kSmemPerBlock) continue;
+              mine[bi] = hgd_tune_entry{static_cast<uint32_t>(precision), E, H, C, wpb, 0};
+              install();
+              const double t = time_shape(mix_max, k, 0, 0, 0);
+              if (t < best * 0.995) {
+                best = t;
+                keep = mine[bi];
+              }
+            }
+          }
+        mine[bi] = keep;
+        install();
+      }
+    }
+    for (size_t bi = 0; bi < present.size(); ++bi) {
+      const hgd_tune_entry& e = mine[bi];
+      char buf[256];
+      std::snprintf(buf, sizeof buf,
+                    "%s    {\"precision\": %d, \"ef_hi\": %u, \"hash_slots\": %u, \"cand_cap\": %u, "
+                    "\"warps_per_block\": %u, \"us_per_query\": %.4f, \"default_us_per_query\": %.4f}",
+                    rows.empty() ? "" : ",\n", precision, e.ef_hi, e.hash_slots, e.cand_cap, e.warps_per_block, best,
+                    t_default);
+      rows += buf;
+    }
+    table.insert(table.end(), mine.begin(), mine.end());
+  }
   for (uint32_t E : kBuckets) {
+    if (ef_per_query) break;
     const uint32_t kk = std::min(k, E);
     if (dout.p) {
       cudaFree(dout.p);

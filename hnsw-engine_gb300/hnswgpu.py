@@ -98,7 +98,7 @@ def lib():
         L.hg_bruteforce_search_batch.argtypes = [vp, vp, sz, sz, vp, C.POINTER(_Filter)]
         L.hg_bruteforce_free.argtypes = [vp]
         L.hg_index_search_batch_noalloc.argtypes = [vp, vp, sz, sz, sz, vp, vp]
-        L.hg_index_autotune.argtypes = [vp, vp, sz, sz, sz, i32, C.c_char_p, sz, C.POINTER(sz)]
+        L.hg_index_autotune.argtypes = [vp, vp, sz, sz, sz, i32, vp, C.c_char_p, sz, C.POINTER(sz)]
         L.hg_index_set_tuning.argtypes = [vp, C.c_char_p]
         L.hg_bruteforce_set_path.argtypes = [vp, i32]
         L.hg_bruteforce_last_path.argtypes = [vp]
@@ -350,16 +350,19 @@ class Index:
         _check(lib().hg_index_search_batch_ex(self._h, C.c_void_p(q_ptr), nq, k, ef, C.c_void_p(out_ptr),
                                               C.byref(opt)))
 
-    def autotune(self, queries, k: int = 10, ef_max: int = 512, precision: int = 0, path=None) -> dict:
+    def autotune(self, queries, k: int = 10, ef_max: int = 512, precision: int = 0, path=None,
+                 ef_per_query=None) -> dict:
         """Time the query kernel's launch shapes per ef bucket on these sample
         queries, install the fastest and return the table (also written to
-        `path` as JSON when given)."""
+        `path` as JSON when given).  With ef_per_query the sample runs as one
+        mixed batch and the shapes are chosen on its total time."""
         import json
 
         q, _ = self._queries(queries)
+        efq = None if ef_per_query is None else np.ascontiguousarray(ef_per_query, dtype=np.uint32)
         need = C.c_size_t(0)
         buf = C.create_string_buffer(1 << 16)
-        _check(lib().hg_index_autotune(self._h, _ptr(q), q.shape[0], k, ef_max, precision, buf, len(buf),
+        _check(lib().hg_index_autotune(self._h, _ptr(q), q.shape[0], k, ef_max, precision, _ptr(efq), buf, len(buf),
                                        C.byref(need)))
         text = buf.value.decode()
         if path is not None:

@@ -21,13 +21,14 @@ from __future__ import annotations
 import numpy as np
 
 
-def int_mixture(n: int, d: int, clusters: int, nq: int, sigma: float = 20.0):
-    """Base (n, d) and query (nq, d) float32 arrays holding integers 0..255."""
+def int_mixture(n: int, d: int, clusters: int, nq: int, sigma: float = 20.0, qseed: int = 1):
+    """Base (n, d) and query (nq, d) float32 arrays holding integers 0..255
+    (queries from seed `qseed`, 1 for every benchmark workload)."""
     r0 = np.random.default_rng(0)
     centers = r0.uniform(0.0, 128.0, size=(clusters, d))
     c = r0.integers(0, clusters, size=n)
     base = np.clip(np.rint(centers[c] + r0.normal(0.0, sigma, size=(n, d))), 0, 255).astype(np.float32)
-    r1 = np.random.default_rng(1)
+    r1 = np.random.default_rng(qseed)
     cq = r1.integers(0, clusters, size=nq)
     queries = np.clip(np.rint(centers[cq] + r1.normal(0.0, sigma, size=(nq, d))), 0, 255).astype(np.float32)
     return base, queries

@@ -108,9 +108,11 @@ int hg_index_search_batch_ex(const hg_index* idx, const float* qs, size_t nq, si
  * kernel's candidate shapes per ef bucket (up to ef_max) on `qs` (nq sample
  * queries, host memory), installs the fastest for `precision` and writes the
  * table as JSON into json (capacity json_cap; *json_len = bytes needed).
- * hg_index_set_tuning installs a table written earlier. */
-int hg_index_autotune(hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef_max, int precision, char* json,
-                      size_t json_cap, size_t* json_len);
+ * With ef_per_query (host, nq entries) the sample runs as one mixed batch and
+ * the shapes are chosen on its total time.  hg_index_set_tuning installs a
+ * table written earlier. */
+int hg_index_autotune(hg_index* idx, const float* qs, size_t nq, size_t k, size_t ef_max, int precision,
+                      const uint32_t* ef_per_query, char* json, size_t json_cap, size_t* json_len);
 int hg_index_set_tuning(hg_index* idx, const char* json);
 
 int hg_index_mark_deleted(hg_index* idx, uint64_t label);
