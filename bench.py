@@ -181,12 +181,17 @@ def run_ours(args, rank, world, local):
     tuning = ix.autotune(sample, k=K, ef_max=int(efs.max()), precision=0, ef_per_query=sample_efs)
     tune_s = time.time() - t0
 
+    use_graph = args.launch == "graph"
+
     def step_device(graph=False):
         ix.search_device(q_d.data_ptr(), NQ, K, ef_max, out_d.data_ptr(), stream.cuda_stream, ef_ptr=ef_d.data_ptr(),
                          graph=graph)
 
-    # recall and traversal counters of this batch (untimed)
+    # recall and traversal counters of this batch (untimed; an NVTX range so a
+    # profiler can pick these launches out)
+    torch.cuda.nvtx.range_push("counters_batch")
     rec, cnt = ix.search_batch_ex(queries, K, ef_per_query=efs, counters=True)
+    torch.cuda.nvtx.range_pop()
     got = rec["label"].astype(np.int64)
 
     recall = workloads.recall_at_k(got, gt)
@@ -198,7 +203,7 @@ def run_ours(args, rank, world, local):
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.zero_()
-            step_device(graph=True)
+            step_device(graph=use_graph)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -206,30 +211,33 @@ def run_ours(args, rank, world, local):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         clocks = Clocks(local)
         with clocks:
+            torch.cuda.nvtx.range_push("timed_steps")
             wall0 = time.perf_counter()
             for i in range(args.steps):
                 flush.zero_()
                 ev[i][0].record(stream)
-                step_device(graph=True)
+                step_device(graph=use_graph)
                 ev[i][1].record(stream)
             torch.cuda.synchronize()
             wall = time.perf_counter() - wall0
+            torch.cuda.nvtx.range_pop()
         if world > 1:
             torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     dev_ms = sum(step_ms)
     # the same step launched kernel by kernel on forked streams
     stream_ms = []
-    with torch.cuda.stream(stream):
-        for i in range(args.warmup + args.steps):
-            flush.zero_()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            step_device(graph=False)
-            b.record(stream)
-            torch.cuda.synchronize()
-            if i >= args.warmup:
-                stream_ms.append(a.elapsed_time(b))
+    if use_graph:
+        with torch.cuda.stream(stream):
+            for i in range(args.warmup + args.steps):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                step_device(graph=False)
+                b.record(stream)
+                torch.cuda.synchronize()
+                if i >= args.warmup:
+                    stream_ms.append(a.elapsed_time(b))
     # device output equals the host-path output
     dev_rec = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(NQ, K)
     if not np.array_equal(dev_rec["label"], rec["label"]):
@@ -272,9 +280,9 @@ def run_ours(args, rank, world, local):
         "config": {"workload": WORKLOAD, "global_batch": world * NQ, "recall_at_10": round(recall, 4),
                    "ef_mix": list(EF_CHOICES), "l2_flush": "256 MiB write before every timed step",
                    "parallelism": f"replicas x{world} (queries per replica fixed)", "build_s": round(build_s, 2),
-                   "launch": "one CUDA-graph replay per step (bucket kernel, per-ef-bucket persistent kernels on "
-                             "prioritised forked streams, rerun pass)",
-                   "streams_ms_per_step": round(statistics.median(stream_ms), 4),
+                   "launch": ("one CUDA-graph replay per step" if use_graph else "kernel launches per step") +
+                             " (bucket kernel, per-ef-bucket persistent kernels on prioritised forked streams, rerun pass)",
+                   "streams_ms_per_step": round(statistics.median(stream_ms), 4) if stream_ms else None,
                    "autotune": {"seconds": round(tune_s, 2),
                                 "sample": "4096 seed-2 queries of the same mixture, ef from the same set (seed 4)",
                                 "buckets": {str(e["ef_hi"]): [e["hash_slots"], e["cand_cap"], e["warps_per_block"],
@@ -558,6 +566,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-serving", action="store_true", help="skip the 1M serving measurement")
     ap.add_argument("--no-precision", action="store_true", help="skip the d=960 precision measurement")
+    ap.add_argument("--launch", choices=["graph", "streams"], default="graph",
+                    help="timed step: one CUDA-graph replay, or kernel launches on forked streams")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -560,7 +560,7 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
   for (uint32_t s = 0; s < splits; ++s) {
     const uint32_t c = cnt[static_cast<size_t>(s) * nq + q];
     if (c == kOver) over = true;
-    else total += c;
+    else total += min(c, cap);
   }
   if (over) {
     if (lane == 0) {
@@ -572,7 +572,7 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
   auto count_le = [&](uint32_t bound) {
     uint32_t c = 0;
     for (uint32_t s = 0; s < splits; ++s) {
-      const uint32_t m = cnt[static_cast<size_t>(s) * nq + q];
+      const uint32_t m = min(cnt[static_cast<size_t>(s) * nq + q], cap);
       const uint64_t* b = buf + (static_cast<size_t>(s) * nq + q) * cap;
       for (uint32_t i = lane; i < m; i += 32) c += static_cast<uint32_t>(b[i] >> 32) <= bound ? 1u : 0u;
     }
@@ -601,7 +601,7 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
   }
   uint32_t w = 0;
   for (uint32_t s = 0; s < splits; ++s) {
-    const uint32_t m = cnt[static_cast<size_t>(s) * nq + q];
+    const uint32_t m = min(cnt[static_cast<size_t>(s) * nq + q], cap);
     const uint64_t* b = buf + (static_cast<size_t>(s) * nq + q) * cap;
     for (uint32_t base = 0; base < m; base += 32) {
       const uint32_t i = base + lane;
@@ -835,6 +835,8 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     if ((e = cudaMalloc(&qq, nq_pad * 4ull)) != cudaSuccess) break;
     if ((e = cudaMalloc(&buf, static_cast<size_t>(splits) * nq * cap * 8)) != cudaSuccess) break;
     if ((e = cudaMalloc(&cnt, static_cast<size_t>(splits) * nq * 4)) != cudaSuccess) break;
+    // counts of (split, query) pairs an aborted CTA never reached read as 0
+    if ((e = cudaMemsetAsync(cnt, 0, static_cast<size_t>(splits) * nq * 4, st)) != cudaSuccess) break;
     if ((e = cudaMalloc(&pool, static_cast<size_t>(nq) * pool_cap * 4)) != cudaSuccess) break;
     if ((e = cudaMalloc(&pool_n, nq * 4ull)) != cudaSuccess) break;
     if ((e = cudaMalloc(&derr, 16)) != cudaSuccess) break;

@@ -821,7 +821,9 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
 
   DP dp;
   dp.init(P);
-  const uint32_t nq = P.nq_dev ? *P.nq_dev : P.nq;
+  // a queue length read from the device never exceeds the batch (its list
+  // holds at most P.nq entries)
+  const uint32_t nq = P.nq_dev ? min(*P.nq_dev, P.nq) : P.nq;
   const bool single_chunk = P.M0 <= 32;
 
   for (;;) {
@@ -830,6 +832,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
     item = __shfl_sync(kFull, item, 0);
     if (item >= nq) break;
     const uint32_t q = P.qidx ? P.qidx[item] : item;
+    if (q >= P.nq) continue;  // list entries are query indices of this batch
 
     uint32_t k = P.kq ? P.kq[q] : P.k_all;
     uint32_t ef = P.efq ? P.efq[q] : P.ef_all;
@@ -1070,7 +1073,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
     if (c.overflow) {
       if (lane == 0) {
         const uint32_t o = atomicAdd(P.ovf_count, 1u);
-        P.ovf_list[o] = q;
+        if (o < P.nq) P.ovf_list[o] = q;  // at most one entry per query of the batch
       }
       continue;
     }
