@@ -175,8 +175,8 @@ def run_ours(args, rank, world, local):
     # launch shapes per ef bucket: autotuned on separate sample queries (seed 2)
     import workloads
 
-    _, sample = workloads.int_mixture(N_BASE, DIM, CLUSTERS, 4096, qseed=2)
-    sample_efs = np.random.default_rng(4).choice(np.array(EF_CHOICES, dtype=np.uint32), 4096)
+    _, sample = workloads.int_mixture(N_BASE, DIM, CLUSTERS, NQ, qseed=2)
+    sample_efs = np.random.default_rng(4).choice(np.array(EF_CHOICES, dtype=np.uint32), NQ)
     t0 = time.time()
     tuning = ix.autotune(sample, k=K, ef_max=int(efs.max()), precision=0, ef_per_query=sample_efs)
     tune_s = time.time() - t0
@@ -284,7 +284,8 @@ def run_ours(args, rank, world, local):
                              " (bucket kernel, per-ef-bucket persistent kernels on prioritised forked streams, rerun pass)",
                    "streams_ms_per_step": round(statistics.median(stream_ms), 4) if stream_ms else None,
                    "autotune": {"seconds": round(tune_s, 2),
-                                "sample": "4096 seed-2 queries of the same mixture, ef from the same set (seed 4)",
+                                "sample": f"{NQ} seed-2 queries of the same mixture, ef from the same set (seed 4)",
+                                "launch_mode": ["per-bucket launches", "one largest-ef-first launch"][tuning["launch_mode"]],
                                 "buckets": {str(e["ef_hi"]): [e["hash_slots"], e["cand_cap"], e["warps_per_block"],
                                                               round(e["default_us_per_query"] / max(e["us_per_query"], 1e-9), 3)]
                                             for e in tuning["entries"]},

@@ -185,6 +185,7 @@ struct hgd_graph {
   PinnedBuf pin_patch;  // tombstone word staging
   // autotuned launch shapes (guarded by ws_mu); version enters graph keys
   std::vector<hgd_tune_entry> tune;
+  int launch_mode = HGD_LAUNCH_BUCKETS;
   uint64_t tune_version = 0;
 };
 
@@ -692,10 +693,13 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     uint32_t slot_base;
   };
   std::vector<hgd_tune_entry> tune;
+  int launch_mode = HGD_LAUNCH_BUCKETS;
   {
     std::lock_guard<std::mutex> lk(g->ws_mu);
     tune = g->tune;
+    launch_mode = g->launch_mode;
   }
+  const bool single = launch_mode == HGD_LAUNCH_SINGLE && spec.n > 1;
   auto tuned = [&](uint32_t E) -> const hgd_tune_entry* {
     static const uint32_t kNominal[] = {16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024};
     uint32_t nominal = 0;
@@ -732,8 +736,9 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     const uint64_t want = (nq + sh.wpb - 1) / sh.wpb;
     sh.blocks = static_cast<int>(std::min<uint64_t>(want, static_cast<uint64_t>(g->sms) * occ));
     sh.slot_base = static_cast<uint32_t>(slots_total);
-    slots_total += static_cast<uint64_t>(sh.blocks) * sh.wpb;
+    if (!single || b + 1 == spec.n) slots_total += static_cast<uint64_t>(sh.blocks) * sh.wpb;
   }
+  if (single) shapes.back().slot_base = 0;
   // shared scratch: spill pools and visited bitmaps acquired per query
   const uint64_t bw = (g->n + 31) / 32 + 1;
   const uint64_t pool_cap = a->pool_cap ? std::max<uint64_t>(a->pool_cap, 32)
@@ -802,6 +807,22 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
       w->ev_join.push_back(e2);
     }
   }
+  if (single) {
+    // one persistent launch, the largest bucket's shape, every query
+    const Shape& sh = shapes.back();
+    hg::SearchParams B = P;
+    B.H = sh.H;
+    B.R = sh.R;
+    B.C = sh.C;
+    B.qidx = w->lists.as<uint32_t>();
+    B.lpt_sizes = work + 32;
+    B.lpt_buckets = spec.n;
+    B.lpt_stride = static_cast<uint32_t>(nq);
+    B.work = work + 8;
+    B.slot_base = 0;
+    cudaError_t e = launch(B, sh.blocks, sh.wpb, st);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("search kernel launch: ") + cudaGetErrorString(e));
+  } else {
   HG_CUDA(cudaEventRecord(w->ev_fork, st));
   for (int b = static_cast<int>(spec.n) - 1; b >= 0; --b) {
     const Shape& sh = shapes[b];
@@ -820,6 +841,7 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     HG_CUDA(cudaEventRecord(w->ev_join[b], sb));
   }
   for (uint32_t b = 0; b < spec.n; ++b) HG_CUDA(cudaStreamWaitEvent(st, w->ev_join[b], 0));
+  }
   // ---- rerun of queries that ran out of spill pool or bitmap: per-warp pool of n keys ----
   {
     const uint64_t rerun_slots = 32;
@@ -888,6 +910,15 @@ int hgd_graph_set_tuning(hgd_graph* g, const hgd_tune_entry* entries, uint32_t n
   }
   std::lock_guard<std::mutex> lk(g->ws_mu);
   g->tune.assign(entries, entries + n);
+  ++g->tune_version;
+  return HGD_OK;
+}
+
+int hgd_graph_set_launch_mode(hgd_graph* g, int mode) {
+  if (!g || (mode != HGD_LAUNCH_BUCKETS && mode != HGD_LAUNCH_SINGLE))
+    return fail(HGD_EINVAL, "hgd_graph_set_launch_mode: bad argument");
+  std::lock_guard<std::mutex> lk(g->ws_mu);
+  g->launch_mode = mode;
   ++g->tune_version;
   return HGD_OK;
 }

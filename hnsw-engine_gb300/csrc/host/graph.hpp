@@ -150,6 +150,7 @@ struct Index::Impl {
   mutable hgd_graph* dev = nullptr;
   mutable bool dev_stale = true;
   std::vector<hgd_tune_entry> tuning;  // launch shapes per ef bucket (autotuner), re-applied on upload
+  int launch_mode = HGD_LAUNCH_BUCKETS;  // per-bucket launches or one largest-ef-first launch
 
   explicit Impl(const Params& p);
   ~Impl();

@@ -70,6 +70,7 @@ hgd_graph* Index::Impl::device_graph() const {
   const int rc = hgd_graph_upload(&v, device, order_of(isa), &out);
   if (rc != HGD_OK) rethrow(rc, "upload to GPU");
   if (!tuning.empty()) hgd_graph_set_tuning(out, tuning.data(), static_cast<uint32_t>(tuning.size()));
+  hgd_graph_set_launch_mode(out, launch_mode);
   dev = out;
   dev_stale = false;
   return dev;

@@ -114,6 +114,7 @@ std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t 
     return best * 1e3 / static_cast<double>(nq);
   };
 
+  int launch_mode = im.launch_mode;
   std::vector<hgd_tune_entry> table;
   for (const auto& t : im.tuning)
     if (static_cast<int>(t.precision) != precision) table.push_back(t);  // keep other precisions
@@ -145,6 +146,7 @@ std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t 
         throw std::runtime_error(std::string("autotune: ") + hgd_last_error());
     };
     cuda_ok(cudaMalloc(&dout.p, nq * k * 16), "alloc");
+    hgd_graph_set_launch_mode(g, HGD_LAUNCH_BUCKETS);
     install();
     const double t_default = time_shape(mix_max, k, 0, 0, 0);
     double best = t_default;
@@ -197,6 +199,43 @@ std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t 
         install();
       }
     }
+    // the other launch mode: one largest-ef-first launch with the top
+    // bucket's shape (the only entry it reads)
+    int mode = HGD_LAUNCH_BUCKETS;
+    {
+      const std::vector<hgd_tune_entry> bucket_table = mine;
+      hgd_graph_set_launch_mode(g, HGD_LAUNCH_SINGLE);
+      const size_t top = present.size() - 1;
+      const uint32_t E = present[top];
+      const uint32_t c_full = std::max<uint32_t>(128, round_up32(E + 32));
+      const uint32_t c_half = std::max<uint32_t>(128, round_up32(E / 2 + 32));
+      double best_single = std::numeric_limits<double>::infinity();
+      hgd_tune_entry keep = mine[top];
+      for (uint32_t H : {512u, 1024u, 2048u, 4096u})
+        for (uint32_t C : {c_full, c_half}) {
+          if (C == c_half && c_half == c_full) continue;
+          for (uint32_t wpb : {1u, 2u, 4u}) {
+            if (static_cast<uint64_t>(wpb) * hgd_shape_smem_bytes(H, E, C) > kSmemPerBlock) continue;
+            mine[top] = hgd_tune_entry{static_cast<uint32_t>(precision), E, H, C, wpb, 0};
+            install();
+            const double t = time_shape(mix_max, k, 0, 0, 0);
+            if (t < best_single) {
+              best_single = t;
+              keep = mine[top];
+            }
+          }
+        }
+      if (best_single < best * 0.995) {
+        mode = HGD_LAUNCH_SINGLE;
+        best = best_single;
+        mine[top] = keep;
+      } else {
+        mine = bucket_table;
+        hgd_graph_set_launch_mode(g, HGD_LAUNCH_BUCKETS);
+      }
+      install();
+    }
+    launch_mode = mode;
     for (size_t bi = 0; bi < present.size(); ++bi) {
       const hgd_tune_entry& e = mine[bi];
       char buf[256];
@@ -253,6 +292,7 @@ std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t 
   {
     std::lock_guard<std::mutex> dg(im.dev_mutex);
     im.tuning = table;
+    im.launch_mode = launch_mode;
   }
   char name[256] = {0};
   uint32_t sms = 0;
@@ -260,8 +300,8 @@ std::string autotune(Index::Impl& im, const float* queries, size_t nq, uint32_t 
   char head[512];
   std::snprintf(head, sizeof head,
                 "{\n  \"device\": \"%s\", \"sms\": %u, \"n\": %zu, \"dim\": %zu, \"M\": %zu, \"metric\": %d,\n"
-                "  \"sample_queries\": %zu, \"k\": %u,\n  \"entries\": [\n",
-                name, sms, im.count, im.dim, im.M, static_cast<int>(im.params.metric), nq, k);
+                "  \"sample_queries\": %zu, \"k\": %u, \"launch_mode\": %d,\n  \"entries\": [\n",
+                name, sms, im.count, im.dim, im.M, static_cast<int>(im.params.metric), nq, k, launch_mode);
   return std::string(head) + rows + "\n  ]\n}\n";
 }
 
@@ -300,13 +340,19 @@ void apply_tuning_json(Index::Impl& im, const std::string& json) {
     table.push_back(e);
     pos = b + 1;
   }
+  uint32_t mode = static_cast<uint32_t>(im.launch_mode);
+  const size_t mpos = json.find("\"launch_mode\"");
+  if (mpos != std::string::npos && mpos < list) field(json.substr(mpos, 32), "launch_mode", &mode);
+  if (mode > 1) throw std::invalid_argument("tuning: launch_mode must be 0 or 1");
   std::unique_lock<std::shared_mutex> lk(im.api_mutex);
   std::lock_guard<std::mutex> g(im.dev_mutex);
   if (im.dev && !table.empty()) {
     const int rc = hgd_graph_set_tuning(im.dev, table.data(), static_cast<uint32_t>(table.size()));
     if (rc != HGD_OK) throw std::invalid_argument(std::string("tuning: ") + hgd_last_error());
   }
+  if (im.dev) hgd_graph_set_launch_mode(im.dev, static_cast<int>(mode));
   im.tuning = table;
+  im.launch_mode = static_cast<int>(mode);
 }
 
 }  // namespace hnsw::gb

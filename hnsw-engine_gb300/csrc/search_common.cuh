@@ -32,6 +32,10 @@ struct SearchParams {
   uint32_t nq;
   const uint32_t* nq_dev;   // if set, nq is read from here (rerun pass)
   const uint32_t* qidx;     // if set, the i-th work item is query qidx[i]
+  // one launch over all ef buckets, largest ef first: work item i maps into
+  // the bucket lists qidx[b * lpt_stride ...] from bucket lpt_buckets-1 down
+  const uint32_t* lpt_sizes;
+  uint32_t lpt_buckets, lpt_stride;
   const uint32_t* efq;      // per query ef (0 = default) or null
   const uint32_t* kq;       // per query k or null
   uint32_t ef_all, ef_default, k_all, k_stride;

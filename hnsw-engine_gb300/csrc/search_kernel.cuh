@@ -823,7 +823,12 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
   dp.init(P);
   // a queue length read from the device never exceeds the batch (its list
   // holds at most P.nq entries)
-  const uint32_t nq = P.nq_dev ? min(*P.nq_dev, P.nq) : P.nq;
+  uint32_t nq = P.nq_dev ? min(*P.nq_dev, P.nq) : P.nq;
+  if (P.lpt_sizes) {
+    nq = 0;
+    for (uint32_t b = 0; b < P.lpt_buckets; ++b) nq += P.lpt_sizes[b];
+    nq = min(nq, P.nq);
+  }
   const bool single_chunk = P.M0 <= 32;
 
   for (;;) {
@@ -831,7 +836,18 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
     if (lane == 0) item = atomicAdd(P.work, 1u);
     item = __shfl_sync(kFull, item, 0);
     if (item >= nq) break;
-    const uint32_t q = P.qidx ? P.qidx[item] : item;
+    uint32_t q;
+    if (P.lpt_sizes) {  // largest-ef bucket first (longest queries start first)
+      uint32_t rem = item;
+      uint32_t b = P.lpt_buckets - 1;
+      while (b > 0 && rem >= P.lpt_sizes[b]) {
+        rem -= P.lpt_sizes[b];
+        --b;
+      }
+      q = P.qidx[static_cast<size_t>(b) * P.lpt_stride + rem];
+    } else {
+      q = P.qidx ? P.qidx[item] : item;
+    }
     if (q >= P.nq) continue;  // list entries are query indices of this batch
 
     uint32_t k = P.kq ? P.kq[q] : P.k_all;

@@ -134,6 +134,12 @@ typedef struct {
   uint32_t reserved;
 } hgd_tune_entry;
 int hgd_graph_set_tuning(hgd_graph* g, const hgd_tune_entry* entries, uint32_t n);
+/* How a batch launches its ef buckets: HGD_LAUNCH_BUCKETS (one persistent
+ * launch per bucket, concurrent on prioritised streams) or HGD_LAUNCH_SINGLE
+ * (one persistent launch with the largest bucket's shape that drains every
+ * query from a device queue, largest ef first).  Default BUCKETS. */
+enum { HGD_LAUNCH_BUCKETS = 0, HGD_LAUNCH_SINGLE = 1 };
+int hgd_graph_set_launch_mode(hgd_graph* g, int mode);
 /* Bytes of per-warp shared memory of a shape (validation for tuners). */
 uint32_t hgd_shape_smem_bytes(uint32_t hash_slots, uint32_t ef_hi, uint32_t cand_cap);
 /* Device name and SM count of the graph's GPU. */

@@ -87,3 +87,25 @@ def test_autotune_keeps_answers(hg, graphs, tmp_path):
     with pytest.raises(ValueError):
         ix2.set_tuning(json.dumps({"entries": [{"precision": 0, "ef_hi": 16, "hash_slots": 300, "cand_cap": 128,
                                                "warps_per_block": 1}]}))
+
+
+def test_single_launch_and_mixed_tuning_keep_answers(hg, graphs):
+    """One largest-ef-first launch over all buckets, and the mixed-batch
+    tuner (which may choose it), answer exactly like the per-bucket launches."""
+    base, q, *_ = graphs.data("c1")
+    ix = hg.Index.load(graphs.path("c1"))
+    efs = np.random.default_rng(6).choice(np.array([10, 20, 40, 80, 160], dtype=np.uint32), q.shape[0])
+    ks = np.random.default_rng(7).choice(np.array([1, 5, 10], dtype=np.uint32), q.shape[0])
+    before = ix.search_batch_ex(q, 10, ef_per_query=efs, k_per_query=ks)
+    single = {"launch_mode": 1, "entries": [{"precision": 0, "ef_hi": 192, "hash_slots": 512, "cand_cap": 224,
+                                             "warps_per_block": 2}]}
+    ix.set_tuning(json.dumps(single))
+    got = ix.search_batch_ex(q, 10, ef_per_query=efs, k_per_query=ks)
+    np.testing.assert_array_equal(got["label"], before["label"])
+    assert got["distance"].tobytes() == before["distance"].tobytes()
+    sample = np.random.default_rng(9).permutation(q)[:512]
+    table = ix.autotune(sample, k=10, ef_max=160, ef_per_query=efs[:512])
+    assert table["launch_mode"] in (0, 1)
+    got = ix.search_batch_ex(q, 10, ef_per_query=efs, k_per_query=ks)
+    np.testing.assert_array_equal(got["label"], before["label"])
+    assert got["distance"].tobytes() == before["distance"].tobytes()
