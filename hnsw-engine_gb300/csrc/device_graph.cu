@@ -255,10 +255,11 @@ class WorkspaceLease {
 // tombstone switch and the tuning table in force.
 std::string graph_key_of(const hgd_search_args* a, bool any_deleted, uint64_t tune_version) {
   char buf[512];
-  std::snprintf(buf, sizeof buf, "%p/%llu/%u/%u/%u/%u/%p/%p/%p/%p/%u/%u/%u/%u/%d/%llu", static_cast<const void*>(a->queries),
-                static_cast<unsigned long long>(a->nq), a->k, a->ef, a->ef_default, a->precision,
-                static_cast<const void*>(a->ef_per_query), static_cast<const void*>(a->k_per_query), a->out,
-                static_cast<const void*>(a->nres), a->hash_slots, a->cand_cap, a->warps_per_block, a->pool_cap,
+  std::snprintf(buf, sizeof buf, "%p/%llu/%u/%u/%u/%u/%p/%p/%p/%p/%p/%u/%u/%u/%u/%d/%llu",
+                static_cast<const void*>(a->queries), static_cast<unsigned long long>(a->nq), a->k, a->ef,
+                a->ef_default, a->precision, static_cast<const void*>(a->ef_per_query),
+                static_cast<const void*>(a->k_per_query), a->out, static_cast<const void*>(a->nres),
+                static_cast<const void*>(a->done_flags), a->hash_slots, a->cand_cap, a->warps_per_block, a->pool_cap,
                 any_deleted ? 1 : 0, static_cast<unsigned long long>(tune_version));
   return buf;
 }
@@ -637,6 +638,7 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   P.num_filters = a->num_filters;
   P.out = d_out;
   P.nres = d_nres;
+  P.done = a->done_flags;
   P.counters = d_cnt;
   // ---- compressed traversal: FP16 / FP8 copies (built once) and the rerank pools ----
   const int prec = static_cast<int>(a->precision);

@@ -8,7 +8,10 @@
 // batches' events, copies each request's rows to its output and records the
 // request's latency from arrival to completion.  The traversal itself is the
 // same per-query algorithm as search_batch, so a request's answer does not
-// depend on what it was batched with.
+// depend on what it was batched with.  The kernels write each query's result
+// row straight into mapped pinned host memory and then raise that query's
+// done flag (system-scope fence first), so a request is returned as soon as
+// its own queries are finished, not when the slowest query of its batch is.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -49,13 +52,21 @@ struct ServerRequest {
 template <typename T>
 struct Pinned {
   T* p = nullptr;
+  T* dev = nullptr;  // device view of mapped memory
   size_t n = 0;
-  bool ensure(size_t need) {
+  bool ensure(size_t need, bool mapped = false) {
     if (need <= n) return true;
     if (p) cudaFreeHost(p);
-    p = nullptr;
+    p = dev = nullptr;
     n = 0;
-    if (cudaMallocHost(&p, need * sizeof(T)) != cudaSuccess) return false;
+    if (cudaHostAlloc(reinterpret_cast<void**>(&p), need * sizeof(T),
+                      mapped ? cudaHostAllocMapped : cudaHostAllocDefault) != cudaSuccess)
+      return false;
+    if (mapped && cudaHostGetDevicePointer(reinterpret_cast<void**>(&dev), p, 0) != cudaSuccess) {
+      cudaFreeHost(p);
+      p = nullptr;
+      return false;
+    }
     n = need;
     return true;
   }
@@ -68,7 +79,10 @@ struct BatchSlot {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev = nullptr;
   Pinned<float> q;
-  Pinned<hg_neighbor> out;
+  Pinned<hg_neighbor> out;  // mapped: the kernels write rows here
+  Pinned<uint32_t> done;    // mapped: per-query done flags
+  std::vector<char> req_done;
+  size_t ndone = 0;
   std::vector<uint32_t> efq, kq;
   std::vector<int32_t> fsel;
   std::vector<hgd_bitset> ftab;
@@ -278,7 +292,10 @@ class Server {
     s.kq.assign(nq, 0);
     s.fsel.assign(nq, -1);
     s.ftab.clear();
-    bool ok = s.q.ensure(nq * dim_) && s.out.ensure(nq * kstride);
+    bool ok = s.q.ensure(nq * dim_) && s.out.ensure(nq * kstride, true) && s.done.ensure(nq, true);
+    if (ok) std::memset(s.done.p, 0, nq * sizeof(uint32_t));
+    s.req_done.assign(take.size(), 0);
+    s.ndone = 0;
     uint64_t row = 0;
     for (size_t i = 0; ok && i < take.size(); ++i) {
       ServerRequest* r = take[i];
@@ -311,7 +328,9 @@ class Server {
       a.filters = s.ftab.empty() ? nullptr : s.ftab.data();
       a.num_filters = static_cast<uint32_t>(s.ftab.size());
       a.filter_of_query = s.ftab.empty() ? nullptr : s.fsel.data();
-      a.out = s.out.p;
+      a.out = s.out.dev;
+      a.out_on_device = 1;
+      a.done_flags = s.done.dev;
       a.stream = s.stream;
       a.synchronize = 0;
       rc = hgd_search(g_, &a);
@@ -340,51 +359,72 @@ class Server {
     launched_.push_back(&s);
   }
 
+  // Returns every request of a launched batch whose done flags are all up,
+  // and frees the slot once all its requests are out and its work is over.
   void complete_loop() {
     cudaSetDevice(im_.device);
+    std::vector<BatchSlot*> snapshot;
+    std::vector<ServerRequest*> finished;
     for (;;) {
-      BatchSlot* fin = nullptr;
       {
         std::lock_guard<std::mutex> lk(mu_);
-        for (size_t i = 0; i < launched_.size(); ++i)
-          if (cudaEventQuery(launched_[i]->ev) == cudaSuccess) {
-            fin = launched_[i];
-            launched_.erase(launched_.begin() + static_cast<long>(i));
-            break;
-          }
-        if (!fin && stop_ && launched_.empty() && pending_.empty()) {
+        if (stop_ && launched_.empty() && pending_.empty()) {
           bool any = false;
           for (auto& s : slots_) any = any || s.inflight;
           if (!any) return;
         }
+        snapshot = launched_;
       }
-      if (!fin) {
-        std::this_thread::sleep_for(std::chrono::microseconds(20));
-        continue;
+      bool progress = false;
+      for (BatchSlot* s : snapshot) {
+        finished.clear();
+        const bool gpu_done = s->ndone == s->reqs.size() || cudaEventQuery(s->ev) != cudaErrorNotReady;
+        for (size_t i = 0; i < s->reqs.size(); ++i) {
+          if (s->req_done[i]) continue;
+          ServerRequest* r = s->reqs[i];
+          const uint32_t* f = s->done.p + s->offset[i];
+          bool all = true;
+          for (uint32_t j = 0; j < r->nq && all; ++j) all = __atomic_load_n(f + j, __ATOMIC_ACQUIRE) != 0u;
+          if (!all) {
+            if (!gpu_done) continue;
+            // the batch is over but this request's rows never arrived
+            r->status = HG_ERUNTIME;
+            r->error = "server: batch ended without finishing a request";
+          } else {
+            for (uint32_t j = 0; j < r->nq; ++j)
+              std::memcpy(r->out + static_cast<size_t>(j) * r->k,
+                          s->out.p + static_cast<size_t>(s->offset[i] + j) * s->kstride, sizeof(hg_neighbor) * r->k);
+          }
+          s->req_done[i] = 1;
+          ++s->ndone;
+          finished.push_back(r);
+        }
+        const bool slot_free = s->ndone == s->reqs.size() && cudaEventQuery(s->ev) != cudaErrorNotReady;
+        if (finished.empty() && !slot_free) continue;
+        progress = true;
+        const auto now = Clock::now();
+        std::lock_guard<std::mutex> lk(mu_);
+        for (ServerRequest* r : finished) {
+          r->latency_ms = std::chrono::duration<double, std::milli>(now - r->arrival).count();
+          r->done = true;
+          if (r->status == HG_OK) {
+            lat_.push_back(r->latency_ms);
+            queries_done_ += r->nq;
+            if (!have_first_ || r->arrival < first_arrival_) first_arrival_ = r->arrival;
+            have_first_ = true;
+            last_done_ = now;
+          }
+        }
+        if (slot_free) {
+          launched_.erase(std::find(launched_.begin(), launched_.end(), s));
+          inflight_bytes_ -= s->bytes;
+          s->inflight = false;
+          s->reqs.clear();
+          cv_.notify_all();
+        }
+        cv_done_.notify_all();
       }
-      const auto now = Clock::now();
-      for (size_t i = 0; i < fin->reqs.size(); ++i) {
-        ServerRequest* r = fin->reqs[i];
-        for (uint32_t j = 0; j < r->nq; ++j)
-          std::memcpy(r->out + static_cast<size_t>(j) * r->k,
-                      fin->out.p + static_cast<size_t>(fin->offset[i] + j) * fin->kstride,
-                      sizeof(hg_neighbor) * r->k);
-      }
-      std::lock_guard<std::mutex> lk(mu_);
-      for (auto* r : fin->reqs) {
-        r->latency_ms = std::chrono::duration<double, std::milli>(now - r->arrival).count();
-        r->done = true;
-        lat_.push_back(r->latency_ms);
-        queries_done_ += r->nq;
-        if (!have_first_ || r->arrival < first_arrival_) first_arrival_ = r->arrival;
-        have_first_ = true;
-      }
-      last_done_ = now;
-      inflight_bytes_ -= fin->bytes;
-      fin->inflight = false;
-      fin->reqs.clear();
-      cv_done_.notify_all();
-      cv_.notify_all();
+      if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(10));
     }
   }
 

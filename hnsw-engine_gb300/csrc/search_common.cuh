@@ -44,6 +44,7 @@ struct SearchParams {
   uint32_t num_filters;
   void* out;                     // 16-byte records
   uint32_t* nres;                // per query result count or null
+  uint32_t* done;                // per query: set to 1 once its output row is final (system scope) or null
   // ---- per-warp shared layout ----
   uint32_t H;  // visited hash slots (power of two)
   uint32_t R;  // result capacity (>= every ef)

@@ -784,6 +784,15 @@ __device__ __forceinline__ void cand_insert(Warp& w, Cands& c, const SearchParam
   c.peak = total > c.peak ? static_cast<uint32_t>(total) : c.peak;
 }
 
+// Publish query q's output row: every lane's writes are fenced at system
+// scope before lane 0 raises the flag, so a host thread that sees the flag
+// (acquire) sees the row (the server's per-request completion).
+__device__ __forceinline__ void signal_done(uint32_t* done, uint32_t q, int lane) {
+  __threadfence_system();
+  __syncwarp();
+  if (lane == 0) *reinterpret_cast<volatile uint32_t*>(done + q) = 1u;
+}
+
 struct QueryOut {
   uint64_t label;
   float dist;
@@ -1119,6 +1128,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       }
     }
     if (!DP::kApprox && P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
+    if (!DP::kApprox && P.done) signal_done(P.done, q, lane);
     if (P.counters && lane == 0) {
       unsigned long long* cp = P.counters + static_cast<size_t>(q) * kCounters;
       cp[0] = n_uplists;
@@ -1229,6 +1239,7 @@ __global__ void __launch_bounds__(128) rerank_kernel(SearchParams P, const float
       row[j] = o;
     }
     if (P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
+    if (P.done) signal_done(P.done, q, lane);
     __syncwarp();
   }
 }

@@ -97,6 +97,8 @@ typedef struct {
   const int32_t* filter_of_query; /* host, nq entries, -1 = unfiltered; NULL: filter 0 for all if any */
   void* out;                     /* nq*k records */
   uint32_t* nres;                /* nullable: per-query result count (no padding) */
+  uint32_t* done_flags;          /* nullable, device-accessible (e.g. mapped pinned memory): entry q
+                                    is set to 1 once query q's row of `out` is final */
   void* stream;                  /* cudaStream_t; NULL = the graph's stream */
   uint64_t* counters;            /* nullable host array, nq x HGD_NCOUNTERS */
   int32_t synchronize;           /* 1: return after the results are in `out`; 0: only enqueue on
