@@ -38,7 +38,7 @@ sys.path.insert(0, str(REPO / "oracle"))
 N_BASE, DIM, CLUSTERS, NQ, K = 200_000, 128, 256, 10_000, 10
 EF_CHOICES = (10, 20, 40, 80, 160, 320)
 M, EFC = 16, 200
-METRIC = "QPS at recall@10>=0.95 (batched mixed-ef search, 200k x 128 L2)"
+METRIC = "QPS at recall@10≥0.95 (served/batched vs plain GPU, same GB300); p50/p99 ms"
 WORKLOAD = "batched-L2-200k: n=200000 d=128 M=16 efC=200, 10000 queries/step, per-query ef U{10..320}, k=10"
 
 

@@ -32,7 +32,6 @@ cudaError_t launch_search(const SearchParams& P, const float* inv, int blocks, i
 int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, uint32_t R, uint32_t C);
 cudaError_t launch_search_approx(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st);
 int occupancy_approx(uint32_t pdc, int metric, int prec, int wpb, size_t smem);
-cudaError_t launch_rerank(const SearchParams& P, const float* inv, int blocks, cudaStream_t st);
 cudaError_t launch_encode(const float* vecs, uint32_t n, uint32_t pd, uint32_t pdc, int prec, void* out,
                           float* scale, cudaStream_t st);
 cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, uint32_t ef_all, uint32_t ef_default,
@@ -872,14 +871,6 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     if (wb > 227u * 1024u) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
     cudaError_t e = launch(B, static_cast<int>(rerun_slots), 1, st);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("rerun kernel launch: ") + cudaGetErrorString(e));
-  }
-  // ---- exact FP32 rerank of the traversal pools ----
-  if (prec != HGD_PREC_FP32) {
-    hg::SearchParams B = P;
-    B.R = next_pow2(P.pool_stride);  // per-warp sort buffer
-    const int blocks = static_cast<int>(std::min<uint64_t>((nq + 3) / 4, static_cast<uint64_t>(g->sms) * 8));
-    cudaError_t e = hg::launch_rerank(B, d_inv, blocks, st);
-    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("rerank kernel launch: ") + cudaGetErrorString(e));
   }
   // ---- results back ----
   if (!a->out_on_device) {

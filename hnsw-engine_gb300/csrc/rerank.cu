@@ -1,22 +1,12 @@
-// rerank.cu -- exact FP32 rerank of compressed-precision traversal pools
-// (distances in the reference's order), and the row encoders that build the
-// FP16 / FP8-E4M3 copies of the vectors.
+// rerank.cu -- the row encoders that build the FP16 / FP8-E4M3 copies of the
+// vectors walked by the compressed-precision traversal (whose exact FP32
+// rerank is fused into the traversal kernel).
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
 
 #include "search_kernel.cuh"
 
 namespace hg {
-
-cudaError_t launch_rerank(const SearchParams& P, const float* inv, int blocks, cudaStream_t st) {
-  const uint32_t pd = P.pd;
-  if (P.metric == 0) {
-    HG_SEARCH_DISPATCH(sk::rerank_t, true, P, inv, blocks, st)
-  } else {
-    HG_SEARCH_DISPATCH(sk::rerank_t, false, P, inv, blocks, st)
-  }
-  return cudaErrorInvalidValue;
-}
 
 namespace {
 

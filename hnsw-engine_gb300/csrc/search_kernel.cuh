@@ -307,6 +307,12 @@ template <int NB, int NT, int S, int G>
 struct ExactDist {
   static constexpr bool kApprox = false;
   static constexpr int kMinBlocks = S >= 16 ? 4 : 5;
+  static constexpr int kSlots = S;
+  template <bool L2>
+  __device__ __forceinline__ static float rows(const Layout<NB, NT, S>& L, const float* __restrict__ vecs, uint32_t pd,
+                                               uint32_t id, uint32_t mask, const float (&qr)[S], int lane) {
+    return lane_dists<NB, NT, S, G, L2>(L, vecs, pd, id, mask, qr, lane);
+  }
   Layout<NB, NT, S> L;
   float qr[S];
   __device__ __forceinline__ void init(const SearchParams& P) {
@@ -391,6 +397,11 @@ struct ApproxDist {
   static constexpr bool kApprox = true;
   static constexpr int kMinBlocks = 5;
   static constexpr int LPR = 32 / RPP;
+  // the exact FP32 layout (reference order, runtime block counts) of the same
+  // padded-width class: the fused rerank computes the pool's exact distances
+  static constexpr int kPdc = LPR * E;
+  using Exact = ExactDist<-1, 0, kPdc == 128 ? 5 : (kPdc == 256 ? 9 : (kPdc == 512 ? 17 : 33)),
+                          kPdc == 128 ? 4 : (kPdc <= 512 ? 2 : 1)>;
   float qa[E];
   __device__ __forceinline__ void init(const SearchParams&) {}
   __device__ __forceinline__ void load_query(const SearchParams& P, const float* raw, const float* inv_norm,
@@ -793,6 +804,38 @@ __device__ __forceinline__ void signal_done(uint32_t* done, uint32_t q, int lane
   if (lane == 0) *reinterpret_cast<volatile uint32_t*>(done + q) = 1u;
 }
 
+// Exact FP32 distances (reference order, layout EX) of the s pool ids in
+// prow, merged 32 at a time into res (sorted, capacity R).  Kept out of line
+// with plain arguments: its registers do not add to the traversal loop's.
+template <class EX, bool L2>
+static __device__ __noinline__ void fused_rerank(const float* __restrict__ vecs, uint32_t pd, uint32_t dim,
+                                                 const float* __restrict__ raw, float inv, bool cosine,
+                                                 const uint32_t* prow, int s, uint64_t* res, uint64_t* stE, int R,
+                                                 int lane) {
+  EX ex;
+  ex.L.nb_rt = static_cast<int>(pd / 64);
+  ex.L.nt_rt = static_cast<int>((pd % 64) / 16);
+#pragma unroll
+  for (int i = 0; i < EX::kSlots; ++i) {
+    const int e = ex.L.elem(i, lane);
+    const float v = (e >= 0 && e < static_cast<int>(dim)) ? __ldg(raw + e) : 0.0f;
+    ex.qr[i] = cosine ? __fmul_rn(v, inv) : v;
+  }
+  int n = 0;
+  for (int c0 = 0; c0 < s; c0 += 32) {
+    const bool live = c0 + lane < s;
+    const uint32_t id = live ? prow[c0 + lane] : kNoId;
+    const uint32_t mask = __ballot_sync(kFull, live);
+    const float d = EX::template rows<L2>(ex.L, vecs, pd, id, mask, ex.qr, lane);
+    const uint64_t v = warp_sort32(live ? mkkey(d, id) : kMaxKey, lane);
+    const int mm = __popc(mask);
+    if (lane < mm) stE[lane] = v;
+    __syncwarp();
+    n = warp_merge(res, n, R, stE, mm, lane);
+    __syncwarp();
+  }
+}
+
 struct QueryOut {
   uint64_t label;
   float dist;
@@ -1103,15 +1146,21 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       continue;
     }
 
-    if (DP::kApprox) {
-      // traversal pool for the exact rerank (sorted by traversal distance)
+    if constexpr (DP::kApprox) {
+      // Exact FP32 rerank of the traversal pool, fused: the pool ids go to the
+      // query's global row, their distances are recomputed in the reference's
+      // order and merged 32 at a time into the (now free) result array.
       uint32_t* prow = P.pool_out + static_cast<size_t>(q) * P.pool_stride;
       for (int j = lane; j < s; j += 32) prow[j] = static_cast<uint32_t>(w.res[j]);
       if (lane == 0) P.pool_n[q] = static_cast<uint32_t>(s);
+      __syncwarp();
+      fused_rerank<typename DP::Exact, L2>(P.vecs, P.pd, P.dim, P.queries + static_cast<size_t>(q) * P.dim,
+                                          inv_norm ? inv_norm[q] : 1.0f, inv_norm != nullptr, prow, s, w.res, w.stE,
+                                          static_cast<int>(P.R), lane);
     }
     // ---- output (search_layer.cpp:166-169, 189-192) ----
-    const int m = DP::kApprox ? 0 : (s < static_cast<int>(k) ? s : static_cast<int>(k));
-    if (!DP::kApprox) {
+    const int m = s < static_cast<int>(k) ? s : static_cast<int>(k);
+    {
       QueryOut* row = static_cast<QueryOut*>(P.out) + static_cast<size_t>(q) * P.k_stride;
       for (uint32_t j = lane; j < P.k_stride; j += 32) {
         QueryOut o;
@@ -1127,8 +1176,8 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
         row[j] = o;
       }
     }
-    if (!DP::kApprox && P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
-    if (!DP::kApprox && P.done) signal_done(P.done, q, lane);
+    if (P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
+    if (P.done) signal_done(P.done, q, lane);
     if (P.counters && lane == 0) {
       unsigned long long* cp = P.counters + static_cast<size_t>(q) * kCounters;
       cp[0] = n_uplists;
@@ -1191,69 +1240,7 @@ int occupancy_t(int wpb, size_t smem) {
     if (S_ <= 33) return FN<sk::ExactDist<-1, 0, 33, 1>, L2>(__VA_ARGS__);                          \
   }
 
-// ---------------------------------------------------------------------------
-// Exact FP32 rerank of the traversal pools of a compressed-precision batch:
-// one warp per query recomputes the distances of its pool in the reference
-// order, sorts (distance, id) and writes the first k results.
-// Shared memory per warp: R keys.
-// ---------------------------------------------------------------------------
-template <class DP, bool L2>
-__global__ void __launch_bounds__(128) rerank_kernel(SearchParams P, const float* __restrict__ inv_norm) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  uint64_t* keys = reinterpret_cast<uint64_t*>(smem) + static_cast<size_t>(wib) * P.R;
-  DP dp;
-  dp.init(P);
-  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + wib; q < P.nq; q += nw) {
-    const int s = static_cast<int>(P.pool_n[q]);
-    const uint32_t* prow = P.pool_out + static_cast<size_t>(q) * P.pool_stride;
-    dp.load_query(P, P.queries + static_cast<size_t>(q) * P.dim, inv_norm, q, lane);
-    for (int c0 = 0; c0 < s; c0 += 32) {
-      const bool live = c0 + lane < s;
-      const uint32_t id = live ? prow[c0 + lane] : kNoId;
-      const uint32_t mask = __ballot_sync(kFull, live);
-      const float d = dp.template dists<L2>(P, id, mask, lane);
-      if (live) keys[c0 + lane] = mkkey(d, id);
-    }
-    int p2 = 1;
-    while (p2 < s) p2 <<= 1;
-    for (int i = s + lane; i < p2; i += 32) keys[i] = kMaxKey;
-    __syncwarp();
-    warp_bitonic(keys, p2, lane);
-    uint32_t k = P.kq ? P.kq[q] : P.k_all;
-    const int m = s < static_cast<int>(k) ? s : static_cast<int>(k);
-    QueryOut* row = static_cast<QueryOut*>(P.out) + static_cast<size_t>(q) * P.k_stride;
-    for (uint32_t j = lane; j < P.k_stride; j += 32) {
-      QueryOut o;
-      if (static_cast<int>(j) < m) {
-        const uint64_t kk = keys[j];
-        o.label = P.labels[static_cast<uint32_t>(kk)];
-        o.dist = key_dist(kk);
-      } else {
-        o.label = ~0ull;
-        o.dist = __int_as_float(0x7f800000);
-      }
-      o.zero = 0;
-      row[j] = o;
-    }
-    if (P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
-    if (P.done) signal_done(P.done, q, lane);
-    __syncwarp();
-  }
-}
-
-template <class DP, bool L2>
-cudaError_t rerank_t(const SearchParams& P, const float* inv, int blocks, cudaStream_t st) {
-  const size_t smem = 4u * P.R * 8u;
-  auto* fn = rerank_kernel<DP, L2>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  if (e != cudaSuccess) return e;
-  fn<<<blocks, 128, smem, st>>>(P, inv);
-  return cudaGetLastError();
-}
-
+// compressed-precision traversal layouts per padded width (rows of pdc elements)
 #define HG_SEARCH_APPROX_DISPATCH(FN, PREC, L2, ...)                      \
   switch (pdc) {                                                           \
     case 128: return FN<sk::ApproxDist<4, 16, PREC>, L2>(__VA_ARGS__);    \
