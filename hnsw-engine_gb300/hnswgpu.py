@@ -138,6 +138,19 @@ def distance_order() -> str:
     return {v: k for k, v in ORDERS.items()}[lib().hg_get_distance_order()]
 
 
+def simd_isa() -> str:
+    """The host kernel order in use (the reference's simd_isa())."""
+    return distance_order()
+
+
+def _float_matrix(x, name: str) -> np.ndarray:
+    """float32, C-contiguous; non-numeric input is a TypeError (as in the reference's binding)."""
+    arr = np.asarray(x)
+    if arr.dtype.kind not in "biuf":
+        raise TypeError(f"{name}: expected a numeric array, got dtype {arr.dtype}")
+    return np.ascontiguousarray(arr, dtype=np.float32)
+
+
 def _to_labels(ids, n: int, start: int) -> np.ndarray:
     if ids is None:
         return np.arange(start, start + n, dtype=np.uint64)
@@ -161,6 +174,7 @@ class _FilterHolder:
     def __init__(self, spec):
         self.struct = None
         self.keep = []
+        self.error = None  # an exception raised by a callable filter
         if spec is None:
             return
         f = _Filter()
@@ -187,7 +201,16 @@ class _FilterHolder:
             self.keep.append(words)
             f.kind, f.words, f.num_labels = 1, words.ctypes.data, int(spec.num_labels)
         elif callable(spec):
-            fn = PRED(lambda label, ctx: 1 if spec(int(label)) else 0)
+            def call(label, ctx):
+                if self.error is not None:
+                    return 0
+                try:
+                    return 1 if spec(int(label)) else 0
+                except BaseException as e:  # re-raised by raise_pending() after the call
+                    self.error = e
+                    return 0
+
+            fn = PRED(call)
             self.keep.append(fn)
             f.kind, f.fn = 2, fn
         else:
@@ -196,6 +219,10 @@ class _FilterHolder:
 
     def ref(self):
         return None if self.struct is None else C.byref(self.struct)
+
+    def raise_pending(self):
+        if self.error is not None:
+            raise self.error
 
 
 def _pack_mask(mask: np.ndarray) -> np.ndarray:
@@ -244,7 +271,7 @@ class Index:
         _check(lib().hg_index_save(self._h, str(path).encode()))
 
     def add(self, vectors, ids=None, num_threads: int = 0):
-        v = np.ascontiguousarray(vectors, dtype=np.float32)
+        v = _float_matrix(vectors, "vectors")
         if v.ndim == 1:
             v = v.reshape(1, -1)
         if v.shape[1] != self.dim:
@@ -253,7 +280,7 @@ class Index:
         _check(lib().hg_index_add_batch(self._h, _ptr(v), _ptr(labels), v.shape[0], num_threads))
 
     def _queries(self, queries):
-        q = np.ascontiguousarray(queries, dtype=np.float32)
+        q = _float_matrix(queries, "queries")
         single = q.ndim == 1
         if single:
             q = q.reshape(1, -1)
@@ -268,7 +295,9 @@ class Index:
         q, _ = self._queries(queries)
         out = np.empty(q.shape[0] * k, dtype=NEIGHBOR)
         fh = _FilterHolder(filter)
-        _check(lib().hg_index_search_batch(self._h, _ptr(q), q.shape[0], k, ef or 0, _ptr(out), 0, fh.ref()))
+        rc = lib().hg_index_search_batch(self._h, _ptr(q), q.shape[0], k, ef or 0, _ptr(out), 0, fh.ref())
+        fh.raise_pending()
+        _check(rc)
         return out.reshape(q.shape[0], k)
 
     def search(self, queries, k: int = 10, ef=None, num_threads: int = 0, filter=None):
@@ -287,7 +316,9 @@ class Index:
         out = np.empty(k, dtype=NEIGHBOR)
         n = C.c_size_t()
         fh = _FilterHolder(filter)
-        _check(lib().hg_index_search(self._h, _ptr(q), k, ef, fh.ref(), _ptr(out), C.byref(n)))
+        rc = lib().hg_index_search(self._h, _ptr(q), k, ef, fh.ref(), _ptr(out), C.byref(n))
+        fh.raise_pending()
+        _check(rc)
         return out[:n.value]
 
     def search_batch_ex(self, queries, k: int, ef: int = 0, ef_per_query=None, k_per_query=None, filters=None,
@@ -329,7 +360,10 @@ class Index:
         if counters:
             cnt = np.zeros((nq, NCOUNTERS), dtype=np.uint64)
             opt.counters = cnt.ctypes.data
-        _check(lib().hg_index_search_batch_ex(self._h, _ptr(q), nq, k, ef, _ptr(out), C.byref(opt)))
+        rc = lib().hg_index_search_batch_ex(self._h, _ptr(q), nq, k, ef, _ptr(out), C.byref(opt))
+        for h in holders:
+            h.raise_pending()
+        _check(rc)
         out = out.reshape(nq, k)
         return (out, cnt) if counters else out
 
