@@ -261,6 +261,74 @@ __device__ __forceinline__ float combine(const Layout<NB, NT, S>& L, const float
   return L2 ? s : __fsub_rn(1.0f, s);
 }
 
+// The per-lane chains of one row: a = acc0 (lanes < 16) / acc1 (lanes >= 16),
+// b = acc2 / acc3 (the first half of combine()).
+template <int NB, int NT, int S, bool L2>
+__device__ __forceinline__ void chains(const Layout<NB, NT, S>& L, const float (&x)[S], const float (&qr)[S],
+                                       float& a, float& b) {
+  a = 0.0f;
+  b = 0.0f;
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    if (i < L.nb()) {
+      if (L2) {
+        const float d = __fsub_rn(qr[i], x[i]);
+        a = __fmaf_rn(d, d, a);
+      } else {
+        a = __fmaf_rn(qr[i], x[i], a);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    if (i >= L.nb() && i < 2 * L.nb()) {
+      if (L2) {
+        const float d = __fsub_rn(qr[i], x[i]);
+        b = __fmaf_rn(d, d, b);
+      } else {
+        b = __fmaf_rn(qr[i], x[i], b);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    if (i >= 2 * L.nb() && i < 2 * L.nb() + L.nt()) {  // lanes >= 16 hold zeros here
+      if (L2) {
+        const float d = __fsub_rn(qr[i], x[i]);
+        a = __fmaf_rn(d, d, a);
+      } else {
+        a = __fmaf_rn(qr[i], x[i], a);
+      }
+    }
+  }
+}
+
+// (acc0 + acc1) + (acc2 + acc3) of two rows with one exchange per sum: lanes
+// < 16 finish row 0, lanes >= 16 row 1 (each lane's 16-lane position l =
+// lane & 15).  Float addition is commutative, so each sum is bit-identical to
+// combine()'s.
+__device__ __forceinline__ float pair_sums(float a0, float b0, float a1, float b1, int lane) {
+  const bool hi = lane >= 16;
+  const float ra = __shfl_xor_sync(kFull, hi ? a0 : a1, 16);
+  const float rb = __shfl_xor_sync(kFull, hi ? b0 : b1, 16);
+  const float xa = hi ? __fadd_rn(ra, a1) : __fadd_rn(a0, ra);
+  const float xb = hi ? __fadd_rn(rb, b1) : __fadd_rn(b0, rb);
+  return __fadd_rn(xa, xb);
+}
+
+// The 16-lane butterfly (8, 4, 2, 1) of four rows at once: p holds rows 0 / 1
+// in lanes < 16 / >= 16, r rows 2 / 3; after the 8-step each 8-lane group
+// holds one row (lanes 0-7 row 0, 8-15 row 2, 16-23 row 1, 24-31 row 3).
+__device__ __forceinline__ float quad_reduce(float p, float r, int lane) {
+  const bool up = (lane & 8) != 0;
+  const float rv = __shfl_xor_sync(kFull, up ? p : r, 8);
+  float v = up ? __fadd_rn(r, rv) : __fadd_rn(p, rv);
+  v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 4));
+  v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 2));
+  v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 1));
+  return v;
+}
+
 // Distances for the lanes in `mask`, G rows in flight; lane j receives the
 // distance of its own id.  All loads of a group are issued before any math.
 template <int NB, int NT, int S, int G, bool L2>
@@ -286,11 +354,33 @@ __device__ __forceinline__ float lane_dists(const Layout<NB, NT, S>& L, const fl
         x[g][i] = (rows[g] != nullptr && e >= 0) ? __ldg(rows[g] + e) : 0.0f;
       }
     }
+    if constexpr (G % 4 == 0) {
+      // four rows per reduction: 2.25 shuffles per row instead of 6
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      if (gl[g] >= 0) {  // warp-uniform
-        const float d = combine<NB, NT, S, L2>(L, x[g], qr);
-        if (gl[g] == lane) mine = d;
+      for (int g0 = 0; g0 < G; g0 += 4) {
+        if (gl[g0] < 0) break;  // warp-uniform: rows fill in order
+        float a[4], b[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) chains<NB, NT, S, L2>(L, x[g0 + j], qr, a[j], b[j]);
+        const float p = pair_sums(a[0], b[0], a[1], b[1], lane);
+        const float r = pair_sums(a[2], b[2], a[3], b[3], lane);
+        float v = quad_reduce(p, r, lane);
+        if (!L2) v = __fsub_rn(1.0f, v);
+        // row j of the group sits in lanes 8 * {0, 2, 1, 3}[j] ..
+        int src = -1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (gl[g0 + j] == lane) src = 8 * ((j & 1) * 2 + (j >> 1));
+        const float got = __shfl_sync(kFull, v, src < 0 ? 0 : src);
+        if (src >= 0) mine = got;
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        if (gl[g] >= 0) {  // warp-uniform
+          const float d = combine<NB, NT, S, L2>(L, x[g], qr);
+          if (gl[g] == lane) mine = d;
+        }
       }
     }
   }

@@ -12,10 +12,12 @@ import pytest
 gpu = pytest.mark.gpu
 
 
-def _clustered(n, d, seed):
+def _clustered(n, d, seed, clusters=16):
+    # the reference's Python-test recipe: N(0, 4^2) centres, unit noise
     r = np.random.default_rng(seed)
-    c = r.normal(size=(8, d)).astype(np.float32) * 4
-    return (c[r.integers(0, 8, n)] + r.normal(size=(n, d))).astype(np.float32)
+    centers = r.normal(0, 4, size=(clusters, d))
+    c = r.integers(0, clusters, size=n)
+    return (centers[c] + r.normal(size=(n, d))).astype(np.float32)
 
 
 def _exact(base, q, k, metric="l2"):
