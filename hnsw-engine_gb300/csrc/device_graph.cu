@@ -642,10 +642,9 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   // ---- compressed traversal: FP16 / FP8 copies (built once) and the rerank pools ----
   const int prec = static_cast<int>(a->precision);
   if (prec != HGD_PREC_FP32) {
-    const uint32_t pdc = round_up(static_cast<uint32_t>(g->dim), 128);
-    if (pdc != 128 && pdc != 256 && pdc != 512 && pdc != 1024)
-      return fail(HGD_EINVAL, "hgd_search: FP16/FP8 traversal supports dim <= 256, 257..512 and 513..1024 "
-                              "rounded to 128/256/512/1024");
+    // rows of the compressed copies: the smallest of 128, 256, 512, 1024 that holds dim
+    const uint32_t pdc = g->dim <= 128 ? 128u : (g->dim <= 256 ? 256u : (g->dim <= 512 ? 512u : 1024u));
+    if (g->dim > 1024) return fail(HGD_EINVAL, "hgd_search: FP16/FP8 traversal supports dim <= 1024");
     DBuf& vb = prec == HGD_PREC_FP16 ? g->v16 : g->v8;
     bool& have = prec == HGD_PREC_FP16 ? g->has16 : g->has8;
     std::lock_guard<std::mutex> build_lock(g->mu);

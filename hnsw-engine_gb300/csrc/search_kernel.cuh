@@ -374,6 +374,22 @@ __device__ __forceinline__ float lane_dists(const Layout<NB, NT, S>& L, const fl
         const float got = __shfl_sync(kFull, v, src < 0 ? 0 : src);
         if (src >= 0) mine = got;
       }
+    } else if constexpr (G == 2) {
+      // two rows per reduction: 3.5 shuffles per row instead of 6
+      if (gl[0] >= 0) {
+        float a[2], b[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) chains<NB, NT, S, L2>(L, x[j], qr, a[j], b[j]);
+        float v = pair_sums(a[0], b[0], a[1], b[1], lane);  // lanes < 16 row 0, >= 16 row 1
+        v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 8));
+        v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 4));
+        v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 2));
+        v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 1));
+        if (!L2) v = __fsub_rn(1.0f, v);
+        const int src = gl[0] == lane ? 0 : (gl[1] == lane ? 16 : -1);
+        const float got = __shfl_sync(kFull, v, src < 0 ? 0 : src);
+        if (src >= 0) mine = got;
+      }
     } else {
 #pragma unroll
       for (int g = 0; g < G; ++g) {

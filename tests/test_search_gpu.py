@@ -249,3 +249,37 @@ def test_errors(hg, graphs):
         ix.search_batch_ex(q[:2], 5, k_per_query=[3, 9])  # per-query k above the row stride
     with pytest.raises(ValueError):
         ix.search_batch_ex(q[:2], 5, filters=[np.array([1, 2])], filter_of_query=[0, 3])
+
+
+@pytest.mark.parametrize("dim", [37, 200, 256, 500, 700])
+@pytest.mark.parametrize("metric", ["l2", "ip"])
+def test_every_distance_layout_vs_oracle(hg, oracle, tmp_path, dim, metric):
+    """Float Gaussian rows (summation order matters) at widths that use the
+    runtime layouts (37, 200, 700) and the two-rows-per-pass layouts (256,
+    500): ids and distances bit-identical to the oracle; the FP16 / FP8 paths'
+    fused rerank returns the exact kernel's distances for the ids it keeps."""
+    rng = np.random.default_rng(dim)
+    base = rng.normal(size=(1500, dim)).astype(np.float32)
+    q = rng.normal(size=(40, dim)).astype(np.float32)
+    ix = hg.Index(dim, metric, 8, 64)
+    ix.add(base, num_threads=0)
+    p = tmp_path / "g.idx"
+    ix.save(p)
+    ix = hg.Index.load(p)
+    ol, od = oracle.OracleIndex(p).search_batch(q, 10, 64)
+    _eq_oracle(ix.search_batch_ex(q, 10, 64), ol, od, f"dim={dim} {metric}")
+    pd = -(-dim // 16) * 16  # graph rows are zero-padded to a multiple of 16 and summed over pd
+    qp = np.zeros((q.shape[0], pd), np.float32)
+    qp[:, :dim] = q
+    bp = np.zeros((base.shape[0], pd), np.float32)
+    bp[:, :dim] = base
+    for prec in (1, 2):
+        rec = ix.search_batch_ex(q, 10, 64, precision=prec)
+        for qi in range(q.shape[0]):
+            for lab, dist in zip(rec["label"][qi], rec["distance"][qi]):
+                # each returned distance is the exact FP32 distance of that id
+                want = oracle.kernel("avx512", metric == "l2", qp[qi], bp[int(lab)])
+                if metric != "l2":
+                    want = np.float32(np.float32(1.0) - want)
+                assert np.float32(dist).tobytes() == np.float32(want).tobytes(), f"dim={dim} prec={prec}"
+
