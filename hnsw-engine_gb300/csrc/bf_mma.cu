@@ -71,8 +71,14 @@ struct MmaParams {
   uint64_t* buf;          // splits x nq x cap candidate keys
   uint32_t* cnt;          // splits x nq: candidates kept, or kOver
   uint32_t* err;          // [0] pipeline wait expired
+  // per-query filters (routed graph queries): bits over rows of filter
+  // fsel[q] (-1 none) instead of `allow`; tombstones over rows
+  const uint32_t* const* allow_tab;
+  const int32_t* fsel;
+  const uint32_t* alive;
   uint32_t n, nq, kchunks, cap, k, nbt, tiles_q, splits, tps;
   int l2;
+  int lenient;  // keep the buffer of a query whose candidates overflow (approximate answer) instead of failing
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -329,6 +335,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t b0 = sp * P.tps, b1 = min(P.nbt, b0 + P.tps);
       const uint32_t q = qt * BM + row_in_tile;
       const bool live_q = q < P.nq;
+      const int32_t fq = (P.fsel && live_q) ? P.fsel[q] : -1;
+      const uint32_t* allow_q = P.fsel ? (fq >= 0 ? P.allow_tab[fq] : nullptr) : P.allow;
       const float cq = P.qc[q];
       const float margin = P.qm[q];
       uint64_t* bufp = P.buf + (static_cast<size_t>(sp) * P.nq + (live_q ? q : 0)) * P.cap;
@@ -354,7 +362,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t j0 = bt * BN + ch * 32u;
           if (j0 >= P.n) continue;  // warp-uniform: padding rows of the last tile
           uint32_t valid = P.n - j0 >= 32u ? 0xFFFFFFFFu : ((1u << (P.n - j0)) - 1u);
-          if (P.allow) valid &= __ldg(P.allow + (j0 >> 5));
+          if (allow_q) valid &= __ldg(allow_q + (j0 >> 5));
+          if (P.alive) valid &= __ldg(P.alive + (j0 >> 5));
           if (!live_q || over) valid = 0u;
           float sv[32];
           const float4* x4 = reinterpret_cast<const float4*>(P.xn + j0);
@@ -405,7 +414,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc_fence_before();
         if (lane == 0) mbar_arrive(tempty(ab));
       }
-      if (ok && live_q) P.cnt[static_cast<size_t>(sp) * P.nq + q] = over ? kOver : cnt;
+      if (ok && live_q) P.cnt[static_cast<size_t>(sp) * P.nq + q] = (over && !P.lenient) ? kOver : cnt;
     }
   }
   __syncwarp();
@@ -551,7 +560,7 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
                               const float* __restrict__ qm, const float* __restrict__ qq, uint32_t nq,
                               uint32_t splits, uint32_t cap, uint32_t k,
                               uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t* __restrict__ pool_n,
-                              uint32_t* __restrict__ err) {
+                              uint32_t* __restrict__ err, int lenient) {
   const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (q >= nq) return;
@@ -589,9 +598,20 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
     }
     const float T = dist_of_key_bits(lo);
     thr = __fadd_ru(T, qm[q]);
+    if (lenient && count_le(okey(thr)) > pool_cap) {
+      // too many survivors for the pool: keep the pool_cap smallest (approximate)
+      uint32_t lo2 = 0u, hi2 = 0xFFFFFFFFu;
+      while (lo2 < hi2) {
+        const uint32_t mid = lo2 + ((hi2 - lo2) >> 1);
+        if (count_le(mid) >= pool_cap) hi2 = mid;
+        else lo2 = mid + 1u;
+      }
+      thr = dist_of_key_bits(lo2);
+      if (count_le(lo2) > pool_cap) thr = nextafterf(thr, -__int_as_float(0x7f800000));  // ties at the edge: drop them
+    }
     // exact mode holds while the k-th distance is below 2^24 (where the
     // reference's own sum is still exact); past it the scan answers
-    if (qq[q] >= 0.0f && static_cast<double>(T) + qq[q] >= 16777216.0) {
+    if (!lenient && qq[q] >= 0.0f && static_cast<double>(T) + qq[q] >= 16777216.0) {
       if (lane == 0) {
         pool_n[q] = 0;
         atomicAdd(err + 1, 1u);
@@ -615,8 +635,8 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
   }
   if (lane == 0) {
     if (w > pool_cap) {
-      pool_n[q] = 0;
-      atomicAdd(err + 1, 1u);
+      pool_n[q] = lenient ? pool_cap : 0;
+      if (!lenient) atomicAdd(err + 1, 1u);
     } else {
       pool_n[q] = w;
     }
@@ -626,12 +646,23 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
 // ---------------------------------------------------------------------------
 // exact distances of the survivors in the reference order, sorted, first k
 // ---------------------------------------------------------------------------
+// Where rerank_kernel writes query q's row: out row out_index[q] (or q) with
+// stride k_stride, the first min(m, k of that row) entries valid, then the
+// row's done flag (system-scope fence first) when `done` is given.
+struct OutMap {
+  const uint32_t* out_index;
+  const uint32_t* kq;
+  uint32_t k_stride;
+  uint32_t* done;
+};
+
 template <int S, bool L2>
 __global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ rows, const uint64_t* __restrict__ labels,
                                                      const float* __restrict__ queries, const float* __restrict__ inv,
                                                      uint32_t nq, uint32_t dim, uint32_t dp, uint32_t k,
                                                      const uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t p2max,
-                                                     const uint32_t* __restrict__ pool_n, Rec* __restrict__ out) {
+                                                     const uint32_t* __restrict__ pool_n, Rec* __restrict__ out,
+                                                     OutMap om) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint64_t* keys = reinterpret_cast<uint64_t*>(smem) + static_cast<size_t>(w) * p2max;
@@ -664,10 +695,14 @@ __global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ r
   for (int i = static_cast<int>(m) + lane; i < p2; i += 32) keys[i] = ~0ull;
   __syncwarp();
   warp_sort(keys, p2, lane);
-  Rec* row = out + static_cast<size_t>(q) * k;
-  for (uint32_t j = lane; j < k; j += 32) {
+  const uint32_t orow = om.out_index ? om.out_index[q] : q;
+  const uint32_t stride = om.k_stride ? om.k_stride : k;
+  const uint32_t kk_row = om.kq ? om.kq[orow] : k;
+  const uint32_t mv = m < kk_row ? m : kk_row;
+  Rec* row = out + static_cast<size_t>(orow) * stride;
+  for (uint32_t j = lane; j < stride; j += 32) {
     Rec o;
-    if (j < m) {
+    if (j < mv) {
       const uint64_t kk = keys[j];
       o.label = labels[static_cast<uint32_t>(kk)];
       o.dist = key_dist(kk);
@@ -678,6 +713,11 @@ __global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ r
     o.zero = 0;
     row[j] = o;
   }
+  if (om.done) {
+    __threadfence_system();
+    __syncwarp();
+    if (lane == 0) *reinterpret_cast<volatile uint32_t*>(om.done + orow) = 1u;
+  }
 }
 
 int slots_of(uint32_t dim) {
@@ -687,11 +727,12 @@ int slots_of(uint32_t dim) {
 template <bool L2>
 cudaError_t launch_rerank(int S, dim3 grid, size_t smem, cudaStream_t st, const float* rows, const uint64_t* labels,
                           const float* queries, const float* inv, uint32_t nq, uint32_t dim, uint32_t dp, uint32_t k,
-                          const uint32_t* pool, uint32_t pool_cap, uint32_t p2max, const uint32_t* pool_n, Rec* out) {
+                          const uint32_t* pool, uint32_t pool_cap, uint32_t p2max, const uint32_t* pool_n, Rec* out,
+                          OutMap om = OutMap{nullptr, nullptr, 0, nullptr}) {
   auto go = [&](auto fn) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    fn<<<grid, 128, smem, st>>>(rows, labels, queries, inv, nq, dim, dp, k, pool, pool_cap, p2max, pool_n, out);
+    fn<<<grid, 128, smem, st>>>(rows, labels, queries, inv, nq, dim, dp, k, pool, pool_cap, p2max, pool_n, out, om);
     return cudaGetLastError();
   };
   if (S <= 6) return go(rerank_kernel<6, L2>);
@@ -879,7 +920,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "select kernel";
     select_kernel<<<(nq * 32 + 255) / 256, 256, 0, st>>>(buf, cnt, qm, qq, nq, splits, cap, k, pool, pool_cap,
-                                                         pool_n, derr);
+                                                         pool_n, derr, 0);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
     const int S = slots_of(r.dim);
@@ -909,6 +950,152 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
                   static_cast<void*>(cnt), static_cast<void*>(pool), static_cast<void*>(pool_n),
                   static_cast<void*>(derr)})
     if (p) cudaFree(p);
+  return e;
+}
+
+namespace {
+
+// Routed queries, prepared (cosine: times 1/||q||) and zero-padded to the
+// rows' padded width: qp[i] = query qlist[i].
+__global__ void gather_queries_kernel(const float* __restrict__ raw, const float* __restrict__ inv,
+                                      const uint32_t* __restrict__ qlist, uint32_t n_r, uint32_t dim, uint32_t pd,
+                                      float* __restrict__ qp) {
+  const uint64_t i = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n_r) return;
+  const uint32_t q = qlist[i];
+  const float iv = inv ? inv[q] : 1.0f;
+  for (uint32_t e = lane; e < pd; e += 32) {
+    const float v = e < dim ? raw[static_cast<size_t>(q) * dim + e] : 0.0f;
+    qp[i * pd + e] = inv ? __fmul_rn(v, iv) : v;
+  }
+}
+
+struct Buf {
+  void* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    const cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+    if (e == cudaSuccess) n = std::max<size_t>(bytes, 256);
+    return e;
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+  ~Buf() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+struct Scratch {
+  Buf qp, q16, qc, qm, qq, buf, cnt, pool, pool_n, err;
+};
+
+Scratch* scratch_new() { return new Scratch(); }
+void scratch_free(Scratch* s) { delete s; }
+
+cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch* sc, cudaStream_t st,
+                          std::string* err) {
+  if (a.n_r == 0) return cudaSuccess;
+  const uint32_t n_r = a.n_r;
+  const uint32_t k = a.k_stride;
+  const uint32_t nq_pad = round_up(n_r, BM);
+  const uint32_t tiles_q = nq_pad / BM;
+  const uint32_t nbt = s->n_pad / BN;
+  uint32_t splits = 1;
+  if (tiles_q < static_cast<uint32_t>(s->sms))
+    splits = std::min<uint32_t>(nbt, (2u * static_cast<uint32_t>(s->sms) + tiles_q - 1) / tiles_q);
+  const uint32_t tps = (nbt + splits - 1) / splits;
+  splits = (nbt + tps - 1) / tps;
+  const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
+  const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(splits * cap, 32), 32));
+  uint32_t p2max = 1;
+  while (p2max < pool_cap) p2max <<= 1;
+  cudaError_t e = cudaSuccess;
+  const char* what = "alloc";
+  do {
+    if ((e = sc->qp.ensure(static_cast<size_t>(n_r) * r.dp * 4)) != cudaSuccess) break;
+    if ((e = sc->q16.ensure(static_cast<size_t>(nq_pad) * s->kp * 2)) != cudaSuccess) break;
+    if ((e = sc->qc.ensure(nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = sc->qm.ensure(nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = sc->qq.ensure(nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = sc->buf.ensure(static_cast<size_t>(splits) * n_r * cap * 8)) != cudaSuccess) break;
+    if ((e = sc->cnt.ensure(static_cast<size_t>(splits) * n_r * 4)) != cudaSuccess) break;
+    if ((e = sc->pool.ensure(static_cast<size_t>(n_r) * pool_cap * 4)) != cudaSuccess) break;
+    if ((e = sc->pool_n.ensure(n_r * 4ull)) != cudaSuccess) break;
+    if ((e = sc->err.ensure(16)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(sc->cnt.p, 0, static_cast<size_t>(splits) * n_r * 4, st)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(sc->err.p, 0, 16, st)) != cudaSuccess) break;
+    what = "gather kernel";
+    gather_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(n_r) * 32 + 255) / 256), 256, 0, st>>>(
+        a.queries, a.inv, a.qlist, n_r, a.dim, r.dp, sc->qp.as<float>());
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    what = "query kernel";
+    prep_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(nq_pad) * 32 + 255) / 256), 256, 0, st>>>(
+        sc->qp.as<float>(), nullptr, n_r, nq_pad, r.dim, s->kp, r.metric == HGD_METRIC_L2 ? 1 : 0, s->db,
+        sc->q16.as<__half>(), sc->qc.as<float>(), sc->qm.as<float>(), sc->qq.as<float>());
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    CUtensorMap map_q;
+    what = "tensor map";
+    if (!make_map(&map_q, sc->q16.p, nq_pad, s->kp, BM)) {
+      e = cudaErrorInvalidValue;
+      break;
+    }
+    MmaParams P{};
+    P.xn = s->xn;
+    P.qc = sc->qc.as<float>();
+    P.qm = sc->qm.as<float>();
+    P.buf = sc->buf.as<uint64_t>();
+    P.cnt = sc->cnt.as<uint32_t>();
+    P.err = sc->err.as<uint32_t>();
+    P.allow_tab = a.allow_tab;
+    P.fsel = a.fsel;
+    P.alive = a.alive;
+    P.n = r.n;
+    P.nq = n_r;
+    P.kchunks = s->kp / BK;
+    P.cap = cap;
+    P.k = k;
+    P.nbt = nbt;
+    P.tiles_q = tiles_q;
+    P.splits = splits;
+    P.tps = tps;
+    P.l2 = r.metric == HGD_METRIC_L2 ? 1 : 0;
+    P.lenient = 1;
+    what = "tensor kernel";
+    if ((e = cudaFuncSetAttribute(bf_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kSmem))) != cudaSuccess)
+      break;
+    const unsigned grid = std::min<uint32_t>(tiles_q * splits, static_cast<uint32_t>(s->sms));
+    bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    what = "select kernel";
+    select_kernel<<<(n_r * 32 + 255) / 256, 256, 0, st>>>(sc->buf.as<uint64_t>(), sc->cnt.as<uint32_t>(),
+                                                          sc->qm.as<float>(), sc->qq.as<float>(), n_r, splits, cap, k,
+                                                          sc->pool.as<uint32_t>(), pool_cap, sc->pool_n.as<uint32_t>(),
+                                                          sc->err.as<uint32_t>(), 1);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    what = "rerank kernel";
+    const int S = slots_of(r.dim);
+    const dim3 rgrid((n_r + 3) / 4);
+    const size_t rsmem = 4ull * p2max * 8;
+    const OutMap om{a.qlist, a.kq, a.k_stride, a.done};
+    e = r.metric == HGD_METRIC_L2
+            ? launch_rerank<true>(S, rgrid, rsmem, st, r.rows, r.labels, sc->qp.as<float>(), nullptr, n_r, r.dim,
+                                  r.dp, k, sc->pool.as<uint32_t>(), pool_cap, p2max, sc->pool_n.as<uint32_t>(),
+                                  static_cast<Rec*>(a.out), om)
+            : launch_rerank<false>(S, rgrid, rsmem, st, r.rows, r.labels, sc->qp.as<float>(), nullptr, n_r, r.dim,
+                                   r.dp, k, sc->pool.as<uint32_t>(), pool_cap, p2max, sc->pool_n.as<uint32_t>(),
+                                   static_cast<Rec*>(a.out), om);
+  } while (false);
+  if (e != cudaSuccess && err) *err = std::string("tensor scan: ") + what + ": " + cudaGetErrorString(e);
   return e;
 }
 

@@ -34,4 +34,27 @@ void store_free(Store* s);
 cudaError_t search(Store* s, const Rows& r, const float* queries, const float* inv, uint32_t nq, uint32_t k,
                    const uint32_t* allow, void* out, cudaStream_t st, bool* redo, std::string* err);
 
+// Queries of a graph batch routed to an exact scan (the compressed-precision
+// forms' answer to restrictive filters): each routed query is scanned over
+// the rows its filter allows (id-space bits, 32 per word) that are alive, and
+// its row of `out` (original index) is written with the first min(m, k)
+// results in the graph's distance order, then its done flag.  Enqueues only.
+struct RoutedArgs {
+  const float* queries;              // device, nq x dim raw queries of the batch
+  const float* inv;                  // device, per query 1/||q|| (cosine) or null
+  const uint32_t* qlist;             // device, n_r original query indices
+  const int32_t* fsel;               // device, n_r filter indices into allow_tab
+  const uint32_t* const* allow_tab;  // device table of id-space bitsets
+  const uint32_t* alive;             // device tombstone bits (1 = alive) or null
+  uint32_t n_r, dim, k_stride;
+  const uint32_t* kq;                // device per original query k, or null (k_stride)
+  void* out;                         // device records, original query rows of k_stride
+  uint32_t* done;                    // device per original query done flags or null
+};
+struct Scratch;
+Scratch* scratch_new();
+void scratch_free(Scratch* s);
+cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch* sc, cudaStream_t st,
+                          std::string* err);
+
 }  // namespace hg::bfm

@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "bf_mma.h"
 #include "hnswgpu_device.h"
 #include "search_common.cuh"
 
@@ -35,7 +36,8 @@ int occupancy_approx(uint32_t pdc, int metric, int prec, int wpb, size_t smem);
 cudaError_t launch_encode(const float* vecs, uint32_t n, uint32_t pd, uint32_t pdc, int prec, void* out,
                           float* scale, cudaStream_t st);
 cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, uint32_t ef_all, uint32_t ef_default,
-                          uint32_t k_all, const BucketSpec& spec, uint32_t* counts, uint32_t* lists, cudaStream_t st);
+                          uint32_t k_all, const BucketSpec& spec, uint32_t* counts, uint32_t* lists, cudaStream_t st,
+                          const uint8_t* skip);
 cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bits, const uint64_t* labels, uint32_t n,
                                     uint32_t* out, cudaStream_t st);
 }  // namespace hg
@@ -133,6 +135,12 @@ struct Workspace {
   // with the same key, replayed after that
   std::string graph_seen, graph_key;
   cudaGraphExec_t graph_exec = nullptr;
+  // queries routed to the exact scan: list, filter per entry, skip flags; the
+  // scan's scratch and stream
+  DBuf scan_qlist, scan_fsel, scan_route;
+  hg::bfm::Scratch* scan_sc = nullptr;
+  cudaStream_t scan_stream = nullptr;
+  cudaEvent_t scan_fork = nullptr, scan_join = nullptr;
   void release_all() {
     for (DBuf* d : {&q, &efq, &kq, &fsel, &fptrs, &fbits, &inv, &out, &nres, &counters, &work, &ovf_list, &pool, &pool_t2,
                     &bitmaps, &pool_big, &bitmaps_big, &owners, &lists, &pool_ids, &pool_n})
@@ -147,6 +155,16 @@ struct Workspace {
     graph_exec = nullptr;
     graph_key.clear();
     graph_seen.clear();
+    scan_qlist.release();
+    scan_fsel.release();
+    scan_route.release();
+    hg::bfm::scratch_free(scan_sc);
+    scan_sc = nullptr;
+    if (scan_stream) cudaStreamDestroy(scan_stream);
+    if (scan_fork) cudaEventDestroy(scan_fork);
+    if (scan_join) cudaEventDestroy(scan_join);
+    scan_stream = nullptr;
+    scan_fork = scan_join = nullptr;
     aux.clear();
     ev_join.clear();
     ev_fork = done = nullptr;
@@ -182,6 +200,8 @@ struct hgd_graph {
   std::mutex ws_mu;
   std::vector<std::unique_ptr<Workspace>> ws;
   PinnedBuf pin_patch;  // tombstone word staging
+  // FP16 copy of the rows for the exact scan of routed filtered queries (built on first use)
+  hg::bfm::Store* scan = nullptr;
   // autotuned launch shapes (guarded by ws_mu); version enters graph keys
   std::vector<hgd_tune_entry> tune;
   int launch_mode = HGD_LAUNCH_BUCKETS;
@@ -409,6 +429,7 @@ void hgd_graph_free(hgd_graph* g) {
     w->release_all();
   }
   g->ws.clear();
+  hg::bfm::store_free(g->scan);
   for (DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->v16, &g->v8, &g->vscale})
     d->release();
   g->pin_patch.release();
@@ -578,6 +599,43 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
       HG_CUDA(cudaMemsetAsync(w->fsel.p, 0, nq * 4, st));
     }
     d_fsel = w->fsel.as<int32_t>();
+  }
+  // ---- compressed-precision batches: restrictive filters go to the exact scan ----
+  std::vector<uint32_t> r_qlist;
+  std::vector<int32_t> r_fsel;
+  const uint8_t* d_skip = nullptr;
+  if (a->precision != HGD_PREC_FP32 && a->filter_scan_permille && a->num_filters && !a->nres && !a->counters &&
+      hg::bfm::supported(static_cast<uint32_t>(g->pd), a->k)) {
+    std::vector<char> routed(a->num_filters, 0);
+    bool any = false;
+    for (uint32_t f = 0; f < a->num_filters; ++f) {
+      const hgd_bitset& bs = a->filters[f];
+      uint64_t ones = 0;
+      const uint64_t words64 = (bs.num_bits + 63) / 64;
+      for (uint64_t i = 0; i < words64; ++i) ones += static_cast<uint64_t>(__builtin_popcountll(bs.words[i]));
+      routed[f] = ones * 1000 <= static_cast<uint64_t>(a->filter_scan_permille) * g->n;
+      any = any || routed[f];
+    }
+    if (any) {
+      std::vector<uint8_t> skip(nq, 0);
+      for (uint64_t q = 0; q < nq; ++q) {
+        const int32_t f = a->filter_of_query ? a->filter_of_query[q] : 0;
+        if (f >= 0 && routed[f]) {
+          skip[q] = 1;
+          r_qlist.push_back(static_cast<uint32_t>(q));
+          r_fsel.push_back(f);
+        }
+      }
+      if (!r_qlist.empty()) {
+        HG_CUDA(w->scan_route.ensure(nq));
+        HG_CUDA(w->scan_qlist.ensure(r_qlist.size() * 4));
+        HG_CUDA(w->scan_fsel.ensure(r_fsel.size() * 4));
+        HG_CUDA(cudaMemcpyAsync(w->scan_route.p, skip.data(), nq, cudaMemcpyHostToDevice, st));
+        HG_CUDA(cudaMemcpyAsync(w->scan_qlist.p, r_qlist.data(), r_qlist.size() * 4, cudaMemcpyHostToDevice, st));
+        HG_CUDA(cudaMemcpyAsync(w->scan_fsel.p, r_fsel.data(), r_fsel.size() * 4, cudaMemcpyHostToDevice, st));
+        d_skip = w->scan_route.as<uint8_t>();
+      }
+    }
   }
   // ---- cosine: 1/||q|| per query ----
   const float* d_inv = nullptr;
@@ -786,7 +844,7 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   P.err = work + 4;
   {
     cudaError_t e = hg::launch_bucket(d_ef, d_k, static_cast<uint32_t>(nq), a->ef, a->ef_default, a->k, spec,
-                                      work + 32, w->lists.as<uint32_t>(), st);
+                                      work + 32, w->lists.as<uint32_t>(), st, d_skip);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("bucket kernel launch: ") + cudaGetErrorString(e));
   }
   // fork: each bucket on its own stream, largest ef first, joined back into st
@@ -806,6 +864,45 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
       w->aux.push_back(s2);
       w->ev_join.push_back(e2);
     }
+  }
+  // routed queries: the exact scan on the workspace's scan stream, concurrent
+  // with the walk, joined before the results leave
+  const bool scanning = !r_qlist.empty();
+  if (scanning) {
+    hg::bfm::Rows rows{g->vecs.as<float>(), g->labels.as<uint64_t>(), static_cast<uint32_t>(g->n),
+                       static_cast<uint32_t>(g->pd), static_cast<uint32_t>(g->pd), g->metric};
+    {
+      std::lock_guard<std::mutex> build_lock(g->mu);
+      if (!g->scan) {
+        std::string err;
+        if (hg::bfm::store_create(rows, st, &g->scan, &err) != cudaSuccess) return fail(HGD_ECUDA, err);
+      }
+    }
+    if (!w->scan_sc) w->scan_sc = hg::bfm::scratch_new();
+    if (!w->scan_stream) {
+      HG_CUDA(cudaStreamCreateWithFlags(&w->scan_stream, cudaStreamNonBlocking));
+      HG_CUDA(cudaEventCreateWithFlags(&w->scan_fork, cudaEventDisableTiming));
+      HG_CUDA(cudaEventCreateWithFlags(&w->scan_join, cudaEventDisableTiming));
+    }
+    HG_CUDA(cudaEventRecord(w->scan_fork, st));
+    HG_CUDA(cudaStreamWaitEvent(w->scan_stream, w->scan_fork, 0));
+    hg::bfm::RoutedArgs ra{};
+    ra.queries = d_q;
+    ra.inv = d_inv;
+    ra.qlist = w->scan_qlist.as<uint32_t>();
+    ra.fsel = w->scan_fsel.as<int32_t>();
+    ra.allow_tab = d_fptrs;
+    ra.alive = g->alive.as<uint32_t>();
+    ra.n_r = static_cast<uint32_t>(r_qlist.size());
+    ra.dim = dim;
+    ra.k_stride = a->k;
+    ra.kq = d_k;
+    ra.out = d_out;
+    ra.done = a->done_flags;
+    std::string err;
+    if (hg::bfm::search_routed(g->scan, rows, ra, w->scan_sc, w->scan_stream, &err) != cudaSuccess)
+      return fail(HGD_ECUDA, err);
+    HG_CUDA(cudaEventRecord(w->scan_join, w->scan_stream));
   }
   if (single) {
     // one persistent launch, the largest bucket's shape, every query
@@ -871,6 +968,7 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     cudaError_t e = launch(B, static_cast<int>(rerun_slots), 1, st);
     if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("rerun kernel launch: ") + cudaGetErrorString(e));
   }
+  if (scanning) HG_CUDA(cudaStreamWaitEvent(st, w->scan_join, 0));
   // ---- results back ----
   if (!a->out_on_device) {
     HG_CUDA(cudaMemcpyAsync(a->out, d_out, nq * a->k * 16, cudaMemcpyDeviceToHost, st));

@@ -99,6 +99,7 @@ class Server {
     max_inflight_ = std::max<uint32_t>(1, std::min<uint32_t>(cfg.max_inflight ? cfg.max_inflight : 4, 15));
     max_batch_ = cfg.max_batch_queries ? cfg.max_batch_queries : 4096;
     precision_ = cfg.precision;
+    filter_scan_permille_ = cfg.filter_scan_permille;
     {
       std::shared_lock<std::shared_mutex> lk(im.api_mutex);
       g_ = im.device_graph();
@@ -331,6 +332,7 @@ class Server {
       a.out = s.out.dev;
       a.out_on_device = 1;
       a.done_flags = s.done.dev;
+      a.filter_scan_permille = filter_scan_permille_;
       a.stream = s.stream;
       a.synchronize = 0;
       rc = hgd_search(g_, &a);
@@ -433,6 +435,7 @@ class Server {
   uint32_t dim_ = 0, ef_default_ = 10, max_inflight_ = 4, max_batch_ = 4096;
   size_t n_ = 0;
   int precision_ = 0;
+  uint32_t filter_scan_permille_ = 0;
   uint64_t budget_ = 0, inflight_bytes_ = 0;
   std::mutex mu_;
   std::condition_variable cv_, cv_done_;

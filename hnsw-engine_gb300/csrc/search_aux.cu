@@ -51,9 +51,11 @@ __global__ void translate_filter_kernel(const uint64_t* __restrict__ words, uint
 // ef (per-query or batch ef, 0 -> default, at least k) is <= hi[b].
 __global__ void bucket_kernel(const uint32_t* __restrict__ efq, const uint32_t* __restrict__ kq, uint32_t nq,
                               uint32_t ef_all, uint32_t ef_default, uint32_t k_all, BucketSpec spec,
-                              uint32_t* __restrict__ counts, uint32_t* __restrict__ lists) {
+                              uint32_t* __restrict__ counts, uint32_t* __restrict__ lists,
+                              const uint8_t* __restrict__ skip) {
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq) return;
+  if (skip && skip[q]) return;  // answered by the exact scan
   const uint32_t k = kq ? kq[q] : k_all;
   uint32_t ef = efq ? efq[q] : ef_all;
   if (ef == 0) ef = ef_default;
@@ -68,9 +70,10 @@ __global__ void bucket_kernel(const uint32_t* __restrict__ efq, const uint32_t* 
 
 cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, uint32_t ef_all, uint32_t ef_default,
                           uint32_t k_all, const BucketSpec& spec, uint32_t* counts, uint32_t* lists,
-                          cudaStream_t st) {
+                          cudaStream_t st, const uint8_t* skip) {
   if (nq == 0) return cudaSuccess;
-  bucket_kernel<<<(nq + 255) / 256, 256, 0, st>>>(efq, kq, nq, ef_all, ef_default, k_all, spec, counts, lists);
+  bucket_kernel<<<(nq + 255) / 256, 256, 0, st>>>(efq, kq, nq, ef_all, ef_default, k_all, spec, counts, lists,
+                                                  skip);
   return cudaGetLastError();
 }
 

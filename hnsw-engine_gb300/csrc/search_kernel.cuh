@@ -1024,7 +1024,10 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       if (f >= 0) fb = P.fbits[f];
     }
     const bool filtered = fb != nullptr || P.deleted_any != 0;
-    uint32_t n_uplists = 0, n_updists = 0, n_lists = 0, n_dists = 0, n_visit = 0;
+    // traversal counters; the upper-layer ones are stored when the descent
+    // ends and nodes visited at layer 0 = distances + the entry point
+    uint32_t n_uplists = 0, n_updists = 0, n_lists = 0, n_dists = 0;
+    bool ran = false;
 
     int s = 0;  // result count
     Cands c{0, 0, 0, kMaxKey, 0, false, false};
@@ -1077,6 +1080,11 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
         }
       }
 
+      if (P.counters && lane == 0) {  // the descent's counters, stored now so they are not kept live
+        unsigned long long* cp = P.counters + static_cast<size_t>(q) * kCounters;
+        cp[0] = n_uplists;
+        cp[1] = n_updists;
+      }
       // ---- layer 0 (search_layer.cpp:58-134) ----
       // Results: sorted base res[0..rtop] in shared memory plus up to 32 newly
       // inserted keys in a register buffer (one per lane: rk, live set rvalid,
@@ -1086,7 +1094,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       if (lane == 0) visit(w, cur, tagged);
       __syncwarp();
       w.vcount = 1;
-      n_visit = 1;
+      ran = true;
       const uint64_t k0 = mkkey(cur_d, cur);
       const bool e0 = !filtered || (bit_of(P.alive, cur) && (!fb || bit_of(fb, cur)));
       if (lane == 0) {
@@ -1176,7 +1184,6 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
           uint32_t U = __ballot_sync(kFull, fresh);
           const int nu = __popc(U);
           w.vcount += nu;
-          n_visit += nu;
           if (!U) continue;
           n_dists += nu;
           // eligibility words load while the rows are gathered
@@ -1265,7 +1272,8 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
                                           static_cast<int>(P.R), lane);
     }
     // ---- output (search_layer.cpp:166-169, 189-192) ----
-    const int m = s < static_cast<int>(k) ? s : static_cast<int>(k);
+    const uint32_t kq = P.kq ? P.kq[q] : P.k_all;  // re-read: not kept live across the walk
+    const int m = s < static_cast<int>(kq) ? s : static_cast<int>(kq);
     {
       QueryOut* row = static_cast<QueryOut*>(P.out) + static_cast<size_t>(q) * P.k_stride;
       for (uint32_t j = lane; j < P.k_stride; j += 32) {
@@ -1286,11 +1294,13 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
     if (P.done) signal_done(P.done, q, lane);
     if (P.counters && lane == 0) {
       unsigned long long* cp = P.counters + static_cast<size_t>(q) * kCounters;
-      cp[0] = n_uplists;
-      cp[1] = n_updists;
+      if (!ran) {
+        cp[0] = 0;
+        cp[1] = 0;
+      }
       cp[2] = n_lists;
       cp[3] = n_dists;
-      cp[4] = n_visit;
+      cp[4] = ran ? n_dists + 1u : 0u;
       cp[5] = c.peak;
       cp[6] = static_cast<unsigned long long>(s);
       cp[7] = (used_bitmap ? kTierBitmap : 0u) | (c.spilled ? kTierPool : 0u) | (P.rerun ? kTierRerun : 0u) |

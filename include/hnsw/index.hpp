@@ -54,6 +54,9 @@ struct SearchOptions {
   /// device-resident batches without filters or counters: capture the launch
   /// sequence into a CUDA graph (second call of a shape) and replay it
   bool use_graph = false;
+  /// FP16 / FP8 batches: queries whose filter allows at most this many per
+  /// mille of the nodes are answered by the exact tensor-core scan (0: off)
+  uint32_t filter_scan_permille = 0;
 };
 
 class Index {

@@ -86,6 +86,10 @@ typedef struct {
                                       (then ef must bound every per-query ef) */
   int32_t out_on_device;           /* 1: out is a device pointer; the call returns once the
                                       work is queued on `stream` */
+  uint32_t filter_scan_permille;   /* precision 1 / 2: queries whose filter allows at most this
+                                      many per mille of the nodes are answered by the exact
+                                      tensor-core scan over the allowed rows (0: off) */
+  uint32_t reserved2;
 } hg_batch_options;
 
 const char* hg_last_error(void);
@@ -176,7 +180,8 @@ typedef struct {
   uint32_t max_batch_queries;  /* queries admitted into one batch (default 4096) */
   uint64_t memory_budget;      /* device bytes for batches in flight; 0 = half the free memory */
   int32_t precision;           /* 0 fp32; 1 fp16; 2 fp8 traversal + exact fp32 rerank */
-  int32_t reserved;
+  uint32_t filter_scan_permille; /* precision 1 / 2: requests whose filter allows at most this many
+                                    per mille of the nodes take the exact tensor-core scan (0: off) */
 } hg_server_config;
 typedef struct {
   const float* queries;        /* nq x dim */

@@ -112,6 +112,12 @@ typedef struct {
   uint32_t cand_cap;             /* candidate head per warp (power of two >= 128) */
   uint32_t warps_per_block;      /* 1..4 */
   uint32_t pool_cap;             /* spill pool entries per warp before a rerun */
+  /* FP16 / FP8 batches with host filters: queries whose filter allows at most
+   * this many per mille of the nodes are answered by the exact tensor-core
+   * scan over the allowed rows instead of a graph walk (0: off).  No
+   * counterpart in the reference. */
+  uint32_t filter_scan_permille;
+  uint32_t reserved3;
 } hgd_search_args;
 
 int hgd_graph_upload(const hgd_graph_view* view, int device, int order, hgd_graph** out);
