@@ -418,8 +418,10 @@ def run_serving(local):
                "note": "one search_batch call per request (the reference API: one k / ef / filter per call)"},
            "batched_fp32_search_batch_ex": {"qps": round(plain_qps, 1), "recall_at_k": plain_recall[0],
                                             "recall_at_10": plain_recall[1], "queries_per_call": chunk}}
-    for name, prec in (("fp32", 0), ("fp8_rerank", 2)):
-        srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, precision=prec)
+    # forms: FP32 walk; FP8 walk + exact rerank; the same with requests whose
+    # filter allows <= 15% of the nodes answered by the exact tensor-core scan
+    for name, prec, scan in (("fp32", 0, 0.0), ("fp8_rerank", 2, 0.0), ("fp8_rerank_filter_scan", 2, 0.15)):
+        srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, precision=prec, filter_scan=scan)
         srv.replay(requests[:2000], np.zeros(2000))  # warm-up: encodes the FP8 copy, sizes the staging
         peak, outs = srv.replay(requests, np.zeros(SERVE_REQUESTS))
         same = all(np.array_equal(outs[i]["label"], plain[offs[i]:offs[i + 1], :ks[i]]["label"])
@@ -441,8 +443,10 @@ def run_serving(local):
                                   "mean_batch_queries": round(st["mean_batch_queries"], 1)})
         srv.close()
         out[name] = form
-    out["served_fp8_over_plain_fp32"] = round(out["fp8_rerank"]["peak_qps"] / per_request_qps, 3)
-    out["served_fp8_over_batched_fp32"] = round(out["fp8_rerank"]["peak_qps"] / plain_qps, 3)
+    best = max(("fp8_rerank", "fp8_rerank_filter_scan"), key=lambda f: out[f]["peak_qps"])
+    out["served_fp8_form"] = best
+    out["served_fp8_over_plain_fp32"] = round(out[best]["peak_qps"] / per_request_qps, 3)
+    out["served_fp8_over_batched_fp32"] = round(out[best]["peak_qps"] / plain_qps, 3)
     return out
 
 
