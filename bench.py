@@ -57,9 +57,12 @@ def workload(rank: int):
     return base, queries, efs
 
 
-def launches_per_batch(ef_max: int) -> int:
-    """Kernels one batch enqueues: the ef-bucketing kernel, one query kernel per
-    ef bucket (16, 32, 64, ... up to ef_max) and the rerun pass."""
+def launches_per_batch(ef_max: int, single_launch: bool = False) -> int:
+    """Kernels one batch enqueues: the ef-bucketing kernel, the query kernels
+    (one largest-ef-first launch, or one per ef bucket 16, 32, 64, ... up to
+    ef_max) and the rerun pass."""
+    if single_launch:
+        return 3
     buckets = 0
     for hi in (16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024):
         if buckets == 11:
@@ -294,7 +297,7 @@ def run_ours(args, rank, world, local):
                    "mean_l0_distances": round(float(cnt[:, 3].mean()), 2)},
         "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": int(NQ * DIM * 4 + NQ * 4),
                 "d2h_bytes_per_step": int(NQ * K * 16)},
-        "gpu_launches": launches_per_batch(ef_max) * args.steps,
+        "gpu_launches": launches_per_batch(ef_max, tuning["launch_mode"] == 1) * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(alg_bytes)},

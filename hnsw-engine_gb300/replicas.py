@@ -45,6 +45,8 @@ def max_over_ranks(value: float, group=None) -> float:
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([float(value)], dtype=torch.float64)
+    on_gpu = dist.get_backend(group) == "nccl"  # NCCL reduces device tensors only
+    dev = torch.device("cuda", torch.cuda.current_device()) if on_gpu else torch.device("cpu")
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
     return float(t.item())
