@@ -284,7 +284,10 @@ def run_ours(args, rank, world, local):
                    "ef_mix": list(EF_CHOICES), "l2_flush": "256 MiB write before every timed step",
                    "parallelism": f"replicas x{world} (queries per replica fixed)", "build_s": round(build_s, 2),
                    "launch": ("one CUDA-graph replay per step" if use_graph else "kernel launches per step") +
-                             " (bucket kernel, per-ef-bucket persistent kernels on prioritised forked streams, rerun pass)",
+                             (" (bucket kernel, one persistent largest-ef-first search launch, rerun pass)"
+                              if tuning["launch_mode"] == 1 else
+                              " (bucket kernel, per-ef-bucket persistent launches on prioritised forked streams, "
+                              "rerun pass)"),
                    "streams_ms_per_step": round(statistics.median(stream_ms), 4) if stream_ms else None,
                    "autotune": {"seconds": round(tune_s, 2),
                                 "sample": f"{NQ} seed-2 queries of the same mixture, ef from the same set (seed 4)",
