@@ -37,6 +37,7 @@
 
 #include "bf_common.cuh"
 #include "bf_mma.h"
+#include "smem_limit.cuh"
 #include "hnswgpu_device.h"
 
 namespace hg::bfm {
@@ -730,7 +731,7 @@ cudaError_t launch_rerank(int S, dim3 grid, size_t smem, cudaStream_t st, const 
                           const uint32_t* pool, uint32_t pool_cap, uint32_t p2max, const uint32_t* pool_n, Rec* out,
                           OutMap om = OutMap{nullptr, nullptr, 0, nullptr}) {
   auto go = [&](auto fn) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaError_t e = open_smem_limit(reinterpret_cast<const void*>(fn));
     if (e != cudaSuccess) return e;
     fn<<<grid, 128, smem, st>>>(rows, labels, queries, inv, nq, dim, dp, k, pool, pool_cap, p2max, pool_n, out, om);
     return cudaGetLastError();
@@ -911,8 +912,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     P.tps = tps;
     P.l2 = r.metric == HGD_METRIC_L2 ? 1 : 0;
     what = "tensor kernel";
-    if ((e = cudaFuncSetAttribute(bf_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(kSmem))) != cudaSuccess)
+    if ((e = open_smem_limit(reinterpret_cast<const void*>(bf_mma_kernel))) != cudaSuccess)
       break;
     const uint32_t items = tiles_q * splits;
     const unsigned grid = std::min<uint32_t>(items, static_cast<uint32_t>(s->sms));
@@ -1070,8 +1070,7 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     P.l2 = r.metric == HGD_METRIC_L2 ? 1 : 0;
     P.lenient = 1;
     what = "tensor kernel";
-    if ((e = cudaFuncSetAttribute(bf_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(kSmem))) != cudaSuccess)
+    if ((e = open_smem_limit(reinterpret_cast<const void*>(bf_mma_kernel))) != cudaSuccess)
       break;
     const unsigned grid = std::min<uint32_t>(tiles_q * splits, static_cast<uint32_t>(s->sms));
     bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);

@@ -20,6 +20,7 @@
 
 #include "bf_common.cuh"
 #include "bf_mma.h"
+#include "smem_limit.cuh"
 #include "hnswgpu_device.h"
 
 namespace hg {
@@ -190,7 +191,7 @@ cudaError_t bf_launch(const BfParams& P, cudaStream_t st) {
   while (p2 < kWarps * static_cast<int>(P.k)) p2 <<= 1;
   const size_t smem = (static_cast<size_t>(kWarps) * QT * P.k + p2) * 8;
   auto* fn = bf_kernel<S, QT, L2>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  cudaError_t e = hg::open_smem_limit(reinterpret_cast<const void*>(fn));
   if (e != cudaSuccess) return e;
   fn<<<(P.nq + QT - 1) / QT, kWarps * 32, smem, st>>>(P);
   return cudaGetLastError();

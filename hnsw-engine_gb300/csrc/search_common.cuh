@@ -90,8 +90,9 @@ struct BucketSpec {
 };
 
 __host__ __device__ inline uint32_t warp_smem_bytes(uint32_t H, uint32_t R, uint32_t C) {
-  // hash + results + candidates (+32 slack) + two 32-entry staging arrays
-  return 4u * H + 8u * R + 8u * (C + 32u) + 2u * 8u * 32u;
+  // hash + results + candidates (+32 slack) + two 32-entry staging arrays +
+  // the warp's rarely used state (64 bytes)
+  return 4u * H + 8u * R + 8u * (C + 32u) + 2u * 8u * 32u + 64u;
 }
 
 }  // namespace hg

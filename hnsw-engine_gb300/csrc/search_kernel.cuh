@@ -41,6 +41,7 @@
 #include <cstdint>
 
 #include "search_common.cuh"
+#include "smem_limit.cuh"
 
 namespace hg {
 namespace sk {
@@ -558,20 +559,43 @@ struct ApproxDist {
 // ---------------------------------------------------------------------------
 // per-warp state
 // ---------------------------------------------------------------------------
+// The warp's shared-memory slab is [hash: H u32][res: R keys][cand: C + 32
+// keys][stA: 32][stE: 32]; the parts are derived from its base and the
+// launch's H / R / C (constant bank) rather than kept in registers.
+// Per-warp state written by every lane with the same value (so each lane
+// reads back a value it wrote itself) or by lane 0 alone for the counters.
+struct WarpCold {
+  uint64_t* pool;        // spill pool in use (null until the first spill)
+  const uint32_t* fb;    // the query's filter bits or null
+  int pool_idx;          // acquired shared pool (-1 none)
+  int big_idx;           // acquired second-tier pool (-1 none)
+  int bm_idx;            // acquired shared bitmap (-1 none)
+  uint32_t peak;         // largest head + pool size seen
+  uint32_t n_lists;      // layer-0 lists read (counters only)
+  uint32_t n_dists;      // layer-0 distances (counters only)
+  uint32_t spilled;      // the candidate pool was used
+};
+static_assert(sizeof(WarpCold) <= 64, "the warp's shared region reserves 64 bytes for WarpCold");
+
+// global warp slot (fixed scratch of the non-shared layouts; acquire's start)
+__device__ __forceinline__ uint64_t warp_slot(const SearchParams& P) {
+  return P.slot_base + static_cast<uint64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+}
+
 struct Warp {
-  uint32_t* hash;
-  uint64_t* res;
-  uint64_t* cand;
-  uint64_t* stA;
-  uint64_t* stE;
-  uint64_t* pool;     // spill pool in use (null until the first spill)
+  unsigned char* base;
+  __device__ __forceinline__ uint32_t* hash() const { return reinterpret_cast<uint32_t*>(base); }
+  __device__ __forceinline__ uint64_t* res(const SearchParams& P) const {
+    return reinterpret_cast<uint64_t*>(base + 4u * P.H);
+  }
+  __device__ __forceinline__ uint64_t* cand(const SearchParams& P) const { return res(P) + P.R; }
+  __device__ __forceinline__ uint64_t* stA(const SearchParams& P) const { return cand(P) + P.C + 32; }
+  __device__ __forceinline__ uint64_t* stE(const SearchParams& P) const { return stA(P) + 32; }
+  // state the traversal loop rarely touches lives in shared memory, not registers
+  __device__ __forceinline__ WarpCold* cold(const SearchParams& P) const {
+    return reinterpret_cast<WarpCold*>(stE(P) + 32);
+  }
   uint32_t* bitmap;   // visited bitmap in use
-  uint64_t slot;      // global warp slot
-  int pool_idx;       // acquired shared pool (-1 none)
-  int big_idx;        // acquired second-tier pool (-1 none)
-  int bm_idx;         // acquired shared bitmap (-1 none)
-  uint32_t hmask;
-  int hshift;
   uint32_t tag;       // epoch << 24 (tagged mode)
   uint32_t vcount;    // visited entries in the hash
   bool bitmap_mode;
@@ -603,15 +627,18 @@ __device__ __forceinline__ int acquire(uint32_t* owner, uint32_t nslots, uint64_
 __device__ __forceinline__ void release_scratch(Warp& w, const SearchParams& P, int lane) {
   __syncwarp();
   __threadfence();
+  WarpCold* cw = w.cold(P);
   if (lane == 0) {
-    if (w.pool_idx >= 0) atomicExch(P.pool_owner + w.pool_idx, 0u);
-    if (w.big_idx >= 0) atomicExch(P.big_owner + w.big_idx, 0u);
-    if (w.bm_idx >= 0) atomicExch(P.bm_owner + w.bm_idx, 0u);
+    if (cw->pool_idx >= 0) atomicExch(P.pool_owner + cw->pool_idx, 0u);
+    if (cw->big_idx >= 0) atomicExch(P.big_owner + cw->big_idx, 0u);
+    if (cw->bm_idx >= 0) atomicExch(P.bm_owner + cw->bm_idx, 0u);
   }
-  w.pool_idx = -1;
-  w.big_idx = -1;
-  w.bm_idx = -1;
-  w.pool = nullptr;
+  __syncwarp();
+  cw->pool_idx = -1;
+  cw->big_idx = -1;
+  cw->bm_idx = -1;
+  cw->pool = nullptr;
+  __syncwarp();
 }
 
 __device__ __forceinline__ bool hash_empty(uint32_t v, uint32_t tag, bool tagged) {
@@ -619,22 +646,22 @@ __device__ __forceinline__ bool hash_empty(uint32_t v, uint32_t tag, bool tagged
 }
 
 // Test-and-mark `id` (valid lanes only); returns true if it was visited.
-__device__ __forceinline__ bool visit(Warp& w, uint32_t id, bool tagged) {
+__device__ __forceinline__ bool visit(Warp& w, const SearchParams& P, uint32_t id, bool tagged) {
   if (w.bitmap_mode) {
     const uint32_t bit = 1u << (id & 31u);
     const uint32_t old = atomicOr(&w.bitmap[id >> 5], bit);
     return (old & bit) != 0;
   }
   const uint32_t key = tagged ? (w.tag | id) : id;
-  uint32_t p = (id * 0x9E3779B1u) >> w.hshift;
+  uint32_t p = (id * 0x9E3779B1u) >> (1 + __clz(P.H));
   for (;;) {
-    const uint32_t v = *reinterpret_cast<volatile const uint32_t*>(&w.hash[p]);
+    const uint32_t v = *reinterpret_cast<volatile const uint32_t*>(&w.hash()[p]);
     if (!hash_empty(v, w.tag, tagged)) {
       if (v == key) return true;
-      p = (p + 1) & w.hmask;
+      p = (p + 1) & (P.H - 1u);
       continue;
     }
-    const uint32_t old = atomicCAS(&w.hash[p], v, key);
+    const uint32_t old = atomicCAS(&w.hash()[p], v, key);
     if (old == v) return false;
     if (old == key) return true;
   }
@@ -644,17 +671,17 @@ __device__ __forceinline__ bool visit(Warp& w, uint32_t id, bool tagged) {
 __device__ __forceinline__ bool to_bitmap(Warp& w, const SearchParams& P, bool tagged, int lane) {
   const uint64_t words = P.bitmap_words;
   if (P.bm_owner) {
-    const int i = acquire(P.bm_owner, P.bm_slots, w.slot, lane);
+    const int i = acquire(P.bm_owner, P.bm_slots, warp_slot(P), lane);
     if (i < 0) return false;
-    w.bm_idx = i;
+    w.cold(P)->bm_idx = i;
     w.bitmap = P.bitmaps + static_cast<uint64_t>(i) * words;
   } else {
-    w.bitmap = P.bitmaps + w.slot * words;
+    w.bitmap = P.bitmaps + warp_slot(P) * words;
   }
   for (uint64_t i = lane; i < words; i += 32) w.bitmap[i] = 0u;
   __syncwarp();
-  for (uint32_t p = lane; p <= w.hmask; p += 32) {
-    const uint32_t v = w.hash[p];
+  for (uint32_t p = lane; p <= (P.H - 1u); p += 32) {
+    const uint32_t v = w.hash()[p];
     if (!hash_empty(v, w.tag, tagged)) {
       const uint32_t id = tagged ? (v & 0x00FFFFFFu) : v;
       atomicOr(&w.bitmap[id >> 5], 1u << (id & 31u));
@@ -722,11 +749,9 @@ __device__ inline uint64_t radix_select(const uint64_t* pool, uint64_t pn, uint6
 // Candidate queue: head = sorted cand[ch, ct) in smem, pool = unsorted spill.
 struct Cands {
   int ch, ct;
-  uint64_t pn;    // pool entries
+  uint32_t pn;    // pool entries (at most the second tier's capacity)
   uint64_t pmin;  // min key in pool (kMaxKey if empty)
-  uint32_t peak;  // largest head + pool size seen
   bool overflow;
-  bool spilled;   // the pool was used
 };
 
 // Move a pool of pn keys to the second tier (capacity big_cap); returns the
@@ -753,37 +778,43 @@ static __device__ __noinline__ int promote_pool(uint64_t* big_pool, uint64_t big
 __device__ __forceinline__ bool pool_append(Warp& w, Cands& c, const SearchParams& P, const uint64_t* src, int cnt,
                                             int lane) {
   if (cnt <= 0) return true;
-  const uint64_t cap = w.big_idx >= 0 ? P.big_cap : P.pool_cap;
+  WarpCold* cw = w.cold(P);
+  uint64_t* pool = cw->pool;
+  const int big_idx = cw->big_idx;
+  const uint64_t cap = big_idx >= 0 ? P.big_cap : P.pool_cap;
   if (c.pn + static_cast<uint64_t>(cnt) > cap) {
-    const int i = (w.big_idx >= 0 || P.big_owner == nullptr || c.pn + static_cast<uint64_t>(cnt) > P.big_cap ||
-                   w.pool == nullptr)
+    const int i = (big_idx >= 0 || P.big_owner == nullptr || c.pn + static_cast<uint64_t>(cnt) > P.big_cap ||
+                   pool == nullptr)
                       ? -1
-                      : promote_pool(P.big_pool, P.big_cap, P.big_owner, P.big_slots, w.pool, c.pn, w.slot, lane);
+                      : promote_pool(P.big_pool, P.big_cap, P.big_owner, P.big_slots, pool, c.pn, warp_slot(P), lane);
     if (i < 0) {
       c.overflow = true;
       return false;
     }
-    if (lane == 0 && w.pool_idx >= 0) atomicExch(P.pool_owner + w.pool_idx, 0u);
-    w.pool_idx = -1;
-    w.big_idx = i;
-    w.pool = P.big_pool + static_cast<uint64_t>(i) * P.big_cap;
+    if (lane == 0 && cw->pool_idx >= 0) atomicExch(P.pool_owner + cw->pool_idx, 0u);
+    __syncwarp();
+    pool = P.big_pool + static_cast<uint64_t>(i) * P.big_cap;
+    cw->pool_idx = -1;
+    cw->big_idx = i;
+    cw->pool = pool;
   }
-  if (w.pool == nullptr) {
+  if (pool == nullptr) {
     if (P.pool_owner) {
-      const int i = acquire(P.pool_owner, P.pool_slots, w.slot, lane);
+      const int i = acquire(P.pool_owner, P.pool_slots, warp_slot(P), lane);
       if (i < 0) {
         c.overflow = true;
         return false;
       }
-      w.pool_idx = i;
-      w.pool = P.pool + static_cast<uint64_t>(i) * P.pool_cap;
+      cw->pool_idx = i;
+      pool = P.pool + static_cast<uint64_t>(i) * P.pool_cap;
     } else {
-      w.pool = P.pool + w.slot * P.pool_cap;
+      pool = P.pool + warp_slot(P) * P.pool_cap;
     }
+    cw->pool = pool;
   }
-  if (lane < cnt) w.pool[c.pn + lane] = src[lane];
+  if (lane < cnt) pool[c.pn + lane] = src[lane];
   c.pn += cnt;
-  c.spilled = true;
+  cw->spilled = 1u;
   return true;
 }
 
@@ -791,6 +822,7 @@ __device__ __forceinline__ bool pool_append(Warp& w, Cands& c, const SearchParam
 // when the result set is full, first drop pool keys farther than the worst.
 __device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P, bool res_full, float worst_d, int lane) {
   __syncwarp();
+  uint64_t* const pool = w.cold(P)->pool;
   if (res_full) {
     uint64_t wpos = 0;
     for (uint64_t base = 0; base < c.pn; base += 32) {
@@ -798,16 +830,16 @@ __device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P,
       uint64_t x = 0;
       bool keep = false;
       if (i < c.pn) {
-        x = w.pool[i];
+        x = pool[i];
         keep = key_dist(x) <= worst_d;
       }
       const uint32_t bal = __ballot_sync(kFull, keep);
       __syncwarp();
-      if (keep) w.pool[wpos + __popc(bal & ((1u << lane) - 1u))] = x;
+      if (keep) pool[wpos + __popc(bal & ((1u << lane) - 1u))] = x;
       wpos += __popc(bal);
       __syncwarp();
     }
-    c.pn = wpos;
+    c.pn = static_cast<uint32_t>(wpos);
   }
   c.ch = c.ct = 0;
   c.pmin = kMaxKey;
@@ -815,23 +847,23 @@ __device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P,
   const uint64_t half = P.C / 2;
   const uint64_t take = c.pn < half ? c.pn : half;
   uint64_t T = kMaxKey;
-  if (c.pn > take) T = radix_select(w.pool, c.pn, take, reinterpret_cast<uint32_t*>(w.cand), lane);
+  if (c.pn > take) T = radix_select(pool, c.pn, take, reinterpret_cast<uint32_t*>(w.cand(P)), lane);
   __syncwarp();
   uint64_t hpos = 0, wpos = 0, newmin = kMaxKey;
   for (uint64_t base = 0; base < c.pn; base += 32) {
     const uint64_t i = base + lane;
     uint64_t x = kMaxKey;
     const bool live = i < c.pn;
-    if (live) x = w.pool[i];
+    if (live) x = pool[i];
     const bool sel = live && x <= T;
     const bool rest = live && !sel;
     const uint32_t bs = __ballot_sync(kFull, sel);
     const uint32_t br = __ballot_sync(kFull, rest);
     __syncwarp();
     const uint32_t below = (1u << lane) - 1u;
-    if (sel) w.cand[hpos + __popc(bs & below)] = x;
+    if (sel) w.cand(P)[hpos + __popc(bs & below)] = x;
     if (rest) {
-      w.pool[wpos + __popc(br & below)] = x;
+      pool[wpos + __popc(br & below)] = x;
       newmin = x < newmin ? x : newmin;
     }
     hpos += __popc(bs);
@@ -841,11 +873,11 @@ __device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P,
   newmin = ~warp_max64(~newmin);
   int p2 = 1;
   while (p2 < static_cast<int>(hpos)) p2 <<= 1;
-  for (int i = static_cast<int>(hpos) + lane; i < p2; i += 32) w.cand[i] = kMaxKey;
+  for (int i = static_cast<int>(hpos) + lane; i < p2; i += 32) w.cand(P)[i] = kMaxKey;
   __syncwarp();
-  warp_bitonic(w.cand, p2, lane);
+  warp_bitonic(w.cand(P), p2, lane);
   c.ct = static_cast<int>(hpos);
-  c.pn = wpos;
+  c.pn = static_cast<uint32_t>(wpos);
   c.pmin = wpos ? newmin : kMaxKey;
 }
 
@@ -860,19 +892,19 @@ __device__ __forceinline__ void cand_insert(Warp& w, Cands& c, const SearchParam
     int lo = c.ch, hi = c.ct;  // first head key farther than the worst result
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if (key_dist(w.cand[mid]) > worst_d) hi = mid;
+      if (key_dist(w.cand(P)[mid]) > worst_d) hi = mid;
       else lo = mid + 1;
     }
     c.ct = lo;
   }
   int mh = m;
   if (c.pn > 0) {
-    mh = __popc(__ballot_sync(kFull, lane < m && w.stA[lane] < c.pmin));
-    if (m > mh && !pool_append(w, c, P, w.stA + mh, m - mh, lane)) return;
+    mh = __popc(__ballot_sync(kFull, lane < m && w.stA(P)[lane] < c.pmin));
+    if (m > mh && !pool_append(w, c, P, w.stA(P) + mh, m - mh, lane)) return;
   }
   if (mh > 0) {
     const int n = c.ct - c.ch;
-    const int nn = warp_merge(w.cand + c.ch, n, C + 32 - c.ch, w.stA, mh, lane);
+    const int nn = warp_merge(w.cand(P) + c.ch, n, C + 32 - c.ch, w.stA(P), mh, lane);
     c.ct = c.ch + nn;
     if (c.ct > C) {
       if (c.ch > 0) {  // compact to the front
@@ -880,9 +912,9 @@ __device__ __forceinline__ void cand_insert(Warp& w, Cands& c, const SearchParam
         for (int base = 0; base < len; base += 32) {
           const int i = base + lane;
           uint64_t x = 0;
-          if (i < len) x = w.cand[c.ch + i];
+          if (i < len) x = w.cand(P)[c.ch + i];
           __syncwarp();
-          if (i < len) w.cand[i] = x;
+          if (i < len) w.cand(P)[i] = x;
           __syncwarp();
         }
         c.ct = len;
@@ -890,15 +922,18 @@ __device__ __forceinline__ void cand_insert(Warp& w, Cands& c, const SearchParam
       }
       if (c.ct > C) {  // spill the largest keys
         const int cnt = c.ct - C;
-        const uint64_t first = w.cand[C];
-        if (!pool_append(w, c, P, w.cand + C, cnt, lane)) return;
+        const uint64_t first = w.cand(P)[C];
+        if (!pool_append(w, c, P, w.cand(P) + C, cnt, lane)) return;
         c.pmin = first < c.pmin ? first : c.pmin;
         c.ct = C;
       }
     }
   }
-  const uint64_t total = static_cast<uint64_t>(c.ct - c.ch) + c.pn;
-  c.peak = total > c.peak ? static_cast<uint32_t>(total) : c.peak;
+  if (P.counters) {
+    WarpCold* cw = w.cold(P);
+    const uint32_t total = static_cast<uint32_t>(c.ct - c.ch) + static_cast<uint32_t>(c.pn);
+    cw->peak = total > cw->peak ? total : cw->peak;
+  }
 }
 
 // Publish query q's output row: every lane's writes are fenced at system
@@ -959,35 +994,31 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
   const uint32_t per_warp = warp_smem_bytes(P.H, P.R, P.C);
   unsigned char* base = smem + static_cast<size_t>(wib) * per_warp;
   Warp w;
-  w.slot = P.slot_base + static_cast<uint64_t>(blockIdx.x) * (blockDim.x >> 5) + wib;
-  w.hash = reinterpret_cast<uint32_t*>(base);
-  w.res = reinterpret_cast<uint64_t*>(base + 4u * P.H);
-  w.cand = w.res + P.R;
-  w.stA = w.cand + P.C + 32;
-  w.stE = w.stA + 32;
-  w.pool = nullptr;
+  w.base = base;
   w.bitmap = nullptr;
-  w.pool_idx = -1;
-  w.big_idx = -1;
-  w.bm_idx = -1;
-  w.hmask = P.H - 1;
-  w.hshift = 32 - (31 - __clz(P.H));
+  {
+    WarpCold* cw = w.cold(P);
+    cw->pool = nullptr;
+    cw->pool_idx = -1;
+    cw->big_idx = -1;
+    cw->bm_idx = -1;
+  }
   const bool tagged = P.tagged != 0;
   uint32_t epoch = 0;
-  for (uint32_t i = lane; i < P.H; i += 32) w.hash[i] = tagged ? 0u : kNoId;
+  for (uint32_t i = lane; i < P.H; i += 32) w.hash()[i] = tagged ? 0u : kNoId;
   __syncwarp();
 
   DP dp;
   dp.init(P);
   // a queue length read from the device never exceeds the batch (its list
   // holds at most P.nq entries)
+  const bool single_chunk = P.M0 <= 32;
   uint32_t nq = P.nq_dev ? min(*P.nq_dev, P.nq) : P.nq;
   if (P.lpt_sizes) {
     nq = 0;
     for (uint32_t b = 0; b < P.lpt_buckets; ++b) nq += P.lpt_sizes[b];
     nq = min(nq, P.nq);
   }
-  const bool single_chunk = P.M0 <= 32;
 
   for (;;) {
     uint32_t item = 0;
@@ -1018,19 +1049,31 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       continue;
     }
     const int efi = static_cast<int>(ef);
-    const uint32_t* fb = nullptr;
-    if (P.fsel) {
-      const int32_t f = P.fsel[q];
-      if (f >= 0) fb = P.fbits[f];
+    bool filtered = P.deleted_any != 0;
+    {
+      const uint32_t* fb = nullptr;
+      if (P.fsel) {
+        const int32_t f = P.fsel[q];
+        if (f >= 0) fb = P.fbits[f];
+      }
+      filtered = filtered || fb != nullptr;
+      WarpCold* cw = w.cold(P);
+      cw->fb = fb;
+      cw->peak = 0;
+      cw->spilled = 0;
+      if (lane == 0) {
+        cw->n_lists = 0;
+        cw->n_dists = 0;
+      }
     }
-    const bool filtered = fb != nullptr || P.deleted_any != 0;
     // traversal counters; the upper-layer ones are stored when the descent
-    // ends and nodes visited at layer 0 = distances + the entry point
-    uint32_t n_uplists = 0, n_updists = 0, n_lists = 0, n_dists = 0;
+    // ends, the layer-0 ones are kept in shared memory, and nodes visited at
+    // layer 0 = distances + the entry point
+    uint32_t n_uplists = 0, n_updists = 0;
     bool ran = false;
 
     int s = 0;  // result count
-    Cands c{0, 0, 0, kMaxKey, 0, false, false};
+    Cands c{0, 0, 0u, kMaxKey, false};
     if (P.n > 0) {
       // ---- query registers (prepare_vector: cosine scaled by 1/||q||) ----
       dp.load_query(P, P.queries + static_cast<size_t>(q) * P.dim, inv_norm, q, lane);
@@ -1039,13 +1082,13 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       w.vcount = 0;
       if (tagged) {
         if (++epoch == 256u) {
-          for (uint32_t i = lane; i < P.H; i += 32) w.hash[i] = 0u;
+          for (uint32_t i = lane; i < P.H; i += 32) w.hash()[i] = 0u;
           __syncwarp();
           epoch = 1;
         }
         w.tag = epoch << 24;
       } else {
-        for (uint32_t i = lane; i < P.H; i += 32) w.hash[i] = kNoId;
+        for (uint32_t i = lane; i < P.H; i += 32) w.hash()[i] = kNoId;
         __syncwarp();
         w.tag = 0;
       }
@@ -1091,18 +1134,19 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       // largest rmax).  Candidates: sorted head cand[ch..ct) (+ spill pool)
       // plus a register buffer (ck, cvalid, smallest cmin).  Buffers are
       // merged into the arrays when 32 keys have gathered.
-      if (lane == 0) visit(w, cur, tagged);
+      if (lane == 0) visit(w, P, cur, tagged);
       __syncwarp();
       w.vcount = 1;
       ran = true;
       const uint64_t k0 = mkkey(cur_d, cur);
-      const bool e0 = !filtered || (bit_of(P.alive, cur) && (!fb || bit_of(fb, cur)));
+      const uint32_t* fb0 = w.cold(P)->fb;
+      const bool e0 = !filtered || (bit_of(P.alive, cur) && (!fb0 || bit_of(fb0, cur)));
       if (lane == 0) {
-        w.cand[0] = k0;
-        if (e0) w.res[0] = k0;
+        w.cand(P)[0] = k0;
+        if (e0) w.res(P)[0] = k0;
       }
       c.ct = 1;
-      c.peak = 1;
+      if (P.counters) w.cold(P)->peak = 1;
       int rtop = e0 ? 0 : -1;
       s = rtop + 1;
       uint64_t rk = kMaxKey, ck = kMaxKey, rmax = 0, cmin = kMaxKey;
@@ -1114,9 +1158,9 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       auto flush_res = [&]() {
         const uint64_t v = warp_sort32(((rvalid >> lane) & 1u) ? rk : kMaxKey, lane);
         const int m = __popc(rvalid);
-        if (lane < m) w.stE[lane] = v;
+        if (lane < m) w.stE(P)[lane] = v;
         __syncwarp();
-        rtop = warp_merge(w.res, rtop + 1, static_cast<int>(P.R), w.stE, m, lane) - 1;
+        rtop = warp_merge(w.res(P), rtop + 1, static_cast<int>(P.R), w.stE(P), m, lane) - 1;
         rvalid = 0;
         rk = kMaxKey;
         rmax = 0;
@@ -1127,7 +1171,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
         const bool full = s >= efi;
         int m = __popc(cvalid);
         if (full) m = __popc(__ballot_sync(kFull, lane < m && key_dist(v) <= worst_d));
-        if (lane < m) w.stA[lane] = v;
+        if (lane < m) w.stA(P)[lane] = v;
         __syncwarp();
         cand_insert(w, c, P, m, full, worst_d, lane);
         cvalid = 0;
@@ -1139,7 +1183,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       uint32_t pf_cid = kNoId, pf_id = kNoId;  // adjacency of the next candidate, loaded ahead
       for (;;) {
         if (c.ch == c.ct && c.pn > 0) refill(w, c, P, s >= efi, worst_d, lane);
-        const uint64_t bh = c.ch < c.ct ? w.cand[c.ch] : kMaxKey;
+        const uint64_t bh = c.ch < c.ct ? w.cand(P)[c.ch] : kMaxKey;
         const uint64_t top = bh < cmin ? bh : cmin;
         if (top == kMaxKey) break;
         if (s >= efi && key_dist(top) > worst_d) break;
@@ -1151,7 +1195,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
         }
         const uint32_t cid = static_cast<uint32_t>(top);
         const uint32_t* lst = P.l0 + static_cast<size_t>(cid) * P.l0_stride;
-        ++n_lists;
+        if (P.counters && lane == 0) w.cold(P)->n_lists++;
         for (uint32_t c0 = 0; c0 < P.M0; c0 += 32) {
           const uint32_t j = c0 + lane;
           uint32_t id;
@@ -1159,7 +1203,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
           else id = j < P.M0 ? __ldg(lst + j) : kNoId;
           if (c0 == 0 && single_chunk) {
             // load the list of the next candidate while this one is expanded
-            const uint64_t nb = c.ch < c.ct ? w.cand[c.ch] : kMaxKey;
+            const uint64_t nb = c.ch < c.ct ? w.cand(P)[c.ch] : kMaxKey;
             const uint64_t nx = nb < cmin ? nb : cmin;
             pf_cid = nx != kMaxKey ? static_cast<uint32_t>(nx) : kNoId;
             if (pf_cid != kNoId) pf_id = lane < static_cast<int>(P.M0)
@@ -1179,16 +1223,17 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
             first = (__ffs(same) - 1) == lane;
           }
           bool fresh = false;
-          if (first) fresh = !visit(w, id, tagged);
+          if (first) fresh = !visit(w, P, id, tagged);
           __syncwarp();
           uint32_t U = __ballot_sync(kFull, fresh);
           const int nu = __popc(U);
           w.vcount += nu;
           if (!U) continue;
-          n_dists += nu;
+          if (P.counters && lane == 0) w.cold(P)->n_dists += nu;
           // eligibility words load while the rows are gathered
           uint32_t ew = ~0u;
           if (filtered && fresh) {
+            const uint32_t* fb = w.cold(P)->fb;
             const uint32_t aw = __ldg(P.alive + (id >> 5));
             const uint32_t fw = fb ? __ldg(fb + (id >> 5)) : ~0u;
             ew = aw & fw;
@@ -1228,7 +1273,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
             if (s < efi) {
               if (++s < efi) continue;
             } else {  // evict the largest of res[rtop] and the buffer
-              const uint64_t bt = rtop >= 0 ? w.res[rtop] : 0ull;
+              const uint64_t bt = rtop >= 0 ? w.res(P)[rtop] : 0ull;
               if (bt > rmax) {
                 --rtop;
               } else {
@@ -1236,12 +1281,15 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
                 rmax = warp_max64(((rvalid >> lane) & 1u) ? rk : 0ull);
               }
             }
-            const uint64_t bt = rtop >= 0 ? w.res[rtop] : 0ull;
+            const uint64_t bt = rtop >= 0 ? w.res(P)[rtop] : 0ull;
             worst_d = key_dist(bt > rmax ? bt : rmax);
           }
           if (c.overflow) break;
-          const uint64_t live = static_cast<uint64_t>(c.ct - c.ch) + c.pn + __popc(cvalid);
-          c.peak = live > c.peak ? static_cast<uint32_t>(live) : c.peak;
+          if (P.counters) {
+            WarpCold* cw = w.cold(P);
+            const uint32_t live = static_cast<uint32_t>(c.ct - c.ch) + c.pn + __popc(cvalid);
+            cw->peak = live > cw->peak ? live : cw->peak;
+          }
         }
         if (c.overflow) break;
       }
@@ -1249,7 +1297,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
     }
 
     const bool used_bitmap = w.bitmap_mode;
-    const bool used_pool2 = w.big_idx >= 0;
+    const bool used_pool2 = w.cold(P)->big_idx >= 0;
     release_scratch(w, P, lane);
     if (c.overflow) {
       if (lane == 0) {
@@ -1264,11 +1312,11 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       // query's global row, their distances are recomputed in the reference's
       // order and merged 32 at a time into the (now free) result array.
       uint32_t* prow = P.pool_out + static_cast<size_t>(q) * P.pool_stride;
-      for (int j = lane; j < s; j += 32) prow[j] = static_cast<uint32_t>(w.res[j]);
+      for (int j = lane; j < s; j += 32) prow[j] = static_cast<uint32_t>(w.res(P)[j]);
       if (lane == 0) P.pool_n[q] = static_cast<uint32_t>(s);
       __syncwarp();
       fused_rerank<typename DP::Exact, L2>(P.vecs, P.pd, P.dim, P.queries + static_cast<size_t>(q) * P.dim,
-                                          inv_norm ? inv_norm[q] : 1.0f, inv_norm != nullptr, prow, s, w.res, w.stE,
+                                          inv_norm ? inv_norm[q] : 1.0f, inv_norm != nullptr, prow, s, w.res(P), w.stE(P),
                                           static_cast<int>(P.R), lane);
     }
     // ---- output (search_layer.cpp:166-169, 189-192) ----
@@ -1279,7 +1327,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       for (uint32_t j = lane; j < P.k_stride; j += 32) {
         QueryOut o;
         if (static_cast<int>(j) < m) {
-          const uint64_t kk = w.res[j];
+          const uint64_t kk = w.res(P)[j];
           o.label = P.labels[static_cast<uint32_t>(kk)];
           o.dist = key_dist(kk);
         } else {
@@ -1293,6 +1341,8 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
     if (P.nres && lane == 0) P.nres[q] = static_cast<uint32_t>(m);
     if (P.done) signal_done(P.done, q, lane);
     if (P.counters && lane == 0) {
+      const WarpCold* cw = w.cold(P);
+      const uint32_t n_lists = cw->n_lists, n_dists = cw->n_dists;
       unsigned long long* cp = P.counters + static_cast<size_t>(q) * kCounters;
       if (!ran) {
         cp[0] = 0;
@@ -1301,9 +1351,9 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       cp[2] = n_lists;
       cp[3] = n_dists;
       cp[4] = ran ? n_dists + 1u : 0u;
-      cp[5] = c.peak;
+      cp[5] = cw->peak;
       cp[6] = static_cast<unsigned long long>(s);
-      cp[7] = (used_bitmap ? kTierBitmap : 0u) | (c.spilled ? kTierPool : 0u) | (P.rerun ? kTierRerun : 0u) |
+      cp[7] = (used_bitmap ? kTierBitmap : 0u) | (cw->spilled ? kTierPool : 0u) | (P.rerun ? kTierRerun : 0u) |
               (used_pool2 ? kTierPool2 : 0u);
     }
     __syncwarp();
@@ -1315,7 +1365,7 @@ template <class DP, bool L2>
 cudaError_t launch_t(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st) {
   const size_t smem = static_cast<size_t>(wpb) * warp_smem_bytes(P.H, P.R, P.C);
   auto* fn = search_kernel<DP, L2>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  cudaError_t e = open_smem_limit(reinterpret_cast<const void*>(fn));
   if (e != cudaSuccess) return e;
   fn<<<blocks, 32 * wpb, smem, st>>>(P, inv);
   return cudaGetLastError();
@@ -1325,8 +1375,7 @@ template <class DP, bool L2>
 int occupancy_t(int wpb, size_t smem) {
   int blocks = 0;
   auto* fn = search_kernel<DP, L2>;
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
-    return 0;
+  if (open_smem_limit(reinterpret_cast<const void*>(fn)) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 32 * wpb, smem) != cudaSuccess) return 0;
   return blocks;
 }
