@@ -413,7 +413,7 @@ __device__ __forceinline__ float lane_dists(const Layout<NB, NT, S>& L, const fl
 template <int NB, int NT, int S, int G>
 struct ExactDist {
   static constexpr bool kApprox = false;
-  static constexpr int kMinBlocks = S >= 16 ? 4 : 6;
+  static constexpr int kMinBlocks = S >= 16 ? 4 : 6;  // (128, 7) measured 9% slower
   static constexpr int kSlots = S;
   template <bool L2>
   __device__ __forceinline__ static float rows(const Layout<NB, NT, S>& L, const float* __restrict__ vecs, uint32_t pd,
