@@ -335,6 +335,7 @@ SERVE_LOADS = (0.25, 0.5, 0.75, 1.0)
 SERVE_FILTERS = 16  # pool of distinct random 10%-density bitsets
 SERVE_RECALL_REQUESTS = 2000
 SERVE_PLAIN_REQUESTS = 2000
+SERVE_RERANK_FACTOR = 4  # FP8 forms: exact rerank of the pool's best 4 x k (at least 32)
 
 
 def serving_workload():
@@ -437,16 +438,20 @@ def run_serving(local):
                "note": "one search_batch call per request (the reference API: one k / ef / filter per call)"},
            "batched_fp32_search_batch_ex": {"qps": round(plain_qps, 1), "recall_at_k": plain_recall[0],
                                             "recall_at_10": plain_recall[1], "queries_per_call": chunk}}
-    # forms: FP32 walk; FP8 walk + exact rerank; the same with requests whose
-    # filter allows <= 15% of the nodes answered by the exact tensor-core scan
-    for name, prec, scan in (("fp32", 0, 0.0), ("fp8_rerank", 2, 0.0), ("fp8_rerank_filter_scan", 2, 0.15)):
-        srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, precision=prec, filter_scan=scan)
+    # forms: FP32 walk; FP8 walk + exact rerank of the pool's best
+    # SERVE_RERANK_FACTOR x k; the same with requests whose filter allows <= 15%
+    # of the nodes answered by the exact tensor-core scan
+    for name, prec, scan, rf in (("fp32", 0, 0.0, 0), ("fp8_rerank", 2, 0.0, SERVE_RERANK_FACTOR),
+                                 ("fp8_rerank_filter_scan", 2, 0.15, SERVE_RERANK_FACTOR)):
+        srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, precision=prec, filter_scan=scan,
+                             rerank_factor=rf)
         srv.replay(requests[:2000], np.zeros(2000))  # warm-up: encodes the FP8 copy, sizes the staging
         peak, outs = srv.replay(requests, np.zeros(SERVE_REQUESTS))
         same = all(np.array_equal(outs[i]["label"], plain[offs[i]:offs[i + 1], :ks[i]]["label"])
                    for i in range(SERVE_REQUESTS)) if prec == 0 else None
         rec = recall(lambda q, k: outs[req_rows[q]][q - offs[req_rows[q]], :k]["label"].astype(np.int64))
         form = {"peak_qps": round(peak["qps"], 1), "recall_at_k": rec[0], "recall_at_10": rec[1],
+                "rerank_factor": rf,
                 "peak_p50_ms": round(peak["p50_ms"], 3), "peak_mean_batch_queries": round(peak["mean_batch_queries"], 1),
                 "loads": []}
         if same is not None:

@@ -721,6 +721,7 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     HG_CUDA(w->pool_n.ensure(nq * 4));
     P.pool_out = w->pool_ids.as<uint32_t>();
     P.pool_n = w->pool_n.as<uint32_t>();
+    P.rerank_factor = a->rerank_factor;
   }
   auto launch = [&](const hg::SearchParams& B, int blocks, int wpb, cudaStream_t sb) {
     return prec == HGD_PREC_FP32 ? hg::launch_search(B, d_inv, blocks, wpb, sb)

@@ -100,6 +100,7 @@ class Server {
     max_batch_ = cfg.max_batch_queries ? cfg.max_batch_queries : 4096;
     precision_ = cfg.precision;
     filter_scan_permille_ = cfg.filter_scan_permille;
+    rerank_factor_ = cfg.rerank_factor;
     {
       std::shared_lock<std::shared_mutex> lk(im.api_mutex);
       g_ = im.device_graph();
@@ -333,6 +334,7 @@ class Server {
       a.out_on_device = 1;
       a.done_flags = s.done.dev;
       a.filter_scan_permille = filter_scan_permille_;
+      a.rerank_factor = rerank_factor_;
       a.stream = s.stream;
       a.synchronize = 0;
       rc = hgd_search(g_, &a);
@@ -436,6 +438,7 @@ class Server {
   size_t n_ = 0;
   int precision_ = 0;
   uint32_t filter_scan_permille_ = 0;
+  uint32_t rerank_factor_ = 0;
   uint64_t budget_ = 0, inflight_bytes_ = 0;
   std::mutex mu_;
   std::condition_variable cv_, cv_done_;

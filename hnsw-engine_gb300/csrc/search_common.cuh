@@ -75,6 +75,7 @@ struct SearchParams {
   uint32_t* pool_out;       // nq x pool_stride: final traversal pool (ids, sorted by traversal distance)
   uint32_t pool_stride;
   uint32_t* pool_n;         // nq: pool size
+  uint32_t rerank_factor;   // rerank the best rerank_factor x k pool entries (>= 32); 0 = all
   uint32_t* work;           // work-queue counter (zeroed before launch)
   uint32_t* ovf_list;       // queries whose pool overflowed
   uint32_t* ovf_count;

@@ -1307,10 +1307,17 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
       continue;
     }
 
+    const uint32_t kq = P.kq ? P.kq[q] : P.k_all;  // re-read: not kept live across the walk
     if constexpr (DP::kApprox) {
       // Exact FP32 rerank of the traversal pool, fused: the pool ids go to the
       // query's global row, their distances are recomputed in the reference's
-      // order and merged 32 at a time into the (now free) result array.
+      // order and merged 32 at a time into the (now free) result array.  With
+      // a rerank factor only the pool's best factor x k (at least 32) are
+      // reranked; the pool is sorted by traversal distance.
+      if (P.rerank_factor) {
+        const uint64_t depth = max(32ull, static_cast<unsigned long long>(P.rerank_factor) * kq);
+        if (static_cast<uint64_t>(s) > depth) s = static_cast<int>(depth);
+      }
       uint32_t* prow = P.pool_out + static_cast<size_t>(q) * P.pool_stride;
       for (int j = lane; j < s; j += 32) prow[j] = static_cast<uint32_t>(w.res(P)[j]);
       if (lane == 0) P.pool_n[q] = static_cast<uint32_t>(s);
@@ -1320,7 +1327,6 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
                                           static_cast<int>(P.R), lane);
     }
     // ---- output (search_layer.cpp:166-169, 189-192) ----
-    const uint32_t kq = P.kq ? P.kq[q] : P.k_all;  // re-read: not kept live across the walk
     const int m = s < static_cast<int>(kq) ? s : static_cast<int>(kq);
     {
       QueryOut* row = static_cast<QueryOut*>(P.out) + static_cast<size_t>(q) * P.k_stride;

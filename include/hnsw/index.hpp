@@ -57,6 +57,9 @@ struct SearchOptions {
   /// FP16 / FP8 batches: queries whose filter allows at most this many per
   /// mille of the nodes are answered by the exact tensor-core scan (0: off)
   uint32_t filter_scan_permille = 0;
+  /// FP16 / FP8 batches: the exact FP32 rerank covers the best
+  /// rerank_factor x k entries of the traversal pool (at least 32); 0 = all
+  uint32_t rerank_factor = 0;
 };
 
 class Index {

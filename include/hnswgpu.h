@@ -89,7 +89,8 @@ typedef struct {
   uint32_t filter_scan_permille;   /* precision 1 / 2: queries whose filter allows at most this
                                       many per mille of the nodes are answered by the exact
                                       tensor-core scan over the allowed rows (0: off) */
-  uint32_t reserved2;
+  uint32_t rerank_factor;          /* precision 1 / 2: exact rerank of the best rerank_factor x k
+                                      pool entries (at least 32); 0 = the whole pool */
 } hg_batch_options;
 
 const char* hg_last_error(void);
@@ -182,6 +183,8 @@ typedef struct {
   int32_t precision;           /* 0 fp32; 1 fp16; 2 fp8 traversal + exact fp32 rerank */
   uint32_t filter_scan_permille; /* precision 1 / 2: requests whose filter allows at most this many
                                     per mille of the nodes take the exact tensor-core scan (0: off) */
+  uint32_t rerank_factor;        /* precision 1 / 2: exact rerank of the best rerank_factor x k pool
+                                    entries (at least 32); 0 = the whole pool */
 } hg_server_config;
 typedef struct {
   const float* queries;        /* nq x dim */

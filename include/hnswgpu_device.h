@@ -117,7 +117,10 @@ typedef struct {
    * scan over the allowed rows instead of a graph walk (0: off).  No
    * counterpart in the reference. */
   uint32_t filter_scan_permille;
-  uint32_t reserved3;
+  /* FP16 / FP8: the exact FP32 rerank covers the best rerank_factor x k
+   * entries of the traversal pool (at least 32); 0 = the whole pool (ef
+   * entries).  No counterpart in the reference. */
+  uint32_t rerank_factor;
 } hgd_search_args;
 
 int hgd_graph_upload(const hgd_graph_view* view, int device, int order, hgd_graph** out);

@@ -14,9 +14,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _check(hg, oracle, ix, base, q, k, ef, prec, metric, min_overlap):
+def _check(hg, oracle, ix, base, q, k, ef, prec, metric, min_overlap, rerank_factor=0):
     exact = ix.search_raw(q, k, ef)
-    rec = ix.search_batch_ex(q, k, ef, precision=prec)
+    rec = ix.search_batch_ex(q, k, ef, precision=prec, rerank_factor=rerank_factor)
     labels = rec["label"].astype(np.int64)
     assert (labels >= 0).all()
     for i in range(q.shape[0]):
@@ -68,3 +68,17 @@ def test_cosine_filters_deletes(hg, oracle, graphs, prec):
     exact = ix.search_raw(q, 10, 160, filter=hg.Bitset(fw, 4000))
     overlap = np.mean([len(set(a) & set(b)) / 10 for a, b in zip(labels, exact["label"].astype(np.int64))])
     assert overlap >= 0.9
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_rerank_factor(hg, oracle, graphs, prec):
+    """A rerank factor covering the whole pool changes nothing; a small one
+    reranks only the pool's best factor x k, with distances still exact."""
+    base, q, *_ = graphs.data("c1")
+    ix = hg.Index.load(graphs.path("c1"))
+    full = ix.search_batch_ex(q[:200], 10, 200, precision=prec)
+    covering = ix.search_batch_ex(q[:200], 10, 200, precision=prec, rerank_factor=20)  # 20 x 10 >= ef
+    assert full.tobytes() == covering.tobytes()
+    o_full = _check(hg, oracle, ix, base, q[:200], 10, 200, prec, "l2", 0.85)
+    o_part = _check(hg, oracle, ix, base, q[:200], 10, 200, prec, "l2", 0.85, rerank_factor=4)
+    assert o_part >= o_full - 0.01, (o_part, o_full)
