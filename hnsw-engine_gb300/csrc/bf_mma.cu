@@ -166,6 +166,31 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// tcgen05.ld without its wait: r may be read only after tmem_wait(r).
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+// Wait for this thread's TMEM loads.  r passes through the wait, so no read
+// of it is scheduled above it.
+__device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                 "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                 "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+               :
+               : "memory");
+}
+
 __device__ __forceinline__ float dist_of_key_bits(uint32_t kb) {
   const uint32_t u = (kb & 0x80000000u) ? (kb & 0x7FFFFFFFu) : ~kb;
   return __uint_as_float(u);
@@ -355,37 +380,53 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tc_fence_after();
         const uint32_t taddr = tmem + ((quarter * 32u) << 16) + ab * BN;
-#pragma unroll 1
-        for (uint32_t ch = 0; ch < BN / 32; ++ch) {
-          __syncwarp();
-          uint32_t r[32];
-          tmem_ld32(taddr + ch * 32u, r);
-          const uint32_t j0 = bt * BN + ch * 32u;
-          if (j0 >= P.n) continue;  // warp-uniform: padding rows of the last tile
-          uint32_t valid = P.n - j0 >= 32u ? 0xFFFFFFFFu : ((1u << (P.n - j0)) - 1u);
-          if (allow_q) valid &= __ldg(allow_q + (j0 >> 5));
-          if (P.alive) valid &= __ldg(P.alive + (j0 >> 5));
-          if (!live_q || over) valid = 0u;
-          float sv[32];
+        // Software-pipelined over the tile's 8 chunks of 32 rows: the TMEM
+        // load and the global loads (row norms, filter and tombstone words)
+        // of chunk ch + 1 are in flight while chunk ch is scored.
+        uint32_t ra[32], rb[32];
+        float xa[32], xb[32];
+        uint32_t va = 0, vb = 0;
+        auto fetch = [&](uint32_t ch, uint32_t (&r)[32], float (&xs)[32], uint32_t& valid) {
+          tmem_ld32_async(taddr + ch * 32u, r);
+          const uint32_t j0 = bt * BN + ch * 32u;  // < n_pad: xn holds n_pad entries
           const float4* x4 = reinterpret_cast<const float4*>(P.xn + j0);
 #pragma unroll
           for (int v = 0; v < 8; ++v) {
             const float4 t = __ldg(x4 + v);
-            const float xs[4] = {t.x, t.y, t.z, t.w};
+            xs[4 * v] = t.x;
+            xs[4 * v + 1] = t.y;
+            xs[4 * v + 2] = t.z;
+            xs[4 * v + 3] = t.w;
+          }
+          valid = 0u;
+          if (j0 < P.n && live_q && !over) {  // padding rows of the last tile stay masked
+            valid = P.n - j0 >= 32u ? 0xFFFFFFFFu : ((1u << (P.n - j0)) - 1u);
+            if (allow_q) valid &= __ldg(allow_q + (j0 >> 5));
+            if (P.alive) valid &= __ldg(P.alive + (j0 >> 5));
+          }
+        };
+        auto score = [&](uint32_t ch, const uint32_t (&r)[32], const float (&xs)[32], uint32_t valid) {
+          const uint32_t j0 = bt * BN + ch * 32u;
+          if (over) valid = 0u;  // set by a compaction of an earlier chunk
+          float sv[32];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const float acc = __uint_as_float(r[4 * v + u]);
-              sv[4 * v + u] = P.l2 ? __fmaf_rn(acc, cq, xs[u]) : __fmul_rn(acc, cq);
-            }
+          for (int c = 0; c < 32; ++c) {
+            const float acc = __uint_as_float(r[c]);
+            sv[c] = P.l2 ? __fmaf_rn(acc, cq, xs[c]) : __fmul_rn(acc, cq);
           }
           if (valid != 0xFFFFFFFFu) {  // masked rows become NaN: never <= thr, ignored by fminf
 #pragma unroll
             for (int c = 0; c < 32; ++c)
               if (!((valid >> c) & 1u)) sv[c] = __int_as_float(0x7fffffff);
           }
-          float mn = sv[0];
+          float m16[16];  // the chunk minimum as a 5-level tree
 #pragma unroll
-          for (int c = 1; c < 32; ++c) mn = fminf(mn, sv[c]);
+          for (int c = 0; c < 16; ++c) m16[c] = fminf(sv[c], sv[c + 16]);
+#pragma unroll
+          for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+            for (int c = 0; c < w; ++c) m16[c] = fminf(m16[c], m16[c + w]);
+          const float mn = m16[0];
           if (mn <= thr) {  // rare once the threshold has settled
 #pragma unroll
             for (int c = 0; c < 32; ++c)
@@ -410,6 +451,22 @@ __global__ void __launch_bounds__(kThreads, 1)
               }
             }
           }
+        };
+        // tcgen05.ld / wait::ld are .sync.aligned: the warp is converged at each
+        __syncwarp();
+        fetch(0, ra, xa, va);
+        tmem_wait(ra);
+#pragma unroll 1
+        for (uint32_t ch = 0; ch < BN / 32; ch += 2) {
+          __syncwarp();
+          fetch(ch + 1, rb, xb, vb);
+          score(ch, ra, xa, va);
+          __syncwarp();
+          tmem_wait(rb);
+          if (ch + 2 < BN / 32) fetch(ch + 2, ra, xa, va);
+          score(ch + 1, rb, xb, vb);
+          __syncwarp();
+          if (ch + 2 < BN / 32) tmem_wait(ra);
         }
         __syncwarp();
         tc_fence_before();
