@@ -818,18 +818,36 @@ __device__ __forceinline__ bool pool_append(Warp& w, Cands& c, const SearchParam
   return true;
 }
 
+// Merge a register buffer (one key per lane, lanes in `valid`) into the sorted
+// array a[0..n) of capacity cap through the staging array st; returns the new
+// length.  Out of line: it runs once per 32 accepted results.
+static __device__ __noinline__ int merge_buffer(uint64_t key, uint32_t valid, uint64_t* a, int n, int cap, uint64_t* st,
+                                                int lane) {
+  const uint64_t v = warp_sort32(((valid >> lane) & 1u) ? key : kMaxKey, lane);
+  const int m = __popc(valid);
+  if (lane < m) st[lane] = v;
+  __syncwarp();
+  return warp_merge(a, n, cap, st, m, lane);
+}
+
 // Refill an empty head from the pool with its smallest keys (at most C/2);
 // when the result set is full, first drop pool keys farther than the worst.
-__device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P, bool res_full, float worst_d, int lane) {
-  __syncwarp();
-  uint64_t* const pool = w.cold(P)->pool;
+// Out of line with plain arguments: a rare path kept out of the traversal
+// loop's instruction footprint.
+struct RefillOut {
+  int ct;
+  uint32_t pn;
+  uint64_t pmin;
+};
+static __device__ __noinline__ RefillOut refill_core(uint64_t* pool, uint32_t pn, uint64_t* cand, uint32_t C,
+                                                     bool res_full, float worst_d, int lane) {
   if (res_full) {
     uint64_t wpos = 0;
-    for (uint64_t base = 0; base < c.pn; base += 32) {
+    for (uint64_t base = 0; base < pn; base += 32) {
       const uint64_t i = base + lane;
       uint64_t x = 0;
       bool keep = false;
-      if (i < c.pn) {
+      if (i < pn) {
         x = pool[i];
         keep = key_dist(x) <= worst_d;
       }
@@ -839,21 +857,20 @@ __device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P,
       wpos += __popc(bal);
       __syncwarp();
     }
-    c.pn = static_cast<uint32_t>(wpos);
+    pn = static_cast<uint32_t>(wpos);
   }
-  c.ch = c.ct = 0;
-  c.pmin = kMaxKey;
-  if (c.pn == 0) return;
-  const uint64_t half = P.C / 2;
-  const uint64_t take = c.pn < half ? c.pn : half;
+  RefillOut o{0, pn, kMaxKey};
+  if (pn == 0) return o;
+  const uint64_t half = C / 2;
+  const uint64_t take = pn < half ? pn : half;
   uint64_t T = kMaxKey;
-  if (c.pn > take) T = radix_select(pool, c.pn, take, reinterpret_cast<uint32_t*>(w.cand(P)), lane);
+  if (pn > take) T = radix_select(pool, pn, take, reinterpret_cast<uint32_t*>(cand), lane);
   __syncwarp();
   uint64_t hpos = 0, wpos = 0, newmin = kMaxKey;
-  for (uint64_t base = 0; base < c.pn; base += 32) {
+  for (uint64_t base = 0; base < pn; base += 32) {
     const uint64_t i = base + lane;
     uint64_t x = kMaxKey;
-    const bool live = i < c.pn;
+    const bool live = i < pn;
     if (live) x = pool[i];
     const bool sel = live && x <= T;
     const bool rest = live && !sel;
@@ -861,7 +878,7 @@ __device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P,
     const uint32_t br = __ballot_sync(kFull, rest);
     __syncwarp();
     const uint32_t below = (1u << lane) - 1u;
-    if (sel) w.cand(P)[hpos + __popc(bs & below)] = x;
+    if (sel) cand[hpos + __popc(bs & below)] = x;
     if (rest) {
       pool[wpos + __popc(br & below)] = x;
       newmin = x < newmin ? x : newmin;
@@ -873,12 +890,22 @@ __device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P,
   newmin = ~warp_max64(~newmin);
   int p2 = 1;
   while (p2 < static_cast<int>(hpos)) p2 <<= 1;
-  for (int i = static_cast<int>(hpos) + lane; i < p2; i += 32) w.cand(P)[i] = kMaxKey;
+  for (int i = static_cast<int>(hpos) + lane; i < p2; i += 32) cand[i] = kMaxKey;
   __syncwarp();
-  warp_bitonic(w.cand(P), p2, lane);
-  c.ct = static_cast<int>(hpos);
-  c.pn = static_cast<uint32_t>(wpos);
-  c.pmin = wpos ? newmin : kMaxKey;
+  warp_bitonic(cand, p2, lane);
+  o.ct = static_cast<int>(hpos);
+  o.pn = static_cast<uint32_t>(wpos);
+  o.pmin = wpos ? newmin : kMaxKey;
+  return o;
+}
+
+__device__ __forceinline__ void refill(Warp& w, Cands& c, const SearchParams& P, bool res_full, float worst_d, int lane) {
+  __syncwarp();
+  const RefillOut o = refill_core(w.cold(P)->pool, c.pn, w.cand(P), P.C, res_full, worst_d, lane);
+  c.ch = 0;
+  c.ct = o.ct;
+  c.pn = o.pn;
+  c.pmin = o.pmin;
 }
 
 // Insert the sorted accepted batch stA[0..m) into the candidate queue.
@@ -1156,11 +1183,7 @@ __global__ void __launch_bounds__(128, DP::kMinBlocks) search_kernel(SearchParam
 
       // merge the result buffer into the sorted base
       auto flush_res = [&]() {
-        const uint64_t v = warp_sort32(((rvalid >> lane) & 1u) ? rk : kMaxKey, lane);
-        const int m = __popc(rvalid);
-        if (lane < m) w.stE(P)[lane] = v;
-        __syncwarp();
-        rtop = warp_merge(w.res(P), rtop + 1, static_cast<int>(P.R), w.stE(P), m, lane) - 1;
+        rtop = merge_buffer(rk, rvalid, w.res(P), rtop + 1, static_cast<int>(P.R), w.stE(P), lane) - 1;
         rvalid = 0;
         rk = kMaxKey;
         rmax = 0;
