@@ -78,6 +78,7 @@ struct MmaParams {
   const int32_t* fsel;
   const uint32_t* alive;
   uint32_t n, nq, kchunks, cap, k, nbt, tiles_q, splits, tps;
+  uint32_t trig;  // a lane's buffer is compacted once it could pass trig - 32 keys (<= cap)
   int l2;
   int lenient;  // keep the buffer of a query whose candidates overflow (approximate answer) instead of failing
 };
@@ -367,6 +368,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const float margin = P.qm[q];
       uint64_t* bufp = P.buf + (static_cast<size_t>(sp) * P.nq + (live_q ? q : 0)) * P.cap;
       uint32_t cnt = 0;
+      uint32_t lim = P.trig;  // compaction point: the threshold tightens early
       float thr = __int_as_float(0x7f800000);
       bool over = false;
       for (uint32_t bt = b0; bt < b1; ++bt, ++acc_i) {
@@ -433,7 +435,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               if (sv[c] <= thr) bufp[cnt++] = (static_cast<uint64_t>(okey(sv[c])) << 32) | (j0 + c);
           }
           // room for the next chunk: compact the lanes that are nearly full
-          uint32_t need = __ballot_sync(kFull, cnt + 32u > P.cap);
+          uint32_t need = __ballot_sync(kFull, cnt + 32u > lim);
           while (need) {
             const int L = __ffs(need) - 1;
             need &= need - 1;
@@ -444,7 +446,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t kept = warp_compact(lb, lc, P.k, lm, lane, &lthr);
             if (lane == L) {
               cnt = kept;
-              thr = lthr;
+              thr = fminf(thr, lthr);  // both bound the k-th: keep the tighter
+              lim = min(P.cap, max(P.trig, cnt + 64u));  // no compaction again before 32 new keys
               if (cnt + 32u > P.cap) {  // the margin keeps too many rows: give this query up
                 over = true;
                 thr = -__int_as_float(0x7f800000);
@@ -962,6 +965,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     P.nq = nq;
     P.kchunks = s->kp / BK;
     P.cap = cap;
+    P.trig = std::min<uint32_t>(cap, std::max<uint32_t>(96, round_up(2 * k + 64, 32)));
     P.k = k;
     P.nbt = nbt;
     P.tiles_q = tiles_q;
@@ -1119,6 +1123,7 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     P.nq = n_r;
     P.kchunks = s->kp / BK;
     P.cap = cap;
+    P.trig = std::min<uint32_t>(cap, std::max<uint32_t>(96, round_up(2 * k + 64, 32)));
     P.k = k;
     P.nbt = nbt;
     P.tiles_q = tiles_q;
