@@ -197,39 +197,55 @@ __device__ __forceinline__ float dist_of_key_bits(uint32_t kb) {
   return __uint_as_float(u);
 }
 
-// The warp compacts the candidate buffer of one of its lanes: T = the k-th
-// smallest distance among b[0..cnt) (cnt >= k, found by bisection on the
-// order-preserving key bits), then the keys within T + margin are kept.
+// The warp compacts the candidate buffer of one of its lanes: a bound T with
+// at least k and at most k + 32 keys of b[0..cnt) at or below it (or the
+// exact k-th smallest, if the key bits allow no such bound) is found by
+// bisection on the order-preserving key bits, then the keys within T + margin
+// are kept.  The buffer (cnt <= 2 * kMaxK + 64) is held in registers, 18 keys
+// per lane.
 __device__ __noinline__ uint32_t warp_compact(uint64_t* b, uint32_t cnt, uint32_t k, float margin, int lane,
                                               float* thr_out) {
+  constexpr int kPer = (2 * static_cast<int>(kMaxK) + 64 + 31) / 32;
+  uint64_t v[kPer];
   uint32_t lo = 0xFFFFFFFFu, hi = 0u;
-  for (uint32_t i = lane; i < cnt; i += 32) {
-    const uint32_t v = static_cast<uint32_t>(b[i] >> 32);
-    lo = min(lo, v);
-    hi = max(hi, v);
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const uint32_t i = static_cast<uint32_t>(j) * 32u + static_cast<uint32_t>(lane);
+    v[j] = i < cnt ? b[i] : ~0ull;
+    if (i < cnt) {
+      const uint32_t kb = static_cast<uint32_t>(v[j] >> 32);
+      lo = min(lo, kb);
+      hi = max(hi, kb);
+    }
   }
   lo = __reduce_min_sync(kFull, lo);
   hi = __reduce_max_sync(kFull, hi);
-  while (lo < hi) {
+  uint32_t chi = cnt;  // keys at or below hi
+  while (lo < hi && chi > k + 32u) {
     const uint32_t mid = lo + ((hi - lo) >> 1);
     uint32_t c = 0;
-    for (uint32_t i = lane; i < cnt; i += 32) c += static_cast<uint32_t>(b[i] >> 32) <= mid ? 1u : 0u;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) c += static_cast<uint32_t>(v[j] >> 32) <= mid ? 1u : 0u;  // padding: ~0 > mid
     c = __reduce_add_sync(kFull, c);
-    if (c >= k) hi = mid;
-    else lo = mid + 1u;
+    if (c >= k) {
+      hi = mid;
+      chi = c;
+    } else {
+      lo = mid + 1u;
+    }
   }
-  const float thr = __fadd_ru(dist_of_key_bits(lo), margin);
+  const float thr = __fadd_ru(dist_of_key_bits(hi), margin);
+  __syncwarp();
   uint32_t w = 0;
-  for (uint32_t base = 0; base < cnt; base += 32) {
-    const uint32_t i = base + lane;
-    const uint64_t v = i < cnt ? b[i] : 0ull;
-    const bool keep = i < cnt && key_dist(v) <= thr;
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const uint32_t i = static_cast<uint32_t>(j) * 32u + static_cast<uint32_t>(lane);
+    const bool keep = i < cnt && key_dist(v[j]) <= thr;
     const uint32_t bal = __ballot_sync(kFull, keep);
-    __syncwarp();
-    if (keep) b[w + __popc(bal & ((1u << lane) - 1u))] = v;
+    if (keep) b[w + __popc(bal & ((1u << lane) - 1u))] = v[j];
     w += __popc(bal);
-    __syncwarp();
   }
+  __syncwarp();
   *thr_out = thr;
   return w;
 }
