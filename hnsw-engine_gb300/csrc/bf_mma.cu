@@ -437,18 +437,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int c = 0; c < 32; ++c)
               if (!((valid >> c) & 1u)) sv[c] = __int_as_float(0x7fffffff);
           }
-          float m16[16];  // the chunk minimum as a 5-level tree
+          float g8[4];  // minima of the four 8-row groups, each a 3-level tree
 #pragma unroll
-          for (int c = 0; c < 16; ++c) m16[c] = fminf(sv[c], sv[c + 16]);
-#pragma unroll
-          for (int w = 8; w > 0; w >>= 1)
-#pragma unroll
-            for (int c = 0; c < w; ++c) m16[c] = fminf(m16[c], m16[c + w]);
-          const float mn = m16[0];
+          for (int g = 0; g < 4; ++g) {
+            const float a0 = fminf(sv[8 * g], sv[8 * g + 4]), a1 = fminf(sv[8 * g + 1], sv[8 * g + 5]);
+            const float a2 = fminf(sv[8 * g + 2], sv[8 * g + 6]), a3 = fminf(sv[8 * g + 3], sv[8 * g + 7]);
+            g8[g] = fminf(fminf(a0, a2), fminf(a1, a3));
+          }
+          const float mn = fminf(fminf(g8[0], g8[1]), fminf(g8[2], g8[3]));
           if (mn <= thr) {  // rare once the threshold has settled
 #pragma unroll
-            for (int c = 0; c < 32; ++c)
-              if (sv[c] <= thr) bufp[cnt++] = (static_cast<uint64_t>(okey(sv[c])) << 32) | (j0 + c);
+            for (int g = 0; g < 4; ++g) {
+              if (g8[g] <= thr) {  // only the groups holding a passing row
+#pragma unroll
+                for (int c = 8 * g; c < 8 * g + 8; ++c)
+                  if (sv[c] <= thr) bufp[cnt++] = (static_cast<uint64_t>(okey(sv[c])) << 32) | (j0 + c);
+              }
+            }
           }
           // room for the next chunk: compact the lanes that are nearly full
           uint32_t need = __ballot_sync(kFull, cnt + 32u > lim);
