@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -154,18 +155,6 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
 
 // tcgen05.ld without its wait: r may be read only after tmem_wait(r).
 __device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32]) {
@@ -851,7 +840,33 @@ bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint32_t kp, uint
 
 uint32_t round_up(uint32_t v, uint32_t m) { return (v + m - 1) / m * m; }
 
+struct Buf {
+  void* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    const cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+    if (e == cudaSuccess) n = std::max<size_t>(bytes, 256);
+    return e;
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+  ~Buf() {
+    if (p) cudaFree(p);
+  }
+};
+
 }  // namespace
+
+// Device buffers of one scan, grown on demand and reused across calls.
+struct Scratch {
+  Buf qp, q16, qc, qm, qq, buf, cnt, pool, pool_n, err;
+};
 
 struct Store {
   __half* x16 = nullptr;
@@ -860,6 +875,8 @@ struct Store {
   DataBound db{};
   CUtensorMap map_x{};
   int sms = 0;
+  std::mutex mu;  // one search() at a time uses `sc`
+  Scratch sc;
 };
 
 bool supported(uint32_t dim, uint32_t k) { return dim >= 1 && dim <= kMaxDim && k >= 1 && k <= kMaxK; }
@@ -927,6 +944,34 @@ void store_free(Store* s) {
   delete s;
 }
 
+// Row splits of the scan (work items = query tiles x splits on a persistent
+// grid of one CTA per SM): from the count that gives two items per SM up to
+// four times it, the one with the shortest critical path, waves x (row tiles
+// per split + a per-item overhead).  The overhead, 64 + 2k row tiles, was
+// fitted to measured 1M-row scans: every item restarts its queries'
+// thresholds, and the select kernel reads every split's candidates.  Fewest
+// splits on ties; the candidate buffers stay within 1 GiB.
+void choose_splits(uint32_t tiles_q, uint32_t nbt, uint32_t sms, uint32_t k, uint64_t bytes_per_split,
+                   uint32_t* splits_out, uint32_t* tps_out) {
+  const uint32_t s0 = std::min<uint32_t>(nbt, std::max<uint32_t>(1, (2u * sms + tiles_q - 1) / tiles_q));
+  uint32_t s_hi = std::min<uint32_t>(nbt, 4u * s0);
+  while (s_hi > s0 && static_cast<uint64_t>(s_hi) * bytes_per_split > (1ull << 30)) --s_hi;
+  const uint64_t overhead = 64u + 2u * static_cast<uint64_t>(k);
+  uint64_t best = ~0ull;
+  for (uint32_t s = s0; s <= s_hi; ++s) {
+    const uint32_t tps = (nbt + s - 1) / s;
+    const uint32_t splits = (nbt + tps - 1) / tps;
+    const uint64_t items = static_cast<uint64_t>(tiles_q) * splits;
+    const uint64_t waves = (items + sms - 1) / sms;
+    const uint64_t t = waves * (tps + overhead);
+    if (t < best) {
+      best = t;
+      *splits_out = splits;
+      *tps_out = tps;
+    }
+  }
+}
+
 cudaError_t search(Store* s, const Rows& r, const float* queries, const float* inv, uint32_t nq, uint32_t k,
                    const uint32_t* allow, void* out, cudaStream_t st, bool* redo, std::string* err) {
   *redo = false;
@@ -934,35 +979,36 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
   const uint32_t nq_pad = round_up(nq, BM);
   const uint32_t tiles_q = nq_pad / BM;
   const uint32_t nbt = s->n_pad / BN;
-  uint32_t splits = 1;
-  if (tiles_q < static_cast<uint32_t>(s->sms))
-    splits = std::min<uint32_t>(nbt, (2u * static_cast<uint32_t>(s->sms) + tiles_q - 1) / tiles_q);
-  const uint32_t tps = (nbt + splits - 1) / splits;
-  splits = (nbt + tps - 1) / tps;
   const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
+  uint32_t splits = 1, tps = nbt;
+  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, static_cast<uint64_t>(nq_pad) * cap * 8, &splits,
+                &tps);
   const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(splits * cap, 32), 32));
   uint32_t p2max = 1;
   while (p2max < pool_cap) p2max <<= 1;
 
-  __half* q16 = nullptr;
-  float *qc = nullptr, *qm = nullptr, *qq = nullptr;
-  uint64_t* buf = nullptr;
-  uint32_t *cnt = nullptr, *pool = nullptr, *pool_n = nullptr, *derr = nullptr;
+  std::lock_guard<std::mutex> lock(s->mu);
+  Scratch& sc = s->sc;
   cudaError_t e = cudaSuccess;
   const char* what = "";
   do {
     what = "alloc";
-    if ((e = cudaMalloc(&q16, static_cast<size_t>(nq_pad) * s->kp * 2)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&qc, nq_pad * 4ull)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&qm, nq_pad * 4ull)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&qq, nq_pad * 4ull)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&buf, static_cast<size_t>(splits) * nq * cap * 8)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&cnt, static_cast<size_t>(splits) * nq * 4)) != cudaSuccess) break;
+    if ((e = sc.q16.ensure(static_cast<size_t>(nq_pad) * s->kp * 2)) != cudaSuccess) break;
+    if ((e = sc.qc.ensure(nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = sc.qm.ensure(nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = sc.qq.ensure(nq_pad * 4ull)) != cudaSuccess) break;
+    if ((e = sc.buf.ensure(static_cast<size_t>(splits) * nq * cap * 8)) != cudaSuccess) break;
+    if ((e = sc.cnt.ensure(static_cast<size_t>(splits) * nq * 4)) != cudaSuccess) break;
+    if ((e = sc.pool.ensure(static_cast<size_t>(nq) * pool_cap * 4)) != cudaSuccess) break;
+    if ((e = sc.pool_n.ensure(nq * 4ull)) != cudaSuccess) break;
+    if ((e = sc.err.ensure(16)) != cudaSuccess) break;
+    __half* q16 = sc.q16.as<__half>();
+    float *qc = sc.qc.as<float>(), *qm = sc.qm.as<float>(), *qq = sc.qq.as<float>();
+    uint64_t* buf = sc.buf.as<uint64_t>();
+    uint32_t *cnt = sc.cnt.as<uint32_t>(), *pool = sc.pool.as<uint32_t>(), *pool_n = sc.pool_n.as<uint32_t>();
+    uint32_t* derr = sc.err.as<uint32_t>();
     // counts of (split, query) pairs an aborted CTA never reached read as 0
     if ((e = cudaMemsetAsync(cnt, 0, static_cast<size_t>(splits) * nq * 4, st)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&pool, static_cast<size_t>(nq) * pool_cap * 4)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&pool_n, nq * 4ull)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&derr, 16)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(derr, 0, 16, st)) != cudaSuccess) break;
     what = "query kernel";
     prep_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(nq_pad) * 32 + 255) / 256), 256, 0, st>>>(
@@ -1026,12 +1072,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     *redo = herr[1] != 0;
   } while (false);
   if (e != cudaSuccess) *err = std::string("tensor brute force: ") + what + ": " + cudaGetErrorString(e);
-  cudaStreamSynchronize(st);
-  for (void* p : {static_cast<void*>(q16), static_cast<void*>(qc), static_cast<void*>(qm), static_cast<void*>(qq),
-                  static_cast<void*>(buf),
-                  static_cast<void*>(cnt), static_cast<void*>(pool), static_cast<void*>(pool_n),
-                  static_cast<void*>(derr)})
-    if (p) cudaFree(p);
+  cudaStreamSynchronize(st);  // the scratch is free for the next call
   return e;
 }
 
@@ -1053,32 +1094,9 @@ __global__ void gather_queries_kernel(const float* __restrict__ raw, const float
   }
 }
 
-struct Buf {
-  void* p = nullptr;
-  size_t n = 0;
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= n) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-    const cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
-    if (e == cudaSuccess) n = std::max<size_t>(bytes, 256);
-    return e;
-  }
-  template <typename T>
-  T* as() const {
-    return static_cast<T*>(p);
-  }
-  ~Buf() {
-    if (p) cudaFree(p);
-  }
-};
 
 }  // namespace
 
-struct Scratch {
-  Buf qp, q16, qc, qm, qq, buf, cnt, pool, pool_n, err;
-};
 
 Scratch* scratch_new() { return new Scratch(); }
 void scratch_free(Scratch* s) { delete s; }
@@ -1091,12 +1109,10 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
   const uint32_t nq_pad = round_up(n_r, BM);
   const uint32_t tiles_q = nq_pad / BM;
   const uint32_t nbt = s->n_pad / BN;
-  uint32_t splits = 1;
-  if (tiles_q < static_cast<uint32_t>(s->sms))
-    splits = std::min<uint32_t>(nbt, (2u * static_cast<uint32_t>(s->sms) + tiles_q - 1) / tiles_q);
-  const uint32_t tps = (nbt + splits - 1) / splits;
-  splits = (nbt + tps - 1) / tps;
   const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
+  uint32_t splits = 1, tps = nbt;
+  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, static_cast<uint64_t>(nq_pad) * cap * 8, &splits,
+                &tps);
   const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(splits * cap, 32), 32));
   uint32_t p2max = 1;
   while (p2max < pool_cap) p2max <<= 1;
