@@ -502,7 +502,7 @@ __device__ __forceinline__ float approx_partial(const SearchParams& P, uint32_t 
 template <int RPP, int E, int PREC>
 struct ApproxDist {
   static constexpr bool kApprox = true;
-  static constexpr int kMinBlocks = 5;  // (128, 6) measured 20% slower on FP8 serving
+  static constexpr int kMinBlocks = 5;  // (128, 6) measured 8% slower on the 1M FP8 walk
   static constexpr int LPR = 32 / RPP;
   // the exact FP32 layout (reference order, runtime block counts) of the same
   // padded-width class: the fused rerank computes the pool's exact distances
