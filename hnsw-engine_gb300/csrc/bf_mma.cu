@@ -625,86 +625,136 @@ __global__ void prep_queries_kernel(const float* __restrict__ raw, const float* 
 }
 
 // ---------------------------------------------------------------------------
-// per query: k-th smallest over the splits, survivors within the margin
+// per query, one CTA: the k-th smallest over the splits by a 4-pass radix
+// select (8-bit digits of the order-preserving key bits), survivors within
+// the margin.  The pool's order does not matter (the rerank sorts it).  The
+// candidates are read 5-7 times by 256 threads; a warp bisecting the key
+// bits read them about 34 times, which dominated scans split many ways
+// (few queries over many rows).
 // ---------------------------------------------------------------------------
-__global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* __restrict__ cnt,
-                              const float* __restrict__ qm, const float* __restrict__ qq, uint32_t nq,
-                              uint32_t splits, uint32_t cap, uint32_t k,
-                              uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t* __restrict__ pool_n,
-                              uint32_t* __restrict__ err, int lenient) {
-  const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (q >= nq) return;
-  uint32_t total = 0;
-  bool over = false;
-  for (uint32_t s = 0; s < splits; ++s) {
-    const uint32_t c = cnt[static_cast<size_t>(s) * nq + q];
-    if (c == kOver) over = true;
-    else total += min(c, cap);
+constexpr int kSelThreads = 256;
+
+__global__ void __launch_bounds__(kSelThreads) select_cta_kernel(
+    const uint64_t* __restrict__ buf, const uint32_t* __restrict__ cnt, const float* __restrict__ qm,
+    const float* __restrict__ qq, uint32_t nq, uint32_t splits, uint32_t cap, uint32_t k,
+    uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t* __restrict__ pool_n, uint32_t* __restrict__ err,
+    int lenient) {
+  __shared__ uint32_t hist[256];
+  __shared__ uint32_t wsum[kSelThreads / 32];
+  __shared__ uint32_t sh_over, sh_total, sh_bucket, sh_before, sh_count, sh_w;
+  const uint32_t q = blockIdx.x;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t == 0) {
+    sh_over = 0u;
+    sh_total = 0u;
+    sh_w = 0u;
   }
-  if (over) {
-    if (lane == 0) {
+  __syncthreads();
+  {
+    uint32_t tot = 0;
+    bool ov = false;
+    for (uint32_t sp = t; sp < splits; sp += kSelThreads) {
+      const uint32_t c = cnt[static_cast<size_t>(sp) * nq + q];
+      if (c == kOver) ov = true;
+      else tot += min(c, cap);
+    }
+    if (ov) atomicOr(&sh_over, 1u);
+    if (tot) atomicAdd(&sh_total, tot);
+  }
+  __syncthreads();
+  if (sh_over) {
+    if (t == 0) {
       pool_n[q] = 0;
       atomicAdd(err + 1, 1u);
     }
     return;
   }
-  auto count_le = [&](uint32_t bound) {
-    uint32_t c = 0;
-    for (uint32_t s = 0; s < splits; ++s) {
-      const uint32_t m = min(cnt[static_cast<size_t>(s) * nq + q], cap);
-      const uint64_t* b = buf + (static_cast<size_t>(s) * nq + q) * cap;
-      for (uint32_t i = lane; i < m; i += 32) c += static_cast<uint32_t>(b[i] >> 32) <= bound ? 1u : 0u;
+  const uint32_t total = sh_total;
+  auto for_each = [&](auto&& f) {
+    for (uint32_t sp = 0; sp < splits; ++sp) {
+      const uint32_t m = min(cnt[static_cast<size_t>(sp) * nq + q], cap);
+      const uint64_t* b = buf + (static_cast<size_t>(sp) * nq + q) * cap;
+      for (uint32_t i = t; i < m; i += kSelThreads) f(b[i]);
     }
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
-    return c;
+  };
+  // block-wide count of keys whose bits are <= kb
+  auto count_le = [&](uint32_t kb) {
+    __syncthreads();
+    if (t == 0) sh_count = 0u;
+    __syncthreads();
+    uint32_t c = 0;
+    for_each([&](uint64_t v) { c += static_cast<uint32_t>(v >> 32) <= kb ? 1u : 0u; });
+    if (c) atomicAdd(&sh_count, c);
+    __syncthreads();
+    return sh_count;
+  };
+  // the r-th smallest (1-based, r <= total) key bits
+  auto radix_select = [&](uint32_t r) {
+    uint32_t prefix = 0u, pmask = 0u;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+      hist[t] = 0u;  // kSelThreads == 256 bins
+      __syncthreads();
+      for_each([&](uint64_t v) {
+        const uint32_t kb = static_cast<uint32_t>(v >> 32);
+        if ((kb & pmask) == prefix) atomicAdd(&hist[(kb >> shift) & 255u], 1u);
+      });
+      __syncthreads();
+      // inclusive scan of the 256 bins: within warps, then across them
+      const uint32_t h = hist[t];
+      uint32_t incl = h;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += u;
+      }
+      if (lane == 31) wsum[warp] = incl;
+      __syncthreads();
+      uint32_t base = 0;
+      for (int w2 = 0; w2 < warp; ++w2) base += wsum[w2];
+      incl += base;
+      const uint32_t excl = incl - h;
+      if (excl < r && r <= incl) {  // exactly one bin
+        sh_bucket = static_cast<uint32_t>(t);
+        sh_before = excl;
+      }
+      __syncthreads();
+      prefix |= sh_bucket << shift;
+      pmask |= 0xFFu << shift;
+      r -= sh_before;
+      __syncthreads();
+    }
+    return prefix;
   };
   float thr = __int_as_float(0x7f800000);
   if (total > k) {
-    uint32_t lo = 0u, hi = 0xFFFFFFFFu;
-    while (lo < hi) {
-      const uint32_t mid = lo + ((hi - lo) >> 1);
-      if (count_le(mid) >= k) hi = mid;
-      else lo = mid + 1u;
-    }
-    const float T = dist_of_key_bits(lo);
+    const float T = dist_of_key_bits(radix_select(k));
     thr = __fadd_ru(T, qm[q]);
     if (lenient && count_le(okey(thr)) > pool_cap) {
       // too many survivors for the pool: keep the pool_cap smallest (approximate)
-      uint32_t lo2 = 0u, hi2 = 0xFFFFFFFFu;
-      while (lo2 < hi2) {
-        const uint32_t mid = lo2 + ((hi2 - lo2) >> 1);
-        if (count_le(mid) >= pool_cap) hi2 = mid;
-        else lo2 = mid + 1u;
-      }
+      const uint32_t lo2 = radix_select(pool_cap);
       thr = dist_of_key_bits(lo2);
       if (count_le(lo2) > pool_cap) thr = nextafterf(thr, -__int_as_float(0x7f800000));  // ties at the edge: drop them
     }
     // exact mode holds while the k-th distance is below 2^24 (where the
     // reference's own sum is still exact); past it the scan answers
     if (!lenient && qq[q] >= 0.0f && static_cast<double>(T) + qq[q] >= 16777216.0) {
-      if (lane == 0) {
+      if (t == 0) {
         pool_n[q] = 0;
         atomicAdd(err + 1, 1u);
       }
       return;
     }
   }
-  uint32_t w = 0;
-  for (uint32_t s = 0; s < splits; ++s) {
-    const uint32_t m = min(cnt[static_cast<size_t>(s) * nq + q], cap);
-    const uint64_t* b = buf + (static_cast<size_t>(s) * nq + q) * cap;
-    for (uint32_t base = 0; base < m; base += 32) {
-      const uint32_t i = base + lane;
-      const uint64_t v = i < m ? b[i] : 0ull;
-      const bool keep = i < m && key_dist(v) <= thr;
-      const uint32_t bal = __ballot_sync(kFull, keep);
-      const uint32_t pos = w + __popc(bal & ((1u << lane) - 1u));
-      if (keep && pos < pool_cap) pool[static_cast<size_t>(q) * pool_cap + pos] = static_cast<uint32_t>(v);
-      w += __popc(bal);
+  __syncthreads();
+  for_each([&](uint64_t v) {
+    if (key_dist(v) <= thr) {
+      const uint32_t pos = atomicAdd(&sh_w, 1u);
+      if (pos < pool_cap) pool[static_cast<size_t>(q) * pool_cap + pos] = static_cast<uint32_t>(v);
     }
-  }
-  if (lane == 0) {
+  });
+  __syncthreads();
+  if (t == 0) {
+    const uint32_t w = sh_w;
     if (w > pool_cap) {
       pool_n[q] = lenient ? pool_cap : 0;
       if (!lenient) atomicAdd(err + 1, 1u);
@@ -713,6 +763,7 @@ __global__ void select_kernel(const uint64_t* __restrict__ buf, const uint32_t* 
     }
   }
 }
+
 
 // ---------------------------------------------------------------------------
 // exact distances of the survivors in the reference order, sorted, first k
@@ -1047,8 +1098,8 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "select kernel";
-    select_kernel<<<(nq * 32 + 255) / 256, 256, 0, st>>>(buf, cnt, qm, qq, nq, splits, cap, k, pool, pool_cap,
-                                                         pool_n, derr, 0);
+    select_cta_kernel<<<nq, kSelThreads, 0, st>>>(buf, cnt, qm, qq, nq, splits, cap, k, pool, pool_cap, pool_n, derr,
+                                                  0);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
     const int S = slots_of(r.dim);
@@ -1175,11 +1226,9 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "select kernel";
-    select_kernel<<<(n_r * 32 + 255) / 256, 256, 0, st>>>(sc->buf.as<uint64_t>(), sc->cnt.as<uint32_t>(),
-                                                          sc->qm.as<float>(), sc->qq.as<float>(), n_r, splits, cap, k,
-                                                          sc->pool.as<uint32_t>(), pool_cap, sc->pool_n.as<uint32_t>(),
-                                                          sc->err.as<uint32_t>(), 1);
-    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    select_cta_kernel<<<n_r, kSelThreads, 0, st>>>(sc->buf.as<uint64_t>(), sc->cnt.as<uint32_t>(), sc->qm.as<float>(),
+                                                   sc->qq.as<float>(), n_r, splits, cap, k, sc->pool.as<uint32_t>(),
+                                                   pool_cap, sc->pool_n.as<uint32_t>(), sc->err.as<uint32_t>(), 1);    if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
     const int S = slots_of(r.dim);
     const dim3 rgrid((n_r + 3) / 4);
