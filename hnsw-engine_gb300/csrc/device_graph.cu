@@ -33,6 +33,8 @@ cudaError_t launch_search(const SearchParams& P, const float* inv, int blocks, i
 int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, uint32_t R, uint32_t C);
 cudaError_t launch_search_approx(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st);
 int occupancy_approx(uint32_t pdc, int metric, int prec, int wpb, size_t smem);
+cudaError_t launch_search_wide(const SearchParams& P, const float* inv, int blocks, cudaStream_t st);
+int occupancy_wide(int metric, int prec, uint32_t R);
 cudaError_t launch_encode(const float* vecs, uint32_t n, uint32_t pd, uint32_t pdc, int prec, void* out,
                           float* scale, cudaStream_t st);
 cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, uint32_t ef_all, uint32_t ef_default,
@@ -905,7 +907,25 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
       return fail(HGD_ECUDA, err);
     HG_CUDA(cudaEventRecord(w->scan_join, w->scan_stream));
   }
-  if (single) {
+  // several warps per query (compressed rows of 128 elements): one CTA per
+  // query, every bucket largest ef first; overflows go to the rerun pass
+  const bool wide = a->warps_per_query >= 4 && prec != HGD_PREC_FP32 && P.pdc == 128 && g->n > 0 &&
+                    g->n < (1ull << 24) && P.M0 <= 32 && a->counters == nullptr;
+  if (wide) {
+    hg::SearchParams B = P;
+    B.R = round_up(ef_max, 32);
+    B.qidx = w->lists.as<uint32_t>();
+    B.lpt_sizes = work + 32;
+    B.lpt_buckets = spec.n;
+    B.lpt_stride = static_cast<uint32_t>(nq);
+    B.work = work + 8;
+    B.slot_base = 0;
+    const int occ = hg::occupancy_wide(g->metric, prec, B.R);
+    if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the several-warps kernel cannot be resident");
+    const int blocks = static_cast<int>(std::min<uint64_t>(nq, static_cast<uint64_t>(g->sms) * occ));
+    cudaError_t e = hg::launch_search_wide(B, d_inv, blocks, st);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("search kernel launch: ") + cudaGetErrorString(e));
+  } else if (single) {
     // one persistent launch, the largest bucket's shape, every query
     const Shape& sh = shapes.back();
     hg::SearchParams B = P;

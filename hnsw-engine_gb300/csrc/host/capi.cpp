@@ -186,6 +186,7 @@ int hg_index_search_batch_ex(const hg_index* idx, const float* qs, size_t nq, si
       opt.use_graph = o->use_graph != 0;
       opt.filter_scan_permille = o->filter_scan_permille;
       opt.rerank_factor = o->rerank_factor;
+      opt.warps_per_query = o->warps_per_query;
     }
     idx->index.search_batch_ex(qs, nq, k, ef, reinterpret_cast<hnsw::Neighbor*>(out), opt);
   });

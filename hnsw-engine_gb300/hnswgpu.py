@@ -40,12 +40,14 @@ class _BatchOptions(C.Structure):
                 ("precision", C.c_int32), ("use_graph", C.c_int32), ("counters", C.c_void_p),
                 ("hash_slots", C.c_uint32), ("cand_cap", C.c_uint32), ("warps_per_block", C.c_uint32),
                 ("pool_cap", C.c_uint32), ("queries_on_device", C.c_int32), ("out_on_device", C.c_int32),
-                ("filter_scan_permille", C.c_uint32), ("rerank_factor", C.c_uint32)]
+                ("filter_scan_permille", C.c_uint32), ("rerank_factor", C.c_uint32),
+                ("warps_per_query", C.c_uint32), ("reserved3", C.c_uint32)]
 
 
 class _ServerConfig(C.Structure):
     _fields_ = [("max_inflight", C.c_uint32), ("max_batch_queries", C.c_uint32), ("memory_budget", C.c_uint64),
-                ("precision", C.c_int32), ("filter_scan_permille", C.c_uint32), ("rerank_factor", C.c_uint32)]
+                ("precision", C.c_int32), ("filter_scan_permille", C.c_uint32), ("rerank_factor", C.c_uint32),
+                ("warps_per_query", C.c_uint32)]
 
 
 class _Request(C.Structure):
@@ -325,12 +327,15 @@ class Index:
     def search_batch_ex(self, queries, k: int, ef: int = 0, ef_per_query=None, k_per_query=None, filters=None,
                         filter_of_query=None, stream=None, precision: int = 0, counters: bool = False,
                         hash_slots: int = 0, cand_cap: int = 0, warps_per_block: int = 0, pool_cap: int = 0,
-                        out=None, filter_scan: float = 0.0, rerank_factor: int = 0):
+                        out=None, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1):
         """search_batch with per-query ef / k / filter.  filter_scan (FP16 / FP8
         only): queries whose filter allows at most this fraction of the nodes
         are answered by the exact tensor-core scan instead of a graph walk.
         rerank_factor (FP16 / FP8 only): the exact FP32 rerank covers the best
-        rerank_factor x k entries of the traversal pool (at least 32); 0 = all."""
+        rerank_factor x k entries of the traversal pool (at least 32); 0 = all.
+        warps_per_query=4 (FP16 / FP8, dim <= 128): four warps walk each query
+        as a beam search (lower latency per query; not the reference's visit
+        order, so recall is the bar)."""
         q, _ = self._queries(queries)
         nq = q.shape[0]
         if out is None:
@@ -340,6 +345,7 @@ class Index:
         opt = _BatchOptions()
         opt.filter_scan_permille = int(round(filter_scan * 1000))
         opt.rerank_factor = int(rerank_factor)
+        opt.warps_per_query = int(warps_per_query)
         keep = []
         if ef_per_query is not None:
             a = np.ascontiguousarray(ef_per_query, dtype=np.uint32)
@@ -558,11 +564,11 @@ class Server:
     own k / ef / filter are admitted into GPU batches as slots and memory free up."""
 
     def __init__(self, index: Index, max_inflight: int = 4, max_batch_queries: int = 4096, memory_budget: int = 0,
-                 precision: int = 0, filter_scan: float = 0.0, rerank_factor: int = 0):
+                 precision: int = 0, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1):
         self._h = None
         self._index = index  # keep the index alive
         cfg = _ServerConfig(max_inflight, max_batch_queries, memory_budget, precision,
-                            int(round(filter_scan * 1000)), int(rerank_factor))
+                            int(round(filter_scan * 1000)), int(rerank_factor), int(warps_per_query))
         h = C.c_void_p()
         _check(lib().hg_server_create(index._h, C.byref(cfg), C.byref(h)))
         self._h = h

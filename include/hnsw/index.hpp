@@ -60,6 +60,9 @@ struct SearchOptions {
   /// FP16 / FP8 batches: the exact FP32 rerank covers the best
   /// rerank_factor x k entries of the traversal pool (at least 32); 0 = all
   uint32_t rerank_factor = 0;
+  /// FP16 / FP8 batches with dim <= 128: 4 = four warps walk each query (a
+  /// beam search: lower latency, not the reference's visit order); 1 = one
+  uint32_t warps_per_query = 1;
 };
 
 class Index {

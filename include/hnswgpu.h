@@ -91,6 +91,9 @@ typedef struct {
                                       tensor-core scan over the allowed rows (0: off) */
   uint32_t rerank_factor;          /* precision 1 / 2: exact rerank of the best rerank_factor x k
                                       pool entries (at least 32); 0 = the whole pool */
+  uint32_t warps_per_query;        /* precision 1 / 2, dim <= 128: 4 = four warps walk each query
+                                      (beam search, lower latency); 0 / 1 = one warp */
+  uint32_t reserved3;
 } hg_batch_options;
 
 const char* hg_last_error(void);
@@ -185,6 +188,8 @@ typedef struct {
                                     per mille of the nodes take the exact tensor-core scan (0: off) */
   uint32_t rerank_factor;        /* precision 1 / 2: exact rerank of the best rerank_factor x k pool
                                     entries (at least 32); 0 = the whole pool */
+  uint32_t warps_per_query;      /* precision 1 / 2, dim <= 128: 4 = four warps walk each query
+                                    (beam search, lower latency); 0 / 1 = one warp */
 } hg_server_config;
 typedef struct {
   const float* queries;        /* nq x dim */

@@ -121,6 +121,12 @@ typedef struct {
    * entries of the traversal pool (at least 32); 0 = the whole pool (ef
    * entries).  No counterpart in the reference. */
   uint32_t rerank_factor;
+  /* FP16 / FP8 with dim <= 128: 4 = one CTA of four warps walks each query, a
+   * beam search expanding four candidates per step (lower latency per query;
+   * its visit order is not the reference's, recall is the bar); 0 or 1 = one
+   * warp per query, the reference's order.  No counterpart in the reference. */
+  uint32_t warps_per_query;
+  uint32_t reserved4;
 } hgd_search_args;
 
 int hgd_graph_upload(const hgd_graph_view* view, int device, int order, hgd_graph** out);

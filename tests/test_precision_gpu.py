@@ -14,9 +14,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _check(hg, oracle, ix, base, q, k, ef, prec, metric, min_overlap, rerank_factor=0):
+def _check(hg, oracle, ix, base, q, k, ef, prec, metric, min_overlap, rerank_factor=0, **kw):
     exact = ix.search_raw(q, k, ef)
-    rec = ix.search_batch_ex(q, k, ef, precision=prec, rerank_factor=rerank_factor)
+    rec = ix.search_batch_ex(q, k, ef, precision=prec, rerank_factor=rerank_factor, **kw)
     labels = rec["label"].astype(np.int64)
     assert (labels >= 0).all()
     for i in range(q.shape[0]):
