@@ -197,20 +197,31 @@ __global__ void __launch_bounds__(32 * kWW) wide_kernel(SearchParams P, const fl
       }
       stage[warp * 32 + lane] = key;
       __syncthreads();
-      // merge (warp 0): each expanded list's new keys, sorted, into the beam (capacity ef)
+      // merge (warp 0): the new keys of all expanded lists are packed to the
+      // front of the stage, then sorted and merged into the beam (capacity
+      // ef) 32 at a time; a step usually brings fewer than 32
       if (warp == 0) {
         uint32_t len = ctl[kCtlLen];
+        const uint64_t worst = len >= ef ? beam[ef - 1] : kMaxKey;
+        uint32_t total = 0;
         for (uint32_t w2 = 0; w2 < nsel; ++w2) {
-          uint64_t v = stage[w2 * 32 + lane];
-          if (len >= ef && v > beam[ef - 1]) v = kMaxKey;  // no better than the worst kept
-          const int m = __popc(__ballot_sync(kFull, v != kMaxKey));
-          if (m == 0) continue;
+          const uint64_t v = stage[w2 * 32 + lane];
+          const bool keep = v != kMaxKey && v < worst;  // no better than the worst kept: dropped
+          const uint32_t b = __ballot_sync(kFull, keep);
+          __syncwarp();
+          if (keep) stage[total + __popc(b & ((1u << lane) - 1u))] = v;  // never past what was read
+          total += __popc(b);
+          __syncwarp();
+        }
+        for (uint32_t base = 0; base < total; base += 32) {
+          const int m = static_cast<int>(min(32u, total - base));
+          uint64_t v = lane < m ? stage[base + lane] : kMaxKey;
           v = warp_sort32(v, lane);
           __syncwarp();
-          stage[w2 * 32 + lane] = v;
+          stage[base + lane] = v;  // base + 32 <= 32 * kWW
           __syncwarp();
           len = static_cast<uint32_t>(warp_merge(beam, static_cast<int>(len), static_cast<int>(ef),
-                                                 stage + w2 * 32, m, lane));
+                                                 stage + base, m, lane));
         }
         if (lane == 0) {
           ctl[kCtlLen] = len;
