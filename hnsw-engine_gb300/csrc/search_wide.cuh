@@ -26,8 +26,9 @@ constexpr uint32_t kWideHashLimit = kWideHash / 8 * 5;  // inserts before the qu
 constexpr uint32_t kWideSteps = 1u << 16;               // bound of the layer-0 loop
 
 // control words after the stage: item, selected count, beam length, visited
-// count, overflow, then the selected ids
-enum : int { kCtlItem = 0, kCtlNsel = 1, kCtlLen = 2, kCtlVisits = 3, kCtlOvf = 4, kCtlSel = 8, kCtlWords = 16 };
+// count, overflow, the scan hint (every beam entry before it is expanded),
+// then the selected ids
+enum : int { kCtlItem = 0, kCtlNsel = 1, kCtlLen = 2, kCtlVisits = 3, kCtlOvf = 4, kCtlHint = 5, kCtlSel = 8, kCtlWords = 16 };
 
 __host__ __device__ inline uint32_t wide_smem_bytes(uint32_t R) {
   return 4u * kWideHash + 8u * R + 8u * 32u * kWW + 4u * kCtlWords;
@@ -146,6 +147,7 @@ __global__ void __launch_bounds__(32 * kWW) wide_kernel(SearchParams P, const fl
         ctl[kCtlLen] = 1u;
         ctl[kCtlVisits] = 1u;
         ctl[kCtlOvf] = 0u;
+        ctl[kCtlHint] = 0u;
         uint32_t dummy = 0;
         wide_visit(hash, cur, tag, &dummy);
       }
@@ -156,8 +158,8 @@ __global__ void __launch_bounds__(32 * kWW) wide_kernel(SearchParams P, const fl
     for (uint32_t step = 0;; ++step) {
       if (warp == 0) {  // the best kWW entries not yet expanded, marked as expanded
         const uint32_t len = ctl[kCtlLen];
-        uint32_t nsel = 0;
-        for (uint32_t base = 0; base < len && nsel < kWW; base += 32) {
+        uint32_t nsel = 0, next = ctl[kCtlHint];
+        for (uint32_t base = next & ~31u; base < len && nsel < kWW; base += 32) {
           const uint32_t i = base + lane;
           const uint64_t v = i < len ? beam[i] : 1ull;
           uint32_t b = __ballot_sync(kFull, i < len && !(v & 1ull));
@@ -168,10 +170,15 @@ __global__ void __launch_bounds__(32 * kWW) wide_kernel(SearchParams P, const fl
               beam[i] = v | 1ull;
               ctl[kCtlSel + nsel] = wkey_id(v);
             }
+            next = base + static_cast<uint32_t>(l) + 1u;  // entries before it are all expanded now
             ++nsel;
           }
         }
-        if (lane == 0) ctl[kCtlNsel] = (ctl[kCtlOvf] || step >= kWideSteps) ? 0u : nsel;
+        __syncwarp();
+        if (lane == 0) {
+          ctl[kCtlNsel] = (ctl[kCtlOvf] || step >= kWideSteps) ? 0u : nsel;
+          ctl[kCtlHint] = next;
+        }
       }
       __syncthreads();
       const uint32_t nsel = ctl[kCtlNsel];
@@ -213,6 +220,7 @@ __global__ void __launch_bounds__(32 * kWW) wide_kernel(SearchParams P, const fl
           total += __popc(b);
           __syncwarp();
         }
+        uint32_t hint = ctl[kCtlHint];
         for (uint32_t base = 0; base < total; base += 32) {
           const int m = static_cast<int>(min(32u, total - base));
           uint64_t v = lane < m ? stage[base + lane] : kMaxKey;
@@ -220,9 +228,12 @@ __global__ void __launch_bounds__(32 * kWW) wide_kernel(SearchParams P, const fl
           __syncwarp();
           stage[base + lane] = v;  // base + 32 <= 32 * kWW
           __syncwarp();
+          // the smallest new key lands at its rank: the hint may not pass it
+          hint = min(hint, static_cast<uint32_t>(lower_bound(beam, static_cast<int>(len), stage[base])));
           len = static_cast<uint32_t>(warp_merge(beam, static_cast<int>(len), static_cast<int>(ef),
                                                  stage + base, m, lane));
         }
+        if (lane == 0) ctl[kCtlHint] = hint;
         if (lane == 0) {
           ctl[kCtlLen] = len;
           if (ctl[kCtlVisits] > kWideHashLimit) ctl[kCtlOvf] = 1u;
