@@ -996,15 +996,16 @@ void store_free(Store* s) {
 }
 
 // Row splits of the scan (work items = query tiles x splits on a persistent
-// grid of one CTA per SM): from the count that gives two items per SM up to
+// grid of one CTA per SM): from the count that gives one item per SM up to
 // four times it, the one with the shortest critical path, waves x (row tiles
-// per split + a per-item overhead).  The overhead, 64 + 2k row tiles, was
+// per split + a per-item overhead).  Every split adds its own candidates to
+// the select step, so a batch of few queries takes one wave, not two.  The overhead, 64 + 2k row tiles, was
 // fitted to measured 1M-row scans: every item restarts its queries'
 // thresholds, and the select kernel reads every split's candidates.  Fewest
 // splits on ties; the candidate buffers stay within 1 GiB.
 void choose_splits(uint32_t tiles_q, uint32_t nbt, uint32_t sms, uint32_t k, uint64_t bytes_per_split,
                    uint32_t* splits_out, uint32_t* tps_out) {
-  const uint32_t s0 = std::min<uint32_t>(nbt, std::max<uint32_t>(1, (2u * sms + tiles_q - 1) / tiles_q));
+  const uint32_t s0 = std::min<uint32_t>(nbt, std::max<uint32_t>(1, (sms + tiles_q - 1) / tiles_q));
   uint32_t s_hi = std::min<uint32_t>(nbt, 4u * s0);
   while (s_hi > s0 && static_cast<uint64_t>(s_hi) * bytes_per_split > (1ull << 30)) --s_hi;
   const uint64_t overhead = 64u + 2u * static_cast<uint64_t>(k);
