@@ -1,7 +1,8 @@
-// search_approx.cu -- the query kernel on compressed rows (FP16 or per-row
+// search_approx.cu -- the query kernels on compressed rows (FP16 or per-row
 // scaled FP8 E4M3, FP32 accumulation) for padded row lengths 128 / 256 /
-// 512 / 1024, both metric families.  The exact FP32 rerank lives in
-// rerank.cu.
+// 512 / 1024, both metric families: one warp per query, and (rows of 128)
+// four warps per query.  Both end with the fused exact FP32 rerank; the row
+// encoders live in rerank.cu.
 #include "search_kernel.cuh"
 #include "search_wide.cuh"
 
