@@ -1,7 +1,7 @@
 """Several warps per query (warps_per_query=4) for the compressed forms.
 
 Layer 0 is a beam search expanding four candidates per step, so the visit
-order is not the reference's and results are judged by recall: every
+order is not the reference's and results are held to a recall bar: every
 returned distance must still be the exact FP32 distance of that id
 (bitwise), rows sorted by (distance, label), and the overlap with the exact
 path close to the one-warp compressed form's.
