@@ -38,9 +38,9 @@ sys.path.insert(0, str(REPO / "oracle"))
 N_BASE, DIM, CLUSTERS, NQ, K = 200_000, 128, 256, 10_000, 10
 EF_CHOICES = (10, 20, 40, 80, 160, 320)
 # DRAM bytes of one search launch over this batch, read from an ncu capture
-# (1.668 GB read + 0.421 GB written): below the algorithmic bytes, since part
+# (1.704 GB read + 0.432 GB written): below the algorithmic bytes, since part
 # of the graph is served from L2
-SEARCH_DRAM_BYTES = 2_089_243_000
+SEARCH_DRAM_BYTES = 2_136_463_000
 M, EFC = 16, 200
 METRIC = "QPS at recall@10≥0.95 (served/batched vs plain GPU, same GB300); p50/p99 ms"
 WORKLOAD = "batched-L2-200k: n=200000 d=128 M=16 efC=200, 10000 queries/step, per-query ef U{10..320}, k=10"
