@@ -561,7 +561,13 @@ class BruteForceIndex:
 
 class Server:
     """Continuous-batching server over an Index (hg_server_*): requests with their
-    own k / ef / filter are admitted into GPU batches as slots and memory free up."""
+    own k / ef / filter are admitted into GPU batches as slots and memory free up.
+
+    precision 1 / 2 serves with FP16 / FP8 traversal and an exact FP32 rerank;
+    with those, filter_scan answers requests whose filter allows at most that
+    fraction of the nodes by the exact tensor-core scan, rerank_factor limits
+    the rerank to the pool's best rerank_factor x k, and warps_per_query=4
+    walks each query with four warps (beam search: lower latency)."""
 
     def __init__(self, index: Index, max_inflight: int = 4, max_batch_queries: int = 4096, memory_budget: int = 0,
                  precision: int = 0, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1):
