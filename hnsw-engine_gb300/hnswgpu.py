@@ -146,6 +146,20 @@ def simd_isa() -> str:
     return distance_order()
 
 
+def _rerank_factor(v) -> int:
+    v = int(v)
+    if v < 0:
+        raise ValueError("rerank_factor must be >= 0 (0 reranks the whole pool)")
+    return v
+
+
+def _warps_per_query(v) -> int:
+    v = int(v)
+    if v not in (0, 1, 4):
+        raise ValueError("warps_per_query must be 1 (one warp, the reference's order) or 4 (beam search)")
+    return v
+
+
 def _float_matrix(x, name: str) -> np.ndarray:
     """float32, C-contiguous; non-numeric input is a TypeError (as in the reference's binding)."""
     arr = np.asarray(x)
@@ -344,8 +358,8 @@ class Index:
             raise ValueError("out: expected a contiguous NEIGHBOR array of nq*k records")
         opt = _BatchOptions()
         opt.filter_scan_permille = int(round(filter_scan * 1000))
-        opt.rerank_factor = int(rerank_factor)
-        opt.warps_per_query = int(warps_per_query)
+        opt.rerank_factor = _rerank_factor(rerank_factor)
+        opt.warps_per_query = _warps_per_query(warps_per_query)
         keep = []
         if ef_per_query is not None:
             a = np.ascontiguousarray(ef_per_query, dtype=np.uint32)
@@ -574,7 +588,8 @@ class Server:
         self._h = None
         self._index = index  # keep the index alive
         cfg = _ServerConfig(max_inflight, max_batch_queries, memory_budget, precision,
-                            int(round(filter_scan * 1000)), int(rerank_factor), int(warps_per_query))
+                            int(round(filter_scan * 1000)), _rerank_factor(rerank_factor),
+                            _warps_per_query(warps_per_query))
         h = C.c_void_p()
         _check(lib().hg_server_create(index._h, C.byref(cfg), C.byref(h)))
         self._h = h

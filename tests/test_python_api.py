@@ -71,6 +71,12 @@ def test_argument_errors(hg):
         ix.search(np.array(["a", "b"]))
     with pytest.raises(ValueError):
         ix.add(np.zeros((4, 7), np.float32))
+    with pytest.raises(ValueError, match="warps_per_query"):
+        ix.search_batch_ex(np.zeros((1, 8), np.float32), 1, precision=2, warps_per_query=2)
+    with pytest.raises(ValueError, match="rerank_factor"):
+        ix.search_batch_ex(np.zeros((1, 8), np.float32), 1, precision=2, rerank_factor=-1)
+    with pytest.raises(ValueError, match="warps_per_query"):
+        hg.Server(ix, precision=2, warps_per_query=8)
     for bad in (dict(dim=0), dict(dim=8, metric="hamming"), dict(dim=8, M=1)):
         with pytest.raises(ValueError):
             hg.Index(**bad)
