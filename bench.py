@@ -41,6 +41,7 @@ EF_CHOICES = (10, 20, 40, 80, 160, 320)
 # (1.704 GB read + 0.432 GB written): below the algorithmic bytes, since part
 # of the graph is served from L2
 SEARCH_DRAM_BYTES = 2_136_463_000
+SEARCH_L2_HIT_RATE = 0.509  # lts__t_sector_hit_rate of the same capture
 M, EFC = 16, 200
 METRIC = "QPS at recall@10≥0.95 (served/batched vs plain GPU, same GB300); p50/p99 ms"
 WORKLOAD = "batched-L2-200k: n=200000 d=128 M=16 efC=200, 10000 queries/step, per-query ef U{10..320}, k=10"
@@ -316,6 +317,7 @@ def run_ours(args, rank, world, local):
                      "frac": round(achieved / peak, 4), "traffic": SEARCH_DRAM_BYTES,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this workload's "
                                        "search launch (one batch, cold L2)",
+                     "l2_hit_rate": SEARCH_L2_HIT_RATE,
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(alg_bytes)},
         "clocks": clocks.summary(),
         "wall_s": round(wall, 3),
