@@ -36,7 +36,10 @@ int occupancy_approx(uint32_t pdc, int metric, int prec, int wpb, size_t smem);
 cudaError_t launch_search_wide(const SearchParams& P, const float* inv, int blocks, cudaStream_t st);
 int occupancy_wide(int metric, int prec, uint32_t R);
 cudaError_t launch_encode(const float* vecs, uint32_t n, uint32_t pd, uint32_t pdc, int prec, void* out,
-                          float* scale, cudaStream_t st);
+                          float* scale, float* aux, cudaStream_t st);
+cudaError_t launch_search_beam(const SearchParams& P, const float* inv, int blocks, int wpb, bool filt,
+                               cudaStream_t st);
+int occupancy_beam(int metric, int prec, int wpb, size_t smem, bool filt);
 cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, uint32_t ef_all, uint32_t ef_default,
                           uint32_t k_all, const BucketSpec& spec, uint32_t* counts, uint32_t* lists, cudaStream_t st,
                           const uint8_t* skip);
@@ -196,7 +199,7 @@ struct hgd_graph {
   DBuf vecs, l0, up, up_blk, labels, alive;
   std::vector<uint32_t> alive_host;
   // compressed copies for FP16 / FP8 traversal (built on first use)
-  DBuf v16, v8, vscale;
+  DBuf v16, v8, vscale, vaux16, vaux8;
   bool has16 = false, has8 = false;
   // batch scratch
   std::mutex ws_mu;
@@ -432,7 +435,8 @@ void hgd_graph_free(hgd_graph* g) {
   }
   g->ws.clear();
   hg::bfm::store_free(g->scan);
-  for (DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->v16, &g->v8, &g->vscale})
+  for (DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->v16, &g->v8, &g->vscale,
+                  &g->vaux16, &g->vaux8})
     d->release();
   g->pin_patch.release();
   if (g->stream) cudaStreamDestroy(g->stream);
@@ -442,7 +446,8 @@ void hgd_graph_free(hgd_graph* g) {
 uint64_t hgd_graph_device_bytes(const hgd_graph* g) {
   if (!g) return 0;
   uint64_t t = 0;
-  for (const DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->v16, &g->v8, &g->vscale})
+  for (const DBuf* d : {&g->vecs, &g->l0, &g->up, &g->up_blk, &g->labels, &g->alive, &g->v16, &g->v8, &g->vscale,
+                  &g->vaux16, &g->vaux8})
     t += d->bytes;
   for (const auto& w : g->ws) t += w->bytes();
   return t;
@@ -706,17 +711,21 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     const uint32_t pdc = g->dim <= 128 ? 128u : (g->dim <= 256 ? 256u : (g->dim <= 512 ? 512u : 1024u));
     if (g->dim > 1024) return fail(HGD_EINVAL, "hgd_search: FP16/FP8 traversal supports dim <= 1024");
     DBuf& vb = prec == HGD_PREC_FP16 ? g->v16 : g->v8;
+    DBuf& va = prec == HGD_PREC_FP16 ? g->vaux16 : g->vaux8;
     bool& have = prec == HGD_PREC_FP16 ? g->has16 : g->has8;
     std::lock_guard<std::mutex> build_lock(g->mu);
     if (!have) {
       HG_CUDA(vb.ensure(g->n * pdc * (prec == HGD_PREC_FP16 ? 2 : 1)));
+      HG_CUDA(va.ensure(g->n * 8));
       if (prec == HGD_PREC_FP8) HG_CUDA(g->vscale.ensure(g->n * 4));
       HG_CUDA(hg::launch_encode(g->vecs.as<float>(), static_cast<uint32_t>(g->n), static_cast<uint32_t>(g->pd), pdc,
-                                prec, vb.p, prec == HGD_PREC_FP8 ? g->vscale.as<float>() : nullptr, st));
+                                prec, vb.p, prec == HGD_PREC_FP8 ? g->vscale.as<float>() : nullptr, va.as<float>(),
+                                st));
       have = true;
     }
     P.vq = vb.p;
     P.vscale = prec == HGD_PREC_FP8 ? g->vscale.as<float>() : nullptr;
+    P.vaux = va.as<float>();
     P.pdc = pdc;
     P.pool_stride = round_up(ef_max, 32);
     HG_CUDA(w->pool_ids.ensure(nq * P.pool_stride * 4));
@@ -911,7 +920,35 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   // query, every bucket largest ef first; overflows go to the rerun pass
   const bool wide = a->warps_per_query >= 4 && prec != HGD_PREC_FP32 && P.pdc == 128 && g->n > 0 &&
                     g->n < (1ull << 24) && P.M0 <= 32 && a->counters == nullptr;
-  if (wide) {
+  // one warp per query, a beam search over several lists per step with
+  // tensor-core distances (compressed rows of 128 elements)
+  const bool beamwalk = !wide && a->lists_per_step >= 1 && prec != HGD_PREC_FP32 && P.pdc == 128 && g->n > 0 &&
+                        g->n < (1ull << 24) && P.M0 <= 32;
+  if (beamwalk) {
+    hg::SearchParams B = P;
+    B.R = round_up(ef_max, 32);
+    // visited hash slots: each query uses the size its own ef calls for
+    // (beam_hash_slots); the launch reserves the largest
+    B.H = hg::beam_hash_slots(ef_max);
+    B.lists_per_step = std::min<uint32_t>(a->lists_per_step, hg::kBeamMaxE);
+    B.qidx = w->lists.as<uint32_t>();
+    B.lpt_sizes = work + 32;
+    B.lpt_buckets = spec.n;
+    B.lpt_stride = static_cast<uint32_t>(nq);
+    B.work = work + 8;
+    B.slot_base = 0;
+    // filters or deletes: the variant that keeps a separate result list
+    const bool filt = a->num_filters > 0 || g->num_deleted > 0;
+    const int wpb = 4;
+    const size_t smem = static_cast<size_t>(wpb) * hg::beam_warp_bytes(B.H, B.R, filt);
+    if (smem > 227u * 1024u) return fail(HGD_EINVAL, "hgd_search: ef too large for the beam walk's shared memory");
+    const int occ = hg::occupancy_beam(g->metric, prec, wpb, smem, filt);
+    if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the beam kernel cannot be resident");
+    const uint64_t want = (nq + wpb - 1) / wpb;
+    const int blocks = static_cast<int>(std::min<uint64_t>(want, static_cast<uint64_t>(g->sms) * occ));
+    cudaError_t e = hg::launch_search_beam(B, d_inv, blocks, wpb, filt, st);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("beam kernel launch: ") + cudaGetErrorString(e));
+  } else if (wide) {
     hg::SearchParams B = P;
     B.R = round_up(ef_max, 32);
     B.qidx = w->lists.as<uint32_t>();

@@ -102,6 +102,7 @@ class Server {
     filter_scan_permille_ = cfg.filter_scan_permille;
     rerank_factor_ = cfg.rerank_factor;
     warps_per_query_ = cfg.warps_per_query;
+    lists_per_step_ = cfg.lists_per_step;
     {
       std::shared_lock<std::shared_mutex> lk(im.api_mutex);
       g_ = im.device_graph();
@@ -337,6 +338,7 @@ class Server {
       a.filter_scan_permille = filter_scan_permille_;
       a.rerank_factor = rerank_factor_;
       a.warps_per_query = warps_per_query_;
+      a.lists_per_step = lists_per_step_;
       a.stream = s.stream;
       a.synchronize = 0;
       rc = hgd_search(g_, &a);
@@ -442,6 +444,7 @@ class Server {
   uint32_t filter_scan_permille_ = 0;
   uint32_t rerank_factor_ = 0;
   uint32_t warps_per_query_ = 1;
+  uint32_t lists_per_step_ = 0;
   uint64_t budget_ = 0, inflight_bytes_ = 0;
   std::mutex mu_;
   std::condition_variable cv_, cv_done_;

@@ -71,6 +71,8 @@ struct SearchParams {
   // ---- compressed traversal (FP16 / FP8-E4M3 rows) ----
   const void* vq;           // n x pdc compressed rows (halves or e4m3 bytes), zero padded
   const float* vscale;      // FP8: per-row scale (row = scale x e4m3 values)
+  const float* vaux;        // per row {scale (1 for FP16), scale^2 |stored row|^2}
+  uint32_t lists_per_step;  // beam walk: neighbour lists expanded per step (1..4)
   uint32_t pdc;             // compressed row length (dim rounded up to 128)
   uint32_t* pool_out;       // nq x pool_stride: final traversal pool (ids, sorted by traversal distance)
   uint32_t pool_stride;
@@ -89,6 +91,24 @@ struct BucketSpec {
   uint32_t n;
   uint32_t hi[kMaxBuckets];
 };
+
+// The beam walk (search_beam.cuh): lists per step at most, and its per-warp
+// shared layout: hash[H] | beam A, B [R each] | (filtered) results A, B
+// [R each] | stage, eligible stage [32 E each] | fresh ids [32 E] | fresh
+// distances [32 E] (also the query staging area: 128 floats).
+constexpr int kBeamMaxE = 4;
+__host__ __device__ inline uint32_t beam_warp_bytes(uint32_t H, uint32_t R, bool filt) {
+  return 4u * H + 16u * R + (filt ? 16u * R : 0u) + 2u * 8u * 32u * kBeamMaxE + 8u * 32u * kBeamMaxE;
+}
+// A query's visited-hash size in the beam walk: the smallest power of two
+// >= 1024 whose 5/8 load holds twice its beam and a step's lists.  A
+// function of ef alone, so a query walks the same way in any batch.
+__host__ __device__ inline uint32_t beam_hash_slots(uint32_t ef) {
+  const uint32_t r = (ef + 31u) / 32u * 32u;
+  uint32_t H = 1024;
+  while (H / 8u * 5u < 2u * (r + 128u)) H <<= 1;
+  return H;
+}
 
 __host__ __device__ inline uint32_t warp_smem_bytes(uint32_t H, uint32_t R, uint32_t C) {
   // hash + results + candidates (+32 slack) + two 32-entry staging arrays +

@@ -40,6 +40,7 @@
 
 #include <cstdint>
 
+#include "compressed_layout.cuh"
 #include "search_common.cuh"
 #include "smem_limit.cuh"
 
@@ -517,7 +518,8 @@ struct ApproxDist {
     const int base = (lane % LPR) * E;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const int idx = base + e;
+      // the copy stores rows in the tensor-core order (compressed_layout.cuh)
+      const int idx = static_cast<int>(cl_logical(static_cast<uint32_t>(base + e), PREC));
       const float v = idx < static_cast<int>(P.dim) ? __ldg(raw + idx) : 0.0f;
       qa[e] = inv_norm ? __fmul_rn(v, inv) : v;
     }

@@ -41,13 +41,13 @@ class _BatchOptions(C.Structure):
                 ("hash_slots", C.c_uint32), ("cand_cap", C.c_uint32), ("warps_per_block", C.c_uint32),
                 ("pool_cap", C.c_uint32), ("queries_on_device", C.c_int32), ("out_on_device", C.c_int32),
                 ("filter_scan_permille", C.c_uint32), ("rerank_factor", C.c_uint32),
-                ("warps_per_query", C.c_uint32), ("reserved3", C.c_uint32)]
+                ("warps_per_query", C.c_uint32), ("lists_per_step", C.c_uint32)]
 
 
 class _ServerConfig(C.Structure):
     _fields_ = [("max_inflight", C.c_uint32), ("max_batch_queries", C.c_uint32), ("memory_budget", C.c_uint64),
                 ("precision", C.c_int32), ("filter_scan_permille", C.c_uint32), ("rerank_factor", C.c_uint32),
-                ("warps_per_query", C.c_uint32)]
+                ("warps_per_query", C.c_uint32), ("lists_per_step", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class _Request(C.Structure):
@@ -157,6 +157,13 @@ def _warps_per_query(v) -> int:
     v = int(v)
     if v not in (0, 1, 4):
         raise ValueError("warps_per_query must be 1 (one warp, the reference's order) or 4 (beam search)")
+    return v
+
+
+def _lists_per_step(v) -> int:
+    v = int(v)
+    if not 0 <= v <= 4:
+        raise ValueError("lists_per_step must be 0 (the reference's order) or 1..4 (beam search)")
     return v
 
 
@@ -341,7 +348,8 @@ class Index:
     def search_batch_ex(self, queries, k: int, ef: int = 0, ef_per_query=None, k_per_query=None, filters=None,
                         filter_of_query=None, stream=None, precision: int = 0, counters: bool = False,
                         hash_slots: int = 0, cand_cap: int = 0, warps_per_block: int = 0, pool_cap: int = 0,
-                        out=None, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1):
+                        out=None, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1,
+                        lists_per_step: int = 0):
         """search_batch with per-query ef / k / filter.  filter_scan (FP16 / FP8
         only): queries whose filter allows at most this fraction of the nodes
         are answered by the exact tensor-core scan instead of a graph walk.
@@ -349,7 +357,10 @@ class Index:
         rerank_factor x k entries of the traversal pool (at least 32); 0 = all.
         warps_per_query=4 (FP16 / FP8, dim <= 128): four warps walk each query
         as a beam search (lower latency per query; not the reference's visit
-        order, so recall is the bar)."""
+        order, so recall is the bar).  lists_per_step=1..4 (FP16 / FP8, dim <=
+        128): one warp walks each query as a beam search expanding that many
+        neighbour lists per step, row distances on the tensor cores (the
+        throughput form; recall is the bar)."""
         q, _ = self._queries(queries)
         nq = q.shape[0]
         if out is None:
@@ -360,6 +371,7 @@ class Index:
         opt.filter_scan_permille = int(round(filter_scan * 1000))
         opt.rerank_factor = _rerank_factor(rerank_factor)
         opt.warps_per_query = _warps_per_query(warps_per_query)
+        opt.lists_per_step = _lists_per_step(lists_per_step)
         keep = []
         if ef_per_query is not None:
             a = np.ascontiguousarray(ef_per_query, dtype=np.uint32)
@@ -396,7 +408,8 @@ class Index:
         return (out, cnt) if counters else out
 
     def search_device(self, q_ptr: int, nq: int, k: int, ef: int, out_ptr: int, stream: int = 0,
-                      ef_ptr: int = 0, k_ptr: int = 0, graph: bool = False, precision: int = 0):
+                      ef_ptr: int = 0, k_ptr: int = 0, graph: bool = False, precision: int = 0,
+                      rerank_factor: int = 0, warps_per_query: int = 1, lists_per_step: int = 0):
         """Enqueue a batch whose queries (nq x dim float32), optional per-query
         ef / k (uint32) and output records (nq x k x 16 bytes) live in device
         memory; returns once the work is on `stream` (a cudaStream_t handle).
@@ -406,6 +419,9 @@ class Index:
         opt.queries_on_device, opt.out_on_device = 1, 1
         opt.use_graph = 1 if graph else 0
         opt.precision = precision
+        opt.rerank_factor = _rerank_factor(rerank_factor)
+        opt.warps_per_query = _warps_per_query(warps_per_query)
+        opt.lists_per_step = _lists_per_step(lists_per_step)
         opt.ef_per_query = ef_ptr or None
         opt.k_per_query = k_ptr or None
         opt.stream = stream or None
@@ -580,16 +596,19 @@ class Server:
     precision 1 / 2 serves with FP16 / FP8 traversal and an exact FP32 rerank;
     with those, filter_scan answers requests whose filter allows at most that
     fraction of the nodes by the exact tensor-core scan, rerank_factor limits
-    the rerank to the pool's best rerank_factor x k, and warps_per_query=4
-    walks each query with four warps (beam search: lower latency)."""
+    the rerank to the pool's best rerank_factor x k, warps_per_query=4
+    walks each query with four warps (beam search: lower latency), and
+    lists_per_step=1..4 walks it with one warp expanding that many lists per
+    step (beam search, tensor-core distances: throughput)."""
 
     def __init__(self, index: Index, max_inflight: int = 4, max_batch_queries: int = 4096, memory_budget: int = 0,
-                 precision: int = 0, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1):
+                 precision: int = 0, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1,
+                 lists_per_step: int = 0):
         self._h = None
         self._index = index  # keep the index alive
         cfg = _ServerConfig(max_inflight, max_batch_queries, memory_budget, precision,
                             int(round(filter_scan * 1000)), _rerank_factor(rerank_factor),
-                            _warps_per_query(warps_per_query))
+                            _warps_per_query(warps_per_query), _lists_per_step(lists_per_step), 0)
         h = C.c_void_p()
         _check(lib().hg_server_create(index._h, C.byref(cfg), C.byref(h)))
         self._h = h

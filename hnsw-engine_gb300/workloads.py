@@ -110,9 +110,13 @@ def exact_knn_f64(base: np.ndarray, queries: np.ndarray, k: int, metric: str = "
 
 
 def recall_at_k(got: np.ndarray, truth: np.ndarray) -> float:
-    """Mean |got_i ∩ truth_i| / k over queries (labels; -1/invalid never match)."""
+    """Mean |got_i ∩ truth_i| / k over queries (labels; -1/invalid never match;
+    a row's labels are distinct)."""
     k = truth.shape[1]
+    g = np.asarray(got, dtype=np.int64)[:, :k]
+    t = np.asarray(truth, dtype=np.int64)
     hits = 0
-    for g, t in zip(got, truth):
-        hits += len(set(int(x) for x in g[:k]) & set(int(x) for x in t))
+    for s in range(0, g.shape[0], 8192):
+        gg, tt = g[s:s + 8192], t[s:s + 8192]
+        hits += int(((gg[:, :, None] == tt[:, None, :]) & (gg[:, :, None] >= 0)).any(2).sum())
     return hits / float(truth.shape[0] * k)

@@ -63,6 +63,11 @@ struct SearchOptions {
   /// FP16 / FP8 batches with dim <= 128: 4 = four warps walk each query (a
   /// beam search: lower latency, not the reference's visit order); 1 = one
   uint32_t warps_per_query = 1;
+  /// FP16 / FP8 batches with dim <= 128: 1..4 = one warp walks each query as
+  /// a beam search expanding this many neighbour lists per step, with row
+  /// distances on the tensor cores (throughput; not the reference's visit
+  /// order); 0 = the one-warp walk in the reference's order
+  uint32_t lists_per_step = 0;
 };
 
 class Index {

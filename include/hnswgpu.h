@@ -93,7 +93,10 @@ typedef struct {
                                       pool entries (at least 32); 0 = the whole pool */
   uint32_t warps_per_query;        /* precision 1 / 2, dim <= 128: 4 = four warps walk each query
                                       (beam search, lower latency); 0 / 1 = one warp */
-  uint32_t reserved3;
+  uint32_t lists_per_step;         /* precision 1 / 2, dim <= 128, warps_per_query <= 1: 1..4 = one
+                                      warp walks each query as a beam search expanding this many
+                                      lists per step, distances on the tensor cores; 0 = the
+                                      one-warp walk in the reference's order */
 } hg_batch_options;
 
 const char* hg_last_error(void);
@@ -190,6 +193,9 @@ typedef struct {
                                     entries (at least 32); 0 = the whole pool */
   uint32_t warps_per_query;      /* precision 1 / 2, dim <= 128: 4 = four warps walk each query
                                     (beam search, lower latency); 0 / 1 = one warp */
+  uint32_t lists_per_step;       /* precision 1 / 2, dim <= 128: one warp per query, a beam search
+                                    expanding this many lists per step (1..4); 0 = off */
+  uint32_t reserved;
 } hg_server_config;
 typedef struct {
   const float* queries;        /* nq x dim */

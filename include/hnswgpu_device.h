@@ -126,7 +126,11 @@ typedef struct {
    * its visit order is not the reference's, recall is the bar); 0 or 1 = one
    * warp per query, the reference's order.  No counterpart in the reference. */
   uint32_t warps_per_query;
-  uint32_t reserved4;
+  /* FP16 / FP8 with dim <= 128 and one warp per query: 1..4 = a beam search
+   * expanding this many neighbour lists per step, row distances on the
+   * tensor cores (mma.sync m16n8k16), for throughput; 0 = the walk in the
+   * reference's order.  No counterpart in the reference. */
+  uint32_t lists_per_step;
 } hgd_search_args;
 
 int hgd_graph_upload(const hgd_graph_view* view, int device, int order, hgd_graph** out);
