@@ -1,31 +1,38 @@
 """Benchmark of the batched HNSW query path on GB300.
 
-Workload (default): batched L2 at 200k -- n=200,000 vectors of d=128 from a
-256-cluster integer Gaussian mixture (seed 0), M=16, ef_construction=200,
-10,000 queries (seed 1) per step with per-query ef drawn uniformly from
-{10,20,40,80,160,320}, k=10, answered in one persistent launch.  The data
-are synthetic stand-ins with SIFT's shape (the ann-benchmarks sets are not
-available offline); recall@10 is measured against exact k-NN.
+Headline (the metric's configuration): QPS at recall@10 >= 0.95 on 1M x 128
+L2.  n = 1,000,000 vectors from a 1,024-cluster integer Gaussian mixture
+(seed 0), M = 16, ef_construction = 200, the graph built by the reference's
+own add_batch (its C++ library compiled on this host) and loaded by both
+sides from the same file; 100,000 queries (seed 1) per step, k = 10.  Every
+form runs at the smallest ef of a fixed list whose recall@10 on the first
+10,000 queries reaches 0.95 (exact k-NN ground truth).  The data are seeded
+synthetic stand-ins with SIFT-1M's shape (the ann-benchmarks sets are not
+available offline).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  `value` is QPS with queries already in HBM
-(device pointers, CUDA events on the launch stream, L2 flushed between
-steps); `e2e` is QPS through the host C ABI with pinned host buffers, the
-host->device copy of the queries and the device->host copy of the results
-inside the timed region.  --impl reference times the reference algorithm on
-the host cores (the oracle's C restatement of search_batch, all threads).
+Prints one JSON line (rank 0).  `value`: QPS of the fastest compressed form
+(FP16 / FP8 traversal + exact FP32 rerank, batched) with queries already in
+HBM, CUDA events on the launch stream; `e2e`: the same form through the host
+C ABI with pinned host buffers, copies inside the timed region;
+`config.plain_fp32`: the plain FP32 search_batch (the reference's algorithm,
+id-exact) measured the same way.  `cpu_baseline` and `--impl reference` time
+the reference's own Index::search_batch on the host cores.  Secondary blocks:
+`batched_200k` (mixed ef in one launch), `serving` (continuous batching at
+1M: p50 / p99 / p999), `precision` (d = 960: FP32 / FP16 / FP8 error and
+recall).
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 from pathlib import Path
 
@@ -35,16 +42,29 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO / "hnsw-engine_gb300"))
 sys.path.insert(0, str(REPO / "oracle"))
 
-N_BASE, DIM, CLUSTERS, NQ, K = 200_000, 128, 256, 10_000, 10
-EF_CHOICES = (10, 20, 40, 80, 160, 320)
-# DRAM bytes of one search launch over this batch, read from an ncu capture
-# (1.704 GB read + 0.432 GB written): below the algorithmic bytes, since part
-# of the graph is served from L2
-SEARCH_DRAM_BYTES = 2_136_463_000
-SEARCH_L2_HIT_RATE = 0.509  # lts__t_sector_hit_rate of the same capture
-M, EFC = 16, 200
 METRIC = "QPS at recall@10≥0.95 (served/batched vs plain GPU, same GB300); p50/p99 ms"
-WORKLOAD = "batched-L2-200k: n=200000 d=128 M=16 efC=200, 10000 queries/step, per-query ef U{10..320}, k=10"
+M, EFC = 16, 200
+HEAD_N, HEAD_DIM, HEAD_CLUSTERS, HEAD_NQ, HEAD_K = 1_000_000, 128, 1024, 100_000, 10
+HEAD_EFS = (16, 24, 32, 40, 48, 56, 64, 80, 96, 128, 160, 256)
+RECALL_TARGET = 0.95
+RECALL_SAMPLE = 10_000
+REF_STEP_QUERIES = 20_000  # reference arm: queries per timed step (a bounded sample)
+WORKLOAD = (f"l2-1M: n={HEAD_N} d={HEAD_DIM} (1,024-cluster integer mixture) M={M} efC={EFC}, graph from the "
+            f"reference's add_batch; {HEAD_NQ} queries/step, k={HEAD_K}, each form at the smallest ef in "
+            f"{list(HEAD_EFS)} with recall@10 >= {RECALL_TARGET} on the first {RECALL_SAMPLE} queries")
+# GPU forms.  fp32_plain is the reference's algorithm (id-exact); the others
+# walk compressed rows and rerank the best 4k of their pool in exact FP32.
+FORMS = [
+    ("fp32_plain", dict(precision=0)),
+    ("fp16_beam2", dict(precision=1, rerank_factor=4, lists_per_step=2)),
+    ("fp8_beam2", dict(precision=2, rerank_factor=4, lists_per_step=2)),
+    ("fp16_beam4", dict(precision=1, rerank_factor=4, lists_per_step=4)),
+    ("fp8_walk", dict(precision=2, rerank_factor=4)),
+    ("fp8_4warps", dict(precision=2, rerank_factor=4, warps_per_query=4)),
+]
+# DRAM bytes (read + write) of one launch of the headline kernel over the
+# batch, from an ncu capture (null until profiled)
+HEAD_DRAM_BYTES = None
 
 
 def dist_env():
@@ -54,43 +74,54 @@ def dist_env():
     return rank, world, local
 
 
-def workload(rank: int):
+# ---------------------------------------------------------------------------
+# graphs: the reference's add_batch, cached per host so both arms load one file
+# ---------------------------------------------------------------------------
+def cache_dir() -> Path:
+    d = Path(os.environ.get("HNSW_BENCH_CACHE") or (Path(tempfile.gettempdir()) / "hnsw-gb300-bench"))
+    d.mkdir(parents=True, exist_ok=True)
+    return d
+
+
+def bench_graph(tag: str, base: np.ndarray, metric: str = "l2"):
+    """(path, seconds, 'built' | 'cached'): the reference's add_batch over base
+    (all host threads), saved in its file format; reused when the same data
+    were built before on this host."""
+    import refcore
+
+    h = hashlib.sha256()
+    h.update(f"{tag}|{metric}|{M}|{EFC}|{base.shape}".encode())
+    h.update(base[:: max(1, base.shape[0] // 4096)].tobytes())
+    path = cache_dir() / f"{tag}-{h.hexdigest()[:16]}.idx"
+    if path.exists():
+        try:
+            refcore.RefIndex(path)  # loads and validates (checksums)
+            return path, 0.0, "cached"
+        except Exception:  # noqa: BLE001 - rebuild a damaged file
+            path.unlink()
+    tmp = path.with_suffix(f".tmp{os.getpid()}")
+    t0 = time.time()
+    refcore.build(base, tmp, metric=metric, M=M, ef_construction=EFC, threads=0)
+    os.replace(tmp, path)
+    return path, time.time() - t0, "built"
+
+
+def head_workload():
     import workloads
 
-    base, queries = workloads.int_mixture(N_BASE, DIM, CLUSTERS, NQ)
-    efs = np.random.default_rng(3 + rank).choice(np.array(EF_CHOICES, dtype=np.uint32), size=NQ)
-    return base, queries, efs
+    return workloads.int_mixture(HEAD_N, HEAD_DIM, HEAD_CLUSTERS, HEAD_NQ)
 
 
-def launches_per_batch(ef_max: int, single_launch: bool = False) -> int:
-    """Kernels one batch enqueues: the ef-bucketing kernel, the query kernels
-    (one largest-ef-first launch, or one per ef bucket 16, 32, 64, ... up to
-    ef_max) and the rerun pass."""
-    if single_launch:
-        return 3
-    buckets = 0
-    for hi in (16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024):
-        if buckets == 11:
-            break
-        buckets += 1
-        if hi >= ef_max:
-            break
-    else:
-        buckets += 1
-    return 2 + buckets
-
-
-def algorithmic_bytes(cnt: np.ndarray) -> float:
-    """Bytes a query must move: query row, upper/level-0 lists, one row per
-    distance, the tombstone bit word per level-0 candidate, the output row."""
-    row = 4 * 128
-    up_list, l0_list = 4 * (1 + M), 4 * (1 + 2 * M)
-    per_q = (4 * DIM + cnt[:, 0] * up_list + cnt[:, 1] * row + cnt[:, 2] * l0_list + cnt[:, 3] * row + K * 16)
-    return float(per_q.sum())
+def first_at_target(rows):
+    """Smallest-ef row whose recall reaches the target (else the best row)."""
+    for r in rows:
+        if r["recall_at_10"] >= RECALL_TARGET:
+            return r
+    return max(rows, key=lambda r: r["recall_at_10"])
 
 
 class Clocks:
-    """nvidia-smi samples during the timed region."""
+    """nvidia-smi samples during the timed region (query only)."""
 
     def __init__(self, index: int = 0):
         self.index = index
@@ -147,123 +178,149 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def algorithmic_bytes(cnt: np.ndarray, dim: int, pd: int, k: int, kw: dict) -> float:
+    """Bytes the walk must move per batch: the query, upper / layer-0 lists
+    (68 / 132 B per list, the file's records), one row per distance (FP32
+    4 pd; FP16 2 x 128 + 8 B row scale and norm on the beam walk; FP8 128 + 8 B
+    on the beam walk, 128 + 4 B on the others), the exact rerank's FP32 rows
+    and the output."""
+    prec = kw.get("precision", 0)
+    beam = kw.get("lists_per_step", 0) > 0
+    row = {0: 4 * pd, 1: 2 * 128 + (8 if beam else 0), 2: 128 + (8 if beam else 4)}[prec]
+    up_list, l0_list = 4 * (1 + M), 4 * (1 + 2 * M)
+    per_q = 4 * dim + cnt[:, 0] * up_list + cnt[:, 1] * row + cnt[:, 2] * l0_list + cnt[:, 3] * row + k * 16
+    if prec:
+        per_q = per_q + cnt[:, 6] * 4 * pd
+    return float(per_q.sum())
+
+
+def launches_per_step(kw: dict) -> int:
+    """Kernels one batch enqueues in these forms: the ef-bucketing kernel, one
+    persistent walk (all queries, largest ef first) and the rerun pass."""
+    return 3
+
+
+# ---------------------------------------------------------------------------
+# reference (CPU) helpers
+# ---------------------------------------------------------------------------
+def ref_time_batches(rx, batches, threads):
+    """Wall seconds of one search_batch call per (queries, k, ef, filter) batch."""
+    t0 = time.perf_counter()
+    outs = [rx.search_batch(q, k, ef, threads=threads, filt=f) for q, k, ef, f in batches]
+    return time.perf_counter() - t0, outs
+
+
+def host_cpu():
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return os.uname().machine
+
+
+def parity(gpu, ref):
+    return {"id_mismatches": int((gpu["label"] != ref["label"]).sum()),
+            "distance_bit_mismatches": int((gpu["distance"].view(np.uint32) != ref["distance"].view(np.uint32)).sum())}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
 def run_ours(args, rank, world, local):
     import torch
 
     import hnswgpu
+    import refcore
+    import workloads
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    base, queries, efs = workload(rank)
-    # graph: built with the library's CPU add_batch (all host threads), saved in
-    # FORMAT v1 and loaded back -- the file a CPU reference would also load
-    tmp = Path(tempfile.mkdtemp(prefix="hnswbench"))
-    gpath = tmp / "graph.idx"
-    t0 = time.time()
-    ix = hnswgpu.Index(DIM, "l2", M, EFC)
-    ix.add(base, num_threads=0)
-    ix.save(gpath)
-    build_s = time.time() - t0
+    base, queries = head_workload()
+    gpath, build_s, build_how = bench_graph("l2-1m", base)
     ix = hnswgpu.Index.load(gpath)
     ix.set_device(local)
+    pd = -(-HEAD_DIM // 16) * 16
 
-    # ground truth: exact k-NN on the GPU (brute force), FP32 exact on integer data
-    bf = hnswgpu.BruteForceIndex(DIM, "l2")
+    # ground truth of the recall sample: exact k-NN on the GPU (integer data:
+    # FP32 is exact), pinned against the reference's brute force on a sample
+    sample = queries[:RECALL_SAMPLE]
+    bf = hnswgpu.BruteForceIndex(HEAD_DIM, "l2")
     bf.add(base)
-    gt = bf.search_raw(queries, K)["label"].astype(np.int64)
+    gt = bf.search_raw(sample, HEAD_K)["label"].astype(np.int64)
     del bf
+    ref_bf = refcore.bruteforce(base, sample[:256], HEAD_K, threads=0)["label"].astype(np.int64)
+    gt_pin = int((ref_bf != gt[:256]).sum())
+
+    # operating point of every form: the smallest ef reaching the recall target
+    sweep = {}
+    for name, kw in FORMS:
+        rows = []
+        for ef in HEAD_EFS:
+            got = ix.search_batch_ex(sample, HEAD_K, ef, **kw)["label"].astype(np.int64)
+            rows.append({"ef": ef, "recall_at_10": round(workloads.recall_at_k(got, gt), 4)})
+            if rows[-1]["recall_at_10"] >= RECALL_TARGET:
+                break
+        sweep[name] = rows
 
     stream = torch.cuda.Stream(device=dev)
     q_d = torch.from_numpy(queries).to(dev)
-    ef_d = torch.from_numpy(efs.astype(np.int32)).to(dev)
-    out_d = torch.empty((NQ, K, 4), dtype=torch.int32, device=dev)  # 16-byte records
+    out_d = torch.empty((HEAD_NQ, HEAD_K, 4), dtype=torch.int32, device=dev)  # 16-byte records
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
-    ef_max = int(efs.max())
 
-    # launch shapes per ef bucket: autotuned on separate sample queries (seed 2)
-    import workloads
+    def step(kw, ef, graph=True):
+        ix.search_device(q_d.data_ptr(), HEAD_NQ, HEAD_K, ef, out_d.data_ptr(), stream.cuda_stream, graph=graph,
+                         **kw)
 
-    _, sample = workloads.int_mixture(N_BASE, DIM, CLUSTERS, NQ, qseed=2)
-    sample_efs = np.random.default_rng(4).choice(np.array(EF_CHOICES, dtype=np.uint32), NQ)
-    t0 = time.time()
-    if args.tuning and Path(args.tuning).exists():
-        # a table saved by an earlier run: the same launch shapes (a profiler
-        # serialises the tuner's timed trials, so it would pick other shapes)
-        tuning = json.loads(Path(args.tuning).read_text())
-        ix.set_tuning(tuning)
-    else:
-        tuning = ix.autotune(sample, k=K, ef_max=int(efs.max()), precision=0, ef_per_query=sample_efs,
-                             path=args.tuning)
-    tune_s = time.time() - t0
-
-    use_graph = args.launch == "graph"
-
-    def step_device(graph=False):
-        ix.search_device(q_d.data_ptr(), NQ, K, ef_max, out_d.data_ptr(), stream.cuda_stream, ef_ptr=ef_d.data_ptr(),
-                         graph=graph)
-
-    # recall and traversal counters of this batch (untimed; an NVTX range so a
-    # profiler can pick these launches out)
-    torch.cuda.nvtx.range_push("counters_batch")
-    rec, cnt = ix.search_batch_ex(queries, K, ef_per_query=efs, counters=True)
-    torch.cuda.nvtx.range_pop()
-    got = rec["label"].astype(np.int64)
-
-    recall = workloads.recall_at_k(got, gt)
-    alg_bytes = algorithmic_bytes(cnt)
-
-    # timed path: the batch's launch sequence replayed as one CUDA graph
-    # (captured on the second warm-up step); the plain-stream path is timed
-    # after it for comparison
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            flush.zero_()
-            step_device(graph=use_graph)
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        clocks = Clocks(local)
-        with clocks:
-            torch.cuda.nvtx.range_push("timed_steps")
-            wall0 = time.perf_counter()
-            for i in range(args.steps):
+    def timed(kw, ef, warmup, steps, clocks=None):
+        """Per-step device milliseconds (CUDA events on the launch stream)."""
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                flush.zero_()
+                step(kw, ef)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            if clocks:
+                clocks.__enter__()
+            for i in range(steps):
                 flush.zero_()
                 ev[i][0].record(stream)
-                step_device(graph=use_graph)
+                step(kw, ef)
                 ev[i][1].record(stream)
             torch.cuda.synchronize()
-            wall = time.perf_counter() - wall0
-            torch.cuda.nvtx.range_pop()
-        if world > 1:
-            torch.distributed.barrier()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    dev_ms = sum(step_ms)
-    # the same step launched kernel by kernel on forked streams
-    stream_ms = []
-    if use_graph:
-        with torch.cuda.stream(stream):
-            for i in range(args.warmup + args.steps):
-                flush.zero_()
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                step_device(graph=False)
-                b.record(stream)
-                torch.cuda.synchronize()
-                if i >= args.warmup:
-                    stream_ms.append(a.elapsed_time(b))
-    # device output equals the host-path output
-    dev_rec = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(NQ, K)
-    if not np.array_equal(dev_rec["label"], rec["label"]):
-        raise RuntimeError("device-resident batch differs from the host-path batch")
+            if clocks:
+                clocks.__exit__()
+        return [a.elapsed_time(b) for a, b in ev]
 
-    # e2e through the host C ABI with pinned host buffers
+    # every form at its operating point (a short timing), then the headline
+    table = {}
+    for name, kw in FORMS:
+        op = first_at_target(sweep[name])
+        ms = timed(kw, op["ef"], 2, 3)
+        table[name] = {"ef": op["ef"], "recall_at_10": op["recall_at_10"],
+                       "qps": round(HEAD_NQ / (statistics.median(ms) / 1e3), 1), "sweep": sweep[name]}
+    compressed = [n for n, _ in FORMS if n != "fp32_plain" and table[n]["recall_at_10"] >= RECALL_TARGET]
+    head = max(compressed, key=lambda n: table[n]["qps"]) if compressed else "fp32_plain"
+    head_kw = dict(FORMS)[head]
+    head_ef = table[head]["ef"]
+    plain_kw = dict(FORMS)["fp32_plain"]
+    plain_ef = table["fp32_plain"]["ef"]
+
+    clocks = Clocks(local)
+    head_ms = timed(head_kw, head_ef, args.warmup, args.steps, clocks)
+    plain_ms = timed(plain_kw, plain_ef, args.warmup, args.steps)
+    dev_ms = sum(head_ms)
+    plain_dev_ms = sum(plain_ms)
+
+    # e2e through the host C ABI: pinned queries in, pinned records out
     q_pin = torch.from_numpy(queries).pin_memory()
-    ef_pin = torch.from_numpy(efs.astype(np.uint32).view(np.int32)).pin_memory()
-    out_pin = torch.empty((NQ, K, 4), dtype=torch.int32).pin_memory()
+    out_pin = torch.empty((HEAD_NQ, HEAD_K, 4), dtype=torch.int32).pin_memory()
     qn = q_pin.numpy()
-    efn = ef_pin.numpy().view(np.uint32)
+    on = out_pin.numpy().view(hnswgpu.NEIGHBOR).reshape(-1)
     e2e_ms = []
     with torch.cuda.stream(stream):
         for i in range(args.warmup + args.steps):
@@ -271,73 +328,179 @@ def run_ours(args, rank, world, local):
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            ix.search_batch_ex(qn, K, ef_per_query=efn, stream=stream.cuda_stream,
-                               out=out_pin.numpy().view(hnswgpu.NEIGHBOR).reshape(-1))
+            ix.search_batch_ex(qn, HEAD_K, head_ef, stream=stream.cuda_stream, out=on, **head_kw)
             b.record(stream)
             torch.cuda.synchronize()
             if i >= args.warmup:
                 e2e_ms.append(a.elapsed_time(b))
     e2e_total = sum(e2e_ms)
+    # the device-resident batch answers as the host call does
+    step(head_kw, head_ef)
+    torch.cuda.synchronize()
+    dev_rec = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(HEAD_NQ, HEAD_K)
+    if not np.array_equal(dev_rec["label"], on.reshape(HEAD_NQ, HEAD_K)["label"]):
+        raise RuntimeError("device-resident batch differs from the host-call batch")
+
+    # traversal counters of the headline form (untimed) -> algorithmic bytes
+    _, cnt = ix.search_batch_ex(queries, HEAD_K, head_ef, counters=True, **head_kw)
+    alg_bytes = algorithmic_bytes(cnt, HEAD_DIM, pd, HEAD_K, head_kw)
 
     if world > 1:  # the job's time is the slowest replica's
         import replicas
 
         dev_ms, e2e_total = replicas.max_over_ranks(dev_ms), replicas.max_over_ranks(e2e_total)
-    qps = world * NQ * args.steps / (dev_ms / 1e3)
-    e2e_qps = world * NQ * args.steps / (e2e_total / 1e3)
+        plain_dev_ms = replicas.max_over_ranks(plain_dev_ms)
+    qps = world * HEAD_NQ * args.steps / (dev_ms / 1e3)
+    e2e_qps = world * HEAD_NQ * args.steps / (e2e_total / 1e3)
+    plain_qps = world * HEAD_NQ * args.steps / (plain_dev_ms / 1e3)
     per_launch_ms = dev_ms / args.steps
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    prec = head_kw.get("precision", 0)
     result = {
         "metric": METRIC, "value": round(qps, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(per_launch_ms, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian mixture, SIFT shape)",
-        "config": {"workload": WORKLOAD, "global_batch": world * NQ, "recall_at_10": round(recall, 4),
-                   "ef_mix": list(EF_CHOICES), "l2_flush": "256 MiB write before every timed step",
-                   "parallelism": f"replicas x{world} (queries per replica fixed)", "build_s": round(build_s, 2),
-                   "launch": ("one CUDA-graph replay per step" if use_graph else "kernel launches per step") +
-                             (" (bucket kernel, one persistent largest-ef-first search launch, rerun pass)"
-                              if tuning["launch_mode"] == 1 else
-                              " (bucket kernel, per-ef-bucket persistent launches on prioritised forked streams, "
-                              "rerun pass)"),
-                   "streams_ms_per_step": round(statistics.median(stream_ms), 4) if stream_ms else None,
-                   "autotune": {"seconds": round(tune_s, 2),
-                                "sample": f"{NQ} seed-2 queries of the same mixture, ef from the same set (seed 4)",
-                                "launch_mode": ["per-bucket launches", "one largest-ef-first launch"][tuning["launch_mode"]],
-                                "buckets": {str(e["ef_hi"]): [e["hash_slots"], e["cand_cap"], e["warps_per_block"],
-                                                              round(e["default_us_per_query"] / max(e["us_per_query"], 1e-9), 3)]
-                                            for e in tuning["entries"]},
-                                "fields": "hash_slots, cand_cap, warps_per_block (0 = default), speed-up over default"},
-                   "mean_l0_expansions": round(float(cnt[:, 2].mean()), 2),
+        "scaling": "weak", "vs_baseline": None, "dtype": {0: "f32", 1: "f16", 2: "fp8-e4m3"}[prec],
+        "data": "synthetic (seeded 1,024-cluster integer Gaussian mixture, SIFT-1M shape)",
+        "config": {"workload": WORKLOAD, "global_batch": world * HEAD_NQ, "form": head, "form_options": head_kw,
+                   "ef": head_ef, "recall_at_10": table[head]["recall_at_10"],
+                   "plain_fp32": {"ef": plain_ef, "recall_at_10": table["fp32_plain"]["recall_at_10"],
+                                  "qps": round(plain_qps, 1), "ms_per_step": round(plain_dev_ms / args.steps, 4)},
+                   "compressed_over_plain": round(qps / plain_qps, 3),
+                   "forms": table, "l2_flush": "256 MiB write before every timed step (the graph and rows "
+                                                "also exceed the 129 MB L2)",
+                   "launch": "one CUDA-graph replay per step: bucket kernel, one persistent walk, rerun pass",
+                   "parallelism": f"replicas x{world} (queries per replica fixed)",
+                   "graph": {"source": "reference add_batch (all host threads), FORMAT v1 file",
+                             "seconds": round(build_s, 1), "how": build_how},
+                   "ground_truth": {"kind": "GPU brute force, exact on integer data",
+                                    "mismatches_vs_reference_bruteforce_256q": gt_pin},
+                   "mean_l0_lists": round(float(cnt[:, 2].mean()), 2),
                    "mean_l0_distances": round(float(cnt[:, 3].mean()), 2)},
-        "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": int(NQ * DIM * 4 + NQ * 4),
-                "d2h_bytes_per_step": int(NQ * K * 16)},
-        "gpu_launches": launches_per_batch(ef_max, tuning["launch_mode"] == 1) * args.steps,
+        "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s",
+                "h2d_bytes_per_step": int(HEAD_NQ * HEAD_DIM * 4), "d2h_bytes_per_step": int(HEAD_NQ * HEAD_K * 16)},
+        "gpu_launches": launches_per_step(head_kw) * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": SEARCH_DRAM_BYTES,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this workload's "
-                                       "search launch (one batch, cold L2)",
-                     "l2_hit_rate": SEARCH_L2_HIT_RATE,
-                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(alg_bytes)},
+                     "frac": round(achieved / peak, 4), "traffic": HEAD_DRAM_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the headline walk "
+                                       "(one launch over the batch)",
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(alg_bytes),
+                     "kernel": "beam_kernel" if head_kw.get("lists_per_step") else "search_kernel"},
         "clocks": clocks.summary(),
-        "wall_s": round(wall, 3),
     }
     if rank == 0 and world == 1:
-        result["cpu_baseline"] = cpu_baseline(gpath, queries, efs)
+        result["cpu_baseline"] = cpu_baseline(ix, gpath, queries, plain_ef)
         del ix
+        if not args.no_batched:
+            result["batched_200k"] = run_batched_200k(local)
         if not args.no_serving:
-            result["serving"] = run_serving(local)
+            result["serving"] = run_serving(local, gpath)
         if not args.no_precision:
             result["precision"] = run_precision(local)
     return result
 
 
-SERVE_N, SERVE_CLUSTERS, SERVE_REQUESTS = 1_000_000, 1024, 20_000
+def cpu_baseline(ix, gpath, queries, ef):
+    """The reference's own search_batch on the host cores (all threads) at the
+    plain path's operating ef, over the whole batch, and the plain GPU path's
+    answers compared with it: ids and distance bits."""
+    import refcore
+
+    threads = os.cpu_count() or 1
+    rx = refcore.RefIndex(gpath)
+    rx.search_batch(queries[:2000], HEAD_K, ef, threads=threads)  # warm-up
+    t0 = time.perf_counter()
+    ref = rx.search_batch(queries, HEAD_K, ef, threads=threads)
+    el = time.perf_counter() - t0
+    gpu = ix.search_raw(queries, HEAD_K, ef)
+    return {"value": round(HEAD_NQ / el, 1), "unit": "queries/s", "cores": threads, "kind": "reference",
+            "sample": f"all {HEAD_NQ} queries of the batch in one reference search_batch call at ef={ef} "
+                      f"(the plain form's operating point), {threads} threads, simd {refcore.isa()}, "
+                      f"host {host_cpu()}",
+            "parity_vs_plain_gpu": {"queries": HEAD_NQ, **parity(gpu, ref)}}
+
+
+# ---------------------------------------------------------------------------
+# batched L2 at 200k: per-query ef in one persistent launch
+# ---------------------------------------------------------------------------
+B2_N, B2_CLUSTERS, B2_NQ = 200_000, 256, 10_000
+B2_EFS = (10, 20, 40, 80, 160, 320)
+
+
+def run_batched_200k(local):
+    """200,000 x 128 (256 clusters), 10,000 queries with ef drawn per query from
+    {10..320}, k = 10: one persistent launch on the GPU (plain FP32) against the
+    reference's search_batch grouped per ef; ids and distances compared."""
+    import torch
+
+    import hnswgpu
+    import refcore
+    import workloads
+
+    base, queries = workloads.int_mixture(B2_N, HEAD_DIM, B2_CLUSTERS, B2_NQ)
+    efs = np.random.default_rng(3).choice(np.array(B2_EFS, dtype=np.uint32), size=B2_NQ)
+    gpath, build_s, how = bench_graph("l2-200k", base)
+    ix = hnswgpu.Index.load(gpath)
+    ix.set_device(local)
+    dev = torch.device("cuda", local)
+    _, sample = workloads.int_mixture(B2_N, HEAD_DIM, B2_CLUSTERS, B2_NQ, qseed=2)
+    sample_efs = np.random.default_rng(4).choice(np.array(B2_EFS, dtype=np.uint32), B2_NQ)
+    ix.autotune(sample, k=HEAD_K, ef_max=int(efs.max()), precision=0, ef_per_query=sample_efs)
+    stream = torch.cuda.Stream(device=dev)
+    q_d = torch.from_numpy(queries).to(dev)
+    ef_d = torch.from_numpy(efs.astype(np.int32)).to(dev)
+    out_d = torch.empty((B2_NQ, HEAD_K, 4), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    ms = []
+    with torch.cuda.stream(stream):
+        for i in range(8):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ix.search_device(q_d.data_ptr(), B2_NQ, HEAD_K, int(efs.max()), out_d.data_ptr(), stream.cuda_stream,
+                             ef_ptr=ef_d.data_ptr(), graph=True)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if i >= 3:
+                ms.append(a.elapsed_time(b))
+    gpu = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(B2_NQ, HEAD_K)
+    bf = hnswgpu.BruteForceIndex(HEAD_DIM, "l2")
+    bf.add(base)
+    gt = bf.search_raw(queries, HEAD_K)["label"].astype(np.int64)
+    del bf
+    threads = os.cpu_count() or 1
+    rx = refcore.RefIndex(gpath)
+    groups = [np.nonzero(efs == e)[0] for e in B2_EFS]
+    batches = [(queries[g], HEAD_K, int(e), None) for g, e in zip(groups, B2_EFS)]
+    ref_time_batches(rx, batches, threads)  # warm-up
+    el, outs = ref_time_batches(rx, batches, threads)
+    ref = np.empty((B2_NQ, HEAD_K), dtype=refcore.NEIGHBOR)
+    for g, o in zip(groups, outs):
+        ref[g] = o
+    return {"workload": f"batched-L2-200k: n={B2_N} d={HEAD_DIM} M={M} efC={EFC} (reference add_batch), {B2_NQ} "
+                        f"queries, per-query ef U{list(B2_EFS)}, k={HEAD_K}, one persistent launch (plain FP32)",
+            "graph_seconds": round(build_s, 1), "graph": how,
+            "qps": round(B2_NQ / (statistics.median(ms) / 1e3), 1), "ms_per_batch": round(statistics.median(ms), 4),
+            "recall_at_10": round(workloads.recall_at_k(gpu["label"].astype(np.int64), gt), 4),
+            "reference_qps": round(B2_NQ / el, 1),
+            "reference": f"search_batch per ef group, {threads} threads, simd {refcore.isa()}",
+            "parity_vs_reference": {"queries": B2_NQ, **parity(gpu, ref)}}
+
+
+# ---------------------------------------------------------------------------
+# serving at 1M
+# ---------------------------------------------------------------------------
+SERVE_REQUESTS = 20_000
 SERVE_LOADS = (0.25, 0.5, 0.75, 1.0)
 SERVE_FILTERS = 16  # pool of distinct random 10%-density bitsets
 SERVE_RECALL_REQUESTS = 2000
-SERVE_PLAIN_REQUESTS = 2000
-SERVE_RERANK_FACTOR = 4  # FP8 forms: exact rerank of the pool's best 4 x k (at least 32)
+SERVE_PLAIN_REQUESTS = 500
+SERVE_FORMS = (
+    # name, server options
+    ("fp32", dict(precision=0)),
+    ("fp16_beam2_scan", dict(precision=1, filter_scan=0.15, rerank_factor=4, lists_per_step=2)),
+    ("fp8_4warps_scan", dict(precision=2, filter_scan=0.15, rerank_factor=4, warps_per_query=4)),
+)
 
 
 def serving_workload():
@@ -350,28 +513,25 @@ def serving_workload():
     ks = r.choice(np.array([1, 10, 100]), SERVE_REQUESTS)
     efs = r.choice(np.arange(16, 513, 16), SERVE_REQUESTS)
     fsel = np.where(r.random(SERVE_REQUESTS) < 0.2, r.integers(0, SERVE_FILTERS, SERVE_REQUESTS), -1)
-    base, queries = workloads.int_mixture(SERVE_N, DIM, SERVE_CLUSTERS, int(nqs.sum()))
+    _, queries = workloads.int_mixture(1, HEAD_DIM, HEAD_CLUSTERS, int(nqs.sum()))
     rf = np.random.default_rng(5)
-    masks = [rf.random(SERVE_N) < 0.1 for _ in range(SERVE_FILTERS)]
-    return base, queries, nqs, ks, efs, fsel, masks
+    masks = [rf.random(HEAD_N) < 0.1 for _ in range(SERVE_FILTERS)]
+    return queries, nqs, ks, efs, fsel, masks
 
 
-def run_serving(local):
-    """The served, batched search at 1M (FP8-E4M3 traversal + exact FP32 rerank,
-    and plain FP32) next to one plain FP32 search_batch over the same queries."""
+def run_serving(local, gpath):
+    """The served, batched search at 1M (continuous batching): FP32 and the
+    compressed forms, p50 / p99 / p999 at 25 / 50 / 75 / 100% of each form's
+    peak, beside plain search_batch calls over the same queries."""
     import hnswgpu
     import workloads
 
-    base, queries, nqs, ks, efs, fsel, masks = serving_workload()
-    t0 = time.time()
-    ix = hnswgpu.Index(DIM, "l2", M, EFC)
-    ix.add(base, num_threads=0)
-    build_s = time.time() - t0
+    base, _ = head_workload()
+    queries, nqs, ks, efs, fsel, masks = serving_workload()
+    ix = hnswgpu.Index.load(gpath)
     ix.set_device(local)
-    bitsets = [hnswgpu.Bitset(workloads.mask_to_words(m), SERVE_N) for m in masks]
-    # launch shapes for both forms, tuned on separate queries (seed 2, same
-    # cluster centres) with the serving ef mix
-    _, sample = workloads.int_mixture(1, DIM, SERVE_CLUSTERS, 4096, qseed=2)
+    bitsets = [hnswgpu.Bitset(workloads.mask_to_words(m), HEAD_N) for m in masks]
+    _, sample = workloads.int_mixture(1, HEAD_DIM, HEAD_CLUSTERS, 4096, qseed=2)
     sample_efs = np.random.default_rng(8).choice(np.arange(16, 513, 16), 4096).astype(np.uint32)
     t0 = time.time()
     for prec in (0, 2):
@@ -384,21 +544,18 @@ def run_serving(local):
     requests = [(queries[offs[i]:offs[i + 1]], int(ks[i]), int(efs[i]), bitsets[fsel[i]] if fsel[i] >= 0 else None)
                 for i in range(SERVE_REQUESTS)]
 
-    # plain FP32 search_batch, the reference's call: one call per request (its
-    # own k, ef and filter), one after another, on a sample of the requests
-    for i in range(200):
+    # plain FP32 search_batch, the reference's call: one call per request
+    for i in range(50):
         ix.search_raw(*requests[i])
     t = time.perf_counter()
     for i in range(SERVE_PLAIN_REQUESTS):
         ix.search_raw(*requests[i])
-    per_request_s = time.perf_counter() - t
-    per_request_qps = int(offs[SERVE_PLAIN_REQUESTS]) / per_request_s
+    per_request_qps = int(offs[SERVE_PLAIN_REQUESTS]) / (time.perf_counter() - t)
 
-    # batched FP32: all queries with per-query ef / k / filter in 65,536-query
-    # calls (host buffers in and out)
+    # batched FP32: all queries with per-query ef / k / filter in 65,536-query calls
     chunk = 65536
     plain = np.empty((total_q, 100), dtype=hnswgpu.NEIGHBOR)
-    for rep in range(2):  # the first pass mirrors the graph and warms up
+    for rep in range(2):  # the first pass warms up
         t = time.perf_counter()
         for s in range(0, total_q, chunk):
             e = min(s + chunk, total_q)
@@ -407,10 +564,9 @@ def run_serving(local):
         plain_s = time.perf_counter() - t
     plain_qps = total_q / plain_s
 
-    # recall against exact k-NN (brute force on the GPU, exact on integer data)
-    # over the first requests, per filter group
+    # recall against exact k-NN over the first requests, per filter group
     sample_q = int(offs[SERVE_RECALL_REQUESTS])
-    bf = hnswgpu.BruteForceIndex(DIM, "l2")
+    bf = hnswgpu.BruteForceIndex(HEAD_DIM, "l2")
     bf.add(base)
     gt = np.empty((sample_q, 100), dtype=np.int64)
     for f in range(-1, SERVE_FILTERS):
@@ -431,31 +587,23 @@ def run_serving(local):
         return round(r_all / sample_q, 4), round(r10 / max(n10, 1), 4)
 
     plain_recall = recall(lambda q, k: plain[q, :k]["label"].astype(np.int64))
-    out = {"workload": f"serving-L2-1M: n={SERVE_N} d={DIM} M={M} efC={EFC}, {SERVE_REQUESTS} requests, "
-                       f"{total_q} queries, 1..256 queries/request log-uniform, k in {{1,10,100}}, "
-                       f"ef in {{16..512 step 16}}, 20% with a 10%-density bitset (pool of {SERVE_FILTERS})",
-           "build_s": round(build_s, 1), "autotune_s": round(tune_s, 1), "queries": total_q,
+    out = {"workload": f"serving-L2-1M: the headline graph, {SERVE_REQUESTS} requests, {total_q} queries, 1..256 "
+                       f"queries/request log-uniform, k in {{1,10,100}}, ef in {{16..512 step 16}}, 20% with a "
+                       f"10%-density bitset (pool of {SERVE_FILTERS})",
+           "autotune_s": round(tune_s, 1), "queries": total_q,
            "plain_fp32_search_batch_per_request": {
                "qps": round(per_request_qps, 1), "requests": SERVE_PLAIN_REQUESTS,
                "note": "one search_batch call per request (the reference API: one k / ef / filter per call)"},
            "batched_fp32_search_batch_ex": {"qps": round(plain_qps, 1), "recall_at_k": plain_recall[0],
                                             "recall_at_10": plain_recall[1], "queries_per_call": chunk}}
-    # forms: FP32 walk; FP8 walk + exact rerank of the pool's best
-    # SERVE_RERANK_FACTOR x k; the same with requests whose
-    # filter allows <= 15% of the nodes answered by the exact tensor-core
-    # scan; the last also walks with four warps per query (beam search)
-    for name, prec, scan, rf, wpq in (("fp32", 0, 0.0, 0, 1), ("fp8_rerank", 2, 0.0, SERVE_RERANK_FACTOR, 1),
-                                      ("fp8_rerank_filter_scan", 2, 0.15, SERVE_RERANK_FACTOR, 1),
-                                      ("fp8_rerank_filter_scan_4warps", 2, 0.15, SERVE_RERANK_FACTOR, 4)):
-        srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, precision=prec, filter_scan=scan,
-                             rerank_factor=rf, warps_per_query=wpq)
-        srv.replay(requests[:2000], np.zeros(2000))  # warm-up: encodes the FP8 copy, sizes the staging
+    for name, opts in SERVE_FORMS:
+        srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, **opts)
+        srv.replay(requests[:2000], np.zeros(2000))  # warm-up: encodes the copy, sizes the staging
         peak, outs = srv.replay(requests, np.zeros(SERVE_REQUESTS))
         same = all(np.array_equal(outs[i]["label"], plain[offs[i]:offs[i + 1], :ks[i]]["label"])
-                   for i in range(SERVE_REQUESTS)) if prec == 0 else None
+                   for i in range(SERVE_REQUESTS)) if opts["precision"] == 0 else None
         rec = recall(lambda q, k: outs[req_rows[q]][q - offs[req_rows[q]], :k]["label"].astype(np.int64))
-        form = {"peak_qps": round(peak["qps"], 1), "recall_at_k": rec[0], "recall_at_10": rec[1],
-                "rerank_factor": rf, "warps_per_query": wpq,
+        form = {"options": opts, "peak_qps": round(peak["qps"], 1), "recall_at_k": rec[0], "recall_at_10": rec[1],
                 "peak_p50_ms": round(peak["p50_ms"], 3), "peak_mean_batch_queries": round(peak["mean_batch_queries"], 1),
                 "loads": []}
         if same is not None:
@@ -471,45 +619,42 @@ def run_serving(local):
                                   "mean_batch_queries": round(st["mean_batch_queries"], 1)})
         srv.close()
         out[name] = form
-    best = max(("fp8_rerank", "fp8_rerank_filter_scan", "fp8_rerank_filter_scan_4warps"),
-               key=lambda f: out[f]["peak_qps"])
-    out["served_fp8_form"] = best
-    out["served_fp8_over_plain_fp32"] = round(out[best]["peak_qps"] / per_request_qps, 3)
-    out["served_fp8_over_batched_fp32"] = round(out[best]["peak_qps"] / plain_qps, 3)
+    best = max((n for n, o in SERVE_FORMS if o["precision"]), key=lambda n: out[n]["peak_qps"])
+    out["served_compressed_form"] = best
+    out["served_compressed_over_batched_fp32"] = round(out[best]["peak_qps"] / plain_qps, 3)
+    out["served_compressed_over_served_fp32"] = round(out[best]["peak_qps"] / out["fp32"]["peak_qps"], 3)
     return out
 
 
+# ---------------------------------------------------------------------------
+# precision at d = 960
+# ---------------------------------------------------------------------------
 PREC_N, PREC_DIM, PREC_NQ = 200_000, 960, 5_000
-PREC_EFS = (40, 64, 128, 256, 512)
+PREC_EFS = (40, 64, 128, 256, 512, 1024)
 
 
 def run_precision(local):
-    """Precision path at d=960: |N(0,1)| x per-dimension scale U[0.05, 1],
-    200,000 rows, 5,000 queries.  For FP32, FP16 and FP8-E4M3 (per-row scale)
-    traversal, each followed by the exact FP32 rerank: QPS and recall@10 per
-    ef, the error of the returned distances against FP64, and the error of
-    the compressed copies' traversal distances against FP64."""
+    """Precision path at d = 960: |N(0,1)| x per-dimension scale U[0.05, 1],
+    200,000 rows, 5,000 queries.  For FP32, FP16 and FP8-E4M3 (per-row
+    scale) traversal, each followed by the exact FP32 rerank: QPS (queries on
+    the device, CUDA events, median of 3) and recall@10 per ef, the error of
+    the returned distances against FP64, and the error of the compressed
+    copies' traversal distances against FP64."""
     import torch
 
     import hnswgpu
     import workloads
 
     base, queries = workloads.scaled_abs_normal(PREC_N, PREC_DIM, PREC_NQ)
-    t0 = time.time()
-    ix = hnswgpu.Index(PREC_DIM, "l2", M, EFC)
-    ix.add(base, num_threads=0)
-    build_s = time.time() - t0
+    gpath, build_s, how = bench_graph("l2-960", base)
+    ix = hnswgpu.Index.load(gpath)
     ix.set_device(local)
     bf = hnswgpu.BruteForceIndex(PREC_DIM, "l2")
     bf.add(base)
-    gt = bf.search_raw(queries, K)["label"].astype(np.int64)
+    gt = bf.search_raw(queries, HEAD_K)["label"].astype(np.int64)
     del bf
     b64 = base.astype(np.float64)
     q64 = queries.astype(np.float64)
-
-    def fp64_dist(qi, ids):
-        return ((b64[ids] - q64[qi][:, None, :]) ** 2).sum(-1)
-
     # traversal distances of the compressed copies on a sample of (query, row) pairs
     rs = np.random.default_rng(7)
     pq = rs.integers(0, PREC_NQ, 20_000)
@@ -525,70 +670,97 @@ def run_precision(local):
         rel = np.abs(((xx - q64[pq]) ** 2).sum(-1) - exact) / np.maximum(exact, 1e-30)
         trav[name] = {"mean_rel": float(rel.mean()), "max_rel": float(rel.max())}
 
-    out = {"workload": f"precision-L2-960: n={PREC_N} d={PREC_DIM} M={M} efC={EFC}, {PREC_NQ} queries, k={K}",
-           "build_s": round(build_s, 1), "traversal_distance_error_vs_fp64": trav, "variants": {}}
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    q_d = torch.from_numpy(queries).to(dev)
+    out_d = torch.empty((PREC_NQ, HEAD_K, 4), dtype=torch.int32, device=dev)
+    out = {"workload": f"precision-L2-960: n={PREC_N} d={PREC_DIM} M={M} efC={EFC} (reference add_batch), "
+                       f"{PREC_NQ} queries, k={HEAD_K}",
+           "graph_seconds": round(build_s, 1), "graph": how, "traversal_distance_error_vs_fp64": trav, "variants": {}}
     for name, prec in (("fp32", 0), ("fp16_rerank", 1), ("fp8_rerank", 2)):
         rows = []
         for ef in PREC_EFS:
-            ix.search_batch_ex(queries[:256], K, ef, precision=prec)  # warm-up (builds the copy once)
-            t = time.perf_counter()
-            rec = ix.search_batch_ex(queries, K, ef, precision=prec)
-            el = time.perf_counter() - t
+            ms = []
+            with torch.cuda.stream(stream):
+                for i in range(5):
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    ix.search_device(q_d.data_ptr(), PREC_NQ, HEAD_K, ef, out_d.data_ptr(), stream.cuda_stream,
+                                     precision=prec)
+                    b.record(stream)
+                    torch.cuda.synchronize()
+                    if i >= 2:
+                        ms.append(a.elapsed_time(b))
+            rec = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(PREC_NQ, HEAD_K)
             got = rec["label"].astype(np.int64)
-            d64 = fp64_dist(np.arange(PREC_NQ), got)
+            d64 = ((b64[got] - q64[:, None, :]) ** 2).sum(-1)
             rel = np.abs(rec["distance"].astype(np.float64) - d64) / np.maximum(d64, 1e-30)
-            rows.append({"ef": ef, "qps": round(PREC_NQ / el, 1), "recall_at_10": round(workloads.recall_at_k(got, gt), 4),
+            rows.append({"ef": ef, "qps": round(PREC_NQ / (statistics.median(ms) / 1e3), 1),
+                         "recall_at_10": round(workloads.recall_at_k(got, gt), 4),
                          "dist_mean_rel_err_vs_fp64": float(rel.mean()), "dist_max_rel_err_vs_fp64": float(rel.max())})
         out["variants"][name] = rows
+    best = max(r["recall_at_10"] for r in out["variants"]["fp32"])
+    out["recall_target_reached"] = best >= RECALL_TARGET
+    out["largest_ef"] = PREC_EFS[-1]
     return out
 
 
-def cpu_baseline(gpath, queries, efs, sample=None):
-    """The reference algorithm (oracle restatement of search_batch) on the host
-    cores, grouped per ef like one reference call per group."""
-    import pyoracle
-
-    threads = os.cpu_count() or 1
-    ox = pyoracle.OracleIndex(gpath, isa=pyoracle.host_isa())
-    nq = queries.shape[0] if sample is None else sample
-    qs, es = queries[:nq], efs[:nq]
-    t0 = time.perf_counter()
-    for ef in EF_CHOICES:
-        sel = es == ef
-        if sel.any():
-            ox.search_batch(qs[sel], K, int(ef), threads=threads)
-    el = time.perf_counter() - t0
-    return {"value": round(nq / el, 1), "unit": "queries/s", "cores": threads, "kind": "port",
-            "sample": f"{nq} queries of the same mixed-ef batch, one search_batch per ef group, "
-                      f"{threads} threads, distance order {pyoracle.host_isa()}"}
-
-
+# ---------------------------------------------------------------------------
+# the reference arm
+# ---------------------------------------------------------------------------
 def run_reference(args, rank, world):
-    """--impl reference: the reference algorithm on the host cores."""
+    """--impl reference: the reference's own Index::search_batch (its C++
+    library compiled on this host) on the host cores, on the headline
+    workload: the same graph file, the operating point picked the same way
+    (smallest ef with recall@10 >= 0.95 on the first 10,000 queries, ground
+    truth from the reference's brute force), each step one search_batch over
+    20,000 queries of the batch with all host threads."""
     if rank != 0:
         return None
-    import hnswgpu  # only to build the same graph file
+    try:
+        import refcore
 
-    base, queries, efs = workload(0)
-    tmp = Path(tempfile.mkdtemp(prefix="hnswref"))
-    gpath = tmp / "graph.idx"
-    ix = hnswgpu.Index(DIM, "l2", M, EFC)
-    ix.add(base, num_threads=0)
-    ix.save(gpath)
-    sample = 4000
-    vals = []
+        refcore.lib()
+    except Exception as e:  # noqa: BLE001
+        return {"impl": "reference", "unavailable": f"the reference library could not be built here: {e}"[:300]}
+    import workloads
+
+    base, queries = head_workload()
+    gpath, build_s, how = bench_graph("l2-1m", base)
+    rx = refcore.RefIndex(gpath)
+    threads = os.cpu_count() or 1
+    sample = queries[:RECALL_SAMPLE]
+    gt = refcore.bruteforce(base, sample, HEAD_K, threads=threads)["label"].astype(np.int64)
+    rows = []
+    for ef in HEAD_EFS:
+        got = rx.search_batch(sample, HEAD_K, ef, threads=threads)["label"].astype(np.int64)
+        rows.append({"ef": ef, "recall_at_10": round(workloads.recall_at_k(got, gt), 4)})
+        if rows[-1]["recall_at_10"] >= RECALL_TARGET:
+            break
+    op = first_at_target(rows)
+    ef = op["ef"]
+    per = []
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(gpath, queries, efs, sample=sample)
+        s = (i * REF_STEP_QUERIES) % HEAD_NQ
+        qs = queries[s:s + REF_STEP_QUERIES]
+        t0 = time.perf_counter()
+        rx.search_batch(qs, HEAD_K, ef, threads=threads)
+        el = time.perf_counter() - t0
         if i >= args.warmup:
-            vals.append(r["value"])
-    v = statistics.median(vals)
-    ms = sample / v * 1e3
+            per.append(el)
+    v = REF_STEP_QUERIES * args.steps / sum(per)
     return {"metric": METRIC, "value": round(v, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian mixture, SIFT shape)",
-            "config": {"workload": WORKLOAD}, "impl": "reference",
-            "cpu_baseline": {"value": round(v, 1), "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"{sample} queries per step of the mixed-ef batch, all host threads"},
+            "warmup": args.warmup, "ms_per_step": round(sum(per) / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 1,024-cluster integer Gaussian mixture, SIFT-1M shape)",
+            "config": {"workload": WORKLOAD, "global_batch": REF_STEP_QUERIES, "form": "reference search_batch",
+                       "ef": ef, "recall_at_10": op["recall_at_10"], "sweep": rows,
+                       "graph": {"source": "reference add_batch (all host threads), FORMAT v1 file",
+                                 "seconds": round(build_s, 1), "how": how}},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(v, 1), "unit": "queries/s", "cores": threads, "kind": "reference",
+                             "sample": f"{REF_STEP_QUERIES} queries of the batch per step, one search_batch call, "
+                                       f"ef={ef}, {threads} threads, simd {refcore.isa()}, host {host_cpu()}"},
             "e2e": {"value": round(v, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -598,12 +770,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--no-serving", action="store_true", help="skip the 1M serving measurement")
-    ap.add_argument("--no-precision", action="store_true", help="skip the d=960 precision measurement")
-    ap.add_argument("--tuning", default=None,
-                    help="launch-shape table: loaded if the file exists, else autotuned and saved there")
-    ap.add_argument("--launch", choices=["graph", "streams"], default="graph",
-                    help="timed step: one CUDA-graph replay, or kernel launches on forked streams")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 200k mixed-ef block")
+    ap.add_argument("--no-serving", action="store_true", help="skip the 1M serving block")
+    ap.add_argument("--no-precision", action="store_true", help="skip the d=960 precision block")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
