@@ -1,471 +1,320 @@
-// build.cpp -- graph construction on the host CPU (Malkov & Yashunin Alg. 1
-// with the Alg. 4 heuristic), restating the reference's add/add_batch
-// (src/index.cpp:48-306) and its locked layer search
-// (src/search_layer.cpp:29-134, Locked = true).
+// build.cpp -- CPU graph construction behind hnsw::Index::add / add_batch.
 //
-// Construction is not on the GPU path: it produces the graph that the query
-// kernels traverse, exactly as the reference's add_batch would.  With one
-// thread the result is deterministic and byte-identical to the reference's
-// single-threaded build on a host using the same distance order; with more
-// threads it is as nondeterministic as the reference's parallel build.
+// The search kernels walk the graph the reference builds, so this builder
+// produces that graph: Malkov & Yashunin's insertion (Alg. 1) with the
+// neighbour-selection heuristic (Alg. 4, no candidate extension, no kept
+// pruned connections), as the reference's src/index.cpp:94-306 and its
+// locked layer search src/search_layer.cpp:29-134 define it.  What has to be
+// the same for the same graph:
+//   * levels: splitmix64 draws from the seed in input order, u in (0, 1]
+//     from the top 53 bits, level = floor(-ln(u) / ln M), at most 64;
+//   * the layer search's order and rules: candidates by (distance, internal
+//     id), a candidate accepted while the result set holds fewer than ef or
+//     it is strictly closer than the farthest result, the search ending when
+//     the closest open candidate is farther than the farthest of ef results;
+//   * M neighbours chosen per layer (level 0 included), reverse edges
+//     appended while a list has room and re-chosen by Alg. 4 from the old
+//     list plus the new node when it is full (cap 2M at level 0, M above);
+//   * upper-layer blocks laid out in input order.
+// With one thread the saved file is byte for byte the reference's (tested);
+// with more threads, as there, the graph depends on thread timing.
+//
+// Design.  insert_batch stores the batch first -- vectors prepared, every
+// level drawn and every upper block placed, with one exact resize -- and
+// then workers pull node ids from a shared counter, each with its own
+// Inserter: visited stamps, a candidate heap and a result list kept sorted,
+// and the buffers of one insertion.  Lists are read and written under the
+// node's stripe lock; the entry point and top level under top_mutex, held
+// for a whole insertion only by a node that becomes the new top.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <exception>
-#include <limits>
+#include <functional>
+#include <queue>
 #include <stdexcept>
 #include <string>
 #include <thread>
-#include <unordered_set>
 
 #include "graph.hpp"
 
-namespace hnsw {
-
-using gb::Cand;
-using gb::CloserFirst;
-using gb::FartherFirst;
-
+namespace hnsw::gb {
 namespace {
 
-/// splitmix64: portable level generator (index.cpp:20-28).
-inline uint64_t splitmix64(uint64_t& s) noexcept {
-  uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+// one splitmix64 step (the reference's level source, src/index.cpp:20-28)
+uint64_t mix_next(uint64_t& state) noexcept {
+  uint64_t z = (state += 0x9E3779B97F4A7C15ULL);
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
   return z ^ (z >> 31);
 }
 
-/// prepare_vector (space.hpp:31-40): copy, or scale to unit length for cosine.
-void prepare(Metric m, const float* src, float* dst, std::size_t dim) {
+// the level of a node from one draw: u = 1 - (draw >> 11) 2^-53 in (0, 1]
+int level_from(uint64_t draw, double mL) {
+  const double u = 1.0 - std::ldexp(static_cast<double>(draw >> 11), -53);
+  const double l = std::floor(-std::log(u) * mL);
+  return l >= kMaxLevel ? kMaxLevel : static_cast<int>(l);
+}
+
+// space.hpp:31-40: a copy, or for cosine the unit vector with the norm
+// accumulated in double in element order
+void prepare_row(Metric m, const float* src, float* dst, std::size_t dim) {
   if (m != Metric::Cosine) {
     std::copy(src, src + dim, dst);
     return;
   }
-  double norm = 0.0;
-  for (std::size_t i = 0; i < dim; ++i) norm += static_cast<double>(src[i]) * src[i];
-  const float inv = norm > 0.0 ? static_cast<float>(1.0 / std::sqrt(norm)) : 1.0f;
-  for (std::size_t i = 0; i < dim; ++i) dst[i] = src[i] * inv;
+  double ss = 0.0;
+  for (std::size_t i = 0; i < dim; ++i) ss += static_cast<double>(src[i]) * src[i];
+  const float scale = ss > 0.0 ? static_cast<float>(1.0 / std::sqrt(ss)) : 1.0f;
+  for (std::size_t i = 0; i < dim; ++i) dst[i] = src[i] * scale;
 }
 
-/// Work sharing over [0, n) with the first exception rethrown after join
-/// (threadpool.cpp:18-52).
-template <typename Fn>
-void parallel_range(std::size_t n, std::size_t threads, Fn&& fn) {
-  if (n == 0) return;
-  if (threads == 0) {
-    const unsigned hw = std::thread::hardware_concurrency();
-    threads = hw ? hw : 1;
-  }
-  threads = std::min(threads, n);
-  if (threads == 1) {
-    for (std::size_t i = 0; i < n; ++i) fn(i);
-    return;
-  }
-  std::atomic<std::size_t> next{0};
-  std::atomic<bool> failed{false};
-  std::exception_ptr err;
-  std::mutex err_mu;
-  auto worker = [&]() {
-    try {
-      while (!failed.load(std::memory_order_relaxed)) {
-        const std::size_t i = next.fetch_add(1, std::memory_order_relaxed);
-        if (i >= n) break;
-        fn(i);
-      }
-    } catch (...) {
-      std::lock_guard<std::mutex> g(err_mu);
-      if (!err) err = std::current_exception();
-      failed.store(true);
+class Inserter {
+ public:
+  explicit Inserter(Index::Impl& g) : g_(g), stamp_(g.capacity, 0u) {}
+
+  // Alg. 1 for node id, whose vector and level are stored already
+  void run(uint32_t id) {
+    const int level = g_.levels[id];
+    const float* q = g_.vec(id);
+    std::unique_lock<std::mutex> top(g_.top_mutex);
+    const uint32_t ep = g_.entry_point;
+    const int top_level = g_.max_level;
+    if (ep == kNoNode) {  // the first node
+      g_.entry_point = id;
+      g_.max_level = level;
+      return;
     }
-  };
-  std::vector<std::thread> pool;
-  pool.reserve(threads - 1);
-  for (std::size_t t = 1; t < threads; ++t) pool.emplace_back(worker);
-  worker();
-  for (auto& t : pool) t.join();
-  if (err) std::rethrow_exception(err);
-}
-
-/// Copy of a neighbour list taken under its stripe lock.
-void snapshot(const Index::Impl& im, uint32_t id, int level, std::vector<uint32_t>& out) {
-  std::lock_guard<std::mutex> g(im.lock_of(id));
-  const uint32_t* l = im.list(id, level);
-  out.assign(l + 1, l + 1 + l[0]);
-}
-
-/// Greedy single-best descent on one layer (first strict improvement wins).
-Cand descend(const Index::Impl& im, const float* q, Cand cur, int level, std::vector<uint32_t>& buf) {
-  for (bool moved = true; moved;) {
-    moved = false;
-    snapshot(im, cur.id, level, buf);
-    for (uint32_t nb : buf) {
-      const float d = im.dist(q, im.vec(nb));
-      if (d < cur.dist) {
-        cur = Cand{d, nb};
-        moved = true;
-      }
+    if (level <= top_level) top.unlock();
+    Cand at{dist_to(q, ep), ep};
+    for (int lc = top_level; lc > level; --lc) at = greedy(q, at, lc);
+    entries_.assign(1, at);
+    for (int lc = std::min(level, top_level); lc >= 0; --lc) {
+      layer_search(q, lc);
+      found_.erase(std::remove_if(found_.begin(), found_.end(), [id](const Cand& c) { return c.id == id; }),
+                   found_.end());
+      select(found_, g_.M, chosen_);
+      link_forward(id, lc);
+      link_backward(id, lc);
+      entries_.swap(found_);
+    }
+    if (level > top_level) {  // still holding top_mutex
+      g_.entry_point = id;
+      g_.max_level = level;
     }
   }
-  return cur;
-}
 
-/// Beam search on one layer from several entry points (Alg. 2, unfiltered);
-/// leaves the ef best in s.res as a heap.
-void beam(const Index::Impl& im, const float* q, const std::vector<Cand>& eps, std::size_t ef, int level,
-          gb::BuildScratch& s) {
-  s.begin(im.capacity);
-  auto& cand = s.cand;
-  auto& res = s.res;
-  cand.clear();
-  res.clear();
-  for (const Cand& e : eps) {
-    if (s.mark[e.id] == s.epoch) continue;
-    s.mark[e.id] = s.epoch;
-    cand.push_back(e);
-    res.push_back(e);
+ private:
+  float dist_to(const float* q, uint32_t id) const { return g_.dist(q, g_.vec(id)); }
+
+  // a copy of node's list at level, taken under its lock
+  void read_list(uint32_t node, int level) {
+    std::lock_guard<std::mutex> g(g_.lock_of(node));
+    const uint32_t* l = g_.list(node, level);
+    nbrs_.assign(l + 1, l + 1 + l[0]);
   }
-  std::make_heap(cand.begin(), cand.end(), FartherFirst{});
-  std::make_heap(res.begin(), res.end(), CloserFirst{});
-  while (res.size() > ef) {
-    std::pop_heap(res.begin(), res.end(), CloserFirst{});
-    res.pop_back();
+
+  // greedy descent: the first strictly closer neighbour in list order moves
+  // the walk, until a pass over the list moves nothing
+  Cand greedy(const float* q, Cand at, int level) {
+    bool moved = true;
+    while (moved) {
+      moved = false;
+      read_list(at.id, level);
+      for (uint32_t nb : nbrs_) {
+        const float d = dist_to(q, nb);
+        if (d < at.dist) {
+          at = Cand{d, nb};
+          moved = true;
+        }
+      }
+    }
+    return at;
   }
-  while (!cand.empty()) {
-    const Cand c = cand.front();
-    if (res.size() >= ef && c.dist > res.front().dist) break;
-    std::pop_heap(cand.begin(), cand.end(), FartherFirst{});
-    cand.pop_back();
-    snapshot(im, c.id, level, s.nbuf);
-    for (uint32_t id : s.nbuf) {
-      if (s.mark[id] == s.epoch) continue;
-      s.mark[id] = s.epoch;
-      const float d = im.dist(q, im.vec(id));
-      if (res.size() < ef || d < res.front().dist) {
-        cand.push_back(Cand{d, id});
-        std::push_heap(cand.begin(), cand.end(), FartherFirst{});
-        res.push_back(Cand{d, id});
-        std::push_heap(res.begin(), res.end(), CloserFirst{});
-        if (res.size() > ef) {
-          std::pop_heap(res.begin(), res.end(), CloserFirst{});
-          res.pop_back();
+
+  void next_stamp() {
+    if (stamp_.size() < g_.capacity) stamp_.resize(g_.capacity, 0u);
+    if (++stamp_id_ == 0) {  // wrapped: every old stamp must read as unvisited
+      std::fill(stamp_.begin(), stamp_.end(), 0u);
+      stamp_id_ = 1;
+    }
+  }
+  bool seen(uint32_t id) {
+    if (stamp_[id] == stamp_id_) return true;
+    stamp_[id] = stamp_id_;
+    return false;
+  }
+
+  // keep found_ sorted by (distance, id) with at most ef entries
+  void offer(const Cand& c, std::size_t ef) {
+    found_.insert(std::upper_bound(found_.begin(), found_.end(), c, closer), c);
+    if (found_.size() > ef) found_.pop_back();
+  }
+
+  // Alg. 2 (unfiltered) from entries_ on one layer; found_ ends sorted
+  void layer_search(const float* q, int level) {
+    const std::size_t ef = g_.ef_construction;
+    next_stamp();
+    found_.clear();
+    open_ = {};
+    for (const Cand& e : entries_) {
+      if (seen(e.id)) continue;
+      open_.push(e);
+      offer(e, ef);
+    }
+    while (!open_.empty()) {
+      const Cand c = open_.top();
+      if (found_.size() >= ef && c.dist > found_.back().dist) break;
+      open_.pop();
+      read_list(c.id, level);
+      for (uint32_t nb : nbrs_) {
+        if (seen(nb)) continue;
+        const float d = dist_to(q, nb);
+        if (found_.size() < ef || d < found_.back().dist) {
+          open_.push(Cand{d, nb});
+          offer(Cand{d, nb}, ef);
         }
       }
     }
   }
-}
 
-/// Alg. 4 without extension / pruned-keeping: scan `sorted` by distance and
-/// keep e unless some kept r is closer to e than e is to the base.
-void heuristic(const Index::Impl& im, const std::vector<Cand>& sorted, std::size_t m, std::vector<Cand>& out) {
-  out.clear();
-  for (const Cand& e : sorted) {
-    if (out.size() >= m) break;
-    const float* ev = im.vec(e.id);
-    bool keep = true;
-    for (const Cand& r : out) {
-      if (im.dist(ev, im.vec(r.id)) < e.dist) {
-        keep = false;
-        break;
-      }
+  // Alg. 4: from candidates sorted by (distance, id), keep one unless a kept
+  // neighbour is strictly closer to it than the base node is
+  void select(const std::vector<Cand>& sorted, std::size_t m, std::vector<Cand>& out) const {
+    out.clear();
+    for (const Cand& c : sorted) {
+      if (out.size() >= m) break;
+      const float* cv = g_.vec(c.id);
+      const bool dominated =
+          std::any_of(out.begin(), out.end(), [&](const Cand& k) { return g_.dist(cv, g_.vec(k.id)) < c.dist; });
+      if (!dominated) out.push_back(c);
     }
-    if (keep) out.push_back(e);
   }
-}
 
-/// Write id's list on `level` and add reverse edges, re-pruning full lists
-/// (Alg. 1 lines 11-16; index.cpp:145-201).
-void wire(Index::Impl& im, uint32_t id, int level, const std::vector<Cand>& chosen) {
-  const std::size_t cap = im.degree_cap(level);
-  std::vector<Cand> pool, kept;
-  {
-    std::lock_guard<std::mutex> g(im.lock_of(id));
-    uint32_t* l = im.list(id, level);
-    if (l[0] == 0) {
-      l[0] = static_cast<uint32_t>(chosen.size());
-      for (std::size_t i = 0; i < chosen.size(); ++i) l[1 + i] = chosen[i].id;
-    } else {
-      // a concurrent inserter linked to us first: merge, never overwrite
-      const float* q = im.vec(id);
-      pool.assign(chosen.begin(), chosen.end());
-      for (uint32_t j = 0; j < l[0]; ++j) {
-        const uint32_t e = l[1 + j];
-        bool seen = false;
-        for (const Cand& c : pool) seen = seen || c.id == e;
-        if (!seen) pool.push_back(Cand{im.dist(q, im.vec(e)), e});
+  // the node's own list: the chosen neighbours, merged with edges that a
+  // concurrent insertion added first (parallel builds) and re-chosen if full
+  void link_forward(uint32_t id, int level) {
+    const std::size_t cap = g_.degree_cap(level);
+    std::lock_guard<std::mutex> g(g_.lock_of(id));
+    uint32_t* l = g_.list(id, level);
+    if (l[0] != 0) {
+      const float* q = g_.vec(id);
+      pool_.assign(chosen_.begin(), chosen_.end());
+      for (uint32_t j = 1; j <= l[0]; ++j) {
+        const uint32_t e = l[j];
+        if (std::none_of(pool_.begin(), pool_.end(), [e](const Cand& c) { return c.id == e; }))
+          pool_.push_back(Cand{dist_to(q, e), e});
       }
-      std::sort(pool.begin(), pool.end(), CloserFirst{});
-      if (pool.size() > cap) {
-        heuristic(im, pool, cap, kept);
-        pool.swap(kept);
+      std::sort(pool_.begin(), pool_.end(), closer);
+      if (pool_.size() > cap) {
+        select(pool_, cap, kept_);
+        pool_.swap(kept_);
       }
-      l[0] = static_cast<uint32_t>(pool.size());
-      for (std::size_t i = 0; i < pool.size(); ++i) l[1 + i] = pool[i].id;
+      write(l, pool_);
+      return;
+    }
+    write(l, chosen_);
+  }
+
+  // reverse edges: appended while there is room, else the full list plus
+  // the new node re-chosen by Alg. 4
+  void link_backward(uint32_t id, int level) {
+    const std::size_t cap = g_.degree_cap(level);
+    for (const Cand& nb : chosen_) {
+      std::lock_guard<std::mutex> g(g_.lock_of(nb.id));
+      uint32_t* l = g_.list(nb.id, level);
+      const uint32_t n = l[0];
+      if (std::find(l + 1, l + 1 + n, id) != l + 1 + n) continue;
+      if (n < cap) {
+        l[1 + n] = id;
+        l[0] = n + 1;
+        continue;
+      }
+      const float* nv = g_.vec(nb.id);
+      pool_.assign(1, Cand{nb.dist, id});
+      for (uint32_t j = 1; j <= n; ++j) pool_.push_back(Cand{g_.dist(nv, g_.vec(l[j])), l[j]});
+      std::sort(pool_.begin(), pool_.end(), closer);
+      select(pool_, cap, kept_);
+      write(l, kept_);
     }
   }
-  for (const Cand& nb : chosen) {
-    std::lock_guard<std::mutex> g(im.lock_of(nb.id));
-    uint32_t* l = im.list(nb.id, level);
-    const uint32_t n = l[0];
-    bool present = false;
-    for (uint32_t j = 0; j < n; ++j) present = present || l[1 + j] == id;
-    if (present) continue;
-    if (n < cap) {
-      l[1 + n] = id;
-      l[0] = n + 1;
-      continue;
-    }
-    const float* nv = im.vec(nb.id);
-    pool.clear();
-    pool.push_back(Cand{nb.dist, id});
-    for (uint32_t j = 0; j < n; ++j) pool.push_back(Cand{im.dist(nv, im.vec(l[1 + j])), l[1 + j]});
-    std::sort(pool.begin(), pool.end(), CloserFirst{});
-    heuristic(im, pool, cap, kept);
-    l[0] = static_cast<uint32_t>(kept.size());
-    for (std::size_t j = 0; j < kept.size(); ++j) l[1 + j] = kept[j].id;
+
+  static void write(uint32_t* l, const std::vector<Cand>& v) {
+    l[0] = static_cast<uint32_t>(v.size());
+    for (std::size_t i = 0; i < v.size(); ++i) l[1 + i] = v[i].id;
   }
+
+  Index::Impl& g_;
+  std::vector<uint32_t> stamp_;
+  uint32_t stamp_id_ = 0;
+  std::vector<uint32_t> nbrs_;
+  std::vector<Cand> entries_, found_, chosen_, pool_, kept_;
+  std::priority_queue<Cand, std::vector<Cand>, FartherFirst> open_;  // closest on top
+};
+
+// Store the batch: rows prepared, levels drawn in input order, upper blocks
+// placed after the ones in use; returns the first new id.
+uint32_t store_batch(Index::Impl& g, const float* vecs, const uint64_t* labels, std::size_t n) {
+  const std::size_t need = g.count + n;
+  if (need > g.capacity) {
+    if (g.params.max_elements > 0)
+      throw std::runtime_error("Index is full (max_elements = " + std::to_string(g.params.max_elements) + ")");
+    g.grow(std::max<std::size_t>(need, g.capacity + g.capacity / 2 + 1024));
+  }
+  const auto first = static_cast<uint32_t>(g.count);
+  std::size_t upper_need = g.upper_used;
+  for (std::size_t i = 0; i < n; ++i) {
+    const uint32_t id = first + static_cast<uint32_t>(i);
+    const int level = level_from(mix_next(g.rng_state), g.mL);
+    g.level_store[id] = static_cast<uint8_t>(level);
+    if (level > 0) {
+      g.upper_offset[id] = upper_need;
+      upper_need += static_cast<std::size_t>(level) * g.upper_stride;
+    }
+  }
+  if (upper_need > g.upper_store.size()) {
+    g.upper_store.resize(upper_need, 0u);
+    g.upper = g.upper_store.data();
+  }
+  g.upper_used = upper_need;
+  g.label_to_id.reserve(need);
+  for (std::size_t i = 0; i < n; ++i) {
+    const uint32_t id = first + static_cast<uint32_t>(i);
+    prepare_row(g.params.metric, vecs + i * g.dim, g.vec_store.data() + std::size_t{id} * g.padded_dim, g.dim);
+    g.label_store[id] = labels[i];
+    g.list0(id)[0] = 0;
+    g.label_to_id.emplace(labels[i], id);
+  }
+  g.count = need;
+  return first;
 }
 
 }  // namespace
 
-// ---------------------------------------------------------------------------
-// Impl
-// ---------------------------------------------------------------------------
-
-Index::Impl::Impl(const Params& p) : params(p) {
-  if (p.dim == 0) throw std::invalid_argument("Index: dim must be > 0");
-  if (p.M < 2) throw std::invalid_argument("Index: M must be >= 2");
-  if (p.M > 2048) throw std::invalid_argument("Index: M must be <= 2048");
-  if (p.ef_construction == 0) throw std::invalid_argument("Index: ef_construction must be > 0");
-  if (p.max_elements > std::numeric_limits<uint32_t>::max() - 1)
-    throw std::invalid_argument("Index: max_elements exceeds the 32-bit internal id space");
-  dim = p.dim;
-  padded_dim = gb::round_up(dim, gb::kPadFloats);
-  M = p.M;
-  M0 = 2 * p.M;
-  ef_construction = std::max(p.ef_construction, p.M);
-  mL = 1.0 / std::log(static_cast<double>(M));
-  l0_stride = 1 + M0;
-  upper_stride = 1 + M;
-  const simd::Kernels& k = simd::active();
-  isa = k.isa;
-  is_l2 = p.metric == Metric::L2;
-  kernel = is_l2 ? k.l2_sq : k.dot;
-  rng_state = p.seed;
-  if (p.max_elements > 0) grow(p.max_elements);
-}
-
-Index::Impl::~Impl() {
-  if (dev) hgd_graph_free(dev);
-}
-
-void Index::Impl::bind_pointers() {
-  vecs = vec_store.data();
-  l0 = l0_store.data();
-  upper = upper_store.data();
-  labels = label_store.data();
-  levels = level_store.data();
-}
-
-void Index::Impl::grow(std::size_t n) {
-  if (n <= capacity) return;
-  if (read_only) throw std::runtime_error("index is read-only (memory-mapped)");
-  if (n > std::numeric_limits<uint32_t>::max() - 1)
-    throw std::runtime_error("Index: capacity exceeds the 32-bit internal id space");
-  vec_store.resize(n * padded_dim, 0.0f);
-  l0_store.resize(n * l0_stride, 0u);
-  label_store.resize(n, 0);
-  level_store.resize(n, 0);
-  upper_offset.resize(n, 0);
-  deleted.resize(n, 0);
-  capacity = n;
-  bind_pointers();
-}
-
-int Index::Impl::draw_level() {
-  const double u = 1.0 - static_cast<double>(splitmix64(rng_state) >> 11) * 0x1.0p-53;  // (0, 1]
-  const double lvl = std::floor(-std::log(u) * mL);
-  return static_cast<int>(std::min(lvl, static_cast<double>(gb::kMaxLevel)));
-}
-
-uint32_t Index::Impl::append(const float* v, uint64_t label) {
-  const auto id = static_cast<uint32_t>(count);
-  prepare(params.metric, v, vec_store.data() + std::size_t{id} * padded_dim, dim);
-  label_store[id] = label;
-  const int level = draw_level();
-  level_store[id] = static_cast<uint8_t>(level);
-  if (level > 0) {
-    upper_offset[id] = upper_used;
-    upper_used += static_cast<std::size_t>(level) * upper_stride;
-    if (upper_store.size() < upper_used) {
-      upper_store.resize(std::max(upper_used, upper_store.size() * 2), 0u);
-      upper = upper_store.data();
+void insert_batch(Index::Impl& g, const float* vecs, const uint64_t* labels, std::size_t n, std::size_t threads) {
+  const uint32_t first = store_batch(g, vecs, labels, n);
+  if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
+  threads = std::min(threads, n);
+  std::atomic<std::size_t> next{0};
+  std::atomic<bool> stop{false};
+  std::exception_ptr err;
+  std::mutex err_mu;
+  auto worker = [&]() {
+    try {
+      Inserter ins(g);
+      for (std::size_t i = next++; i < n && !stop.load(std::memory_order_relaxed); i = next++)
+        ins.run(first + static_cast<uint32_t>(i));
+    } catch (...) {
+      std::lock_guard<std::mutex> lk(err_mu);
+      if (!err) err = std::current_exception();
+      stop = true;
     }
-  }
-  list0(id)[0] = 0;
-  label_to_id.emplace(label, id);
-  ++count;
-  return id;
+  };
+  std::vector<std::thread> pool;
+  for (std::size_t t = 1; t < threads; ++t) pool.emplace_back(worker);
+  worker();  // the calling thread works too
+  for (auto& t : pool) t.join();
+  if (err) std::rethrow_exception(err);
 }
 
-std::unique_ptr<gb::BuildScratch> Index::Impl::take_scratch() {
-  std::lock_guard<std::mutex> g(scratch_mutex);
-  if (scratch_free.empty()) return std::make_unique<gb::BuildScratch>();
-  auto s = std::move(scratch_free.back());
-  scratch_free.pop_back();
-  return s;
-}
-
-void Index::Impl::give_scratch(std::unique_ptr<gb::BuildScratch> s) {
-  std::lock_guard<std::mutex> g(scratch_mutex);
-  scratch_free.push_back(std::move(s));
-}
-
-void Index::Impl::link(uint32_t id) {
-  const int level = levels[id];
-  const float* q = vec(id);
-  std::unique_lock<std::mutex> top(top_mutex);
-  const uint32_t ep = entry_point;
-  const int top_level = max_level;
-  if (ep == gb::kNoNode) {
-    entry_point = id;
-    max_level = level;
-    return;
-  }
-  if (level <= top_level) top.unlock();  // only a new top node keeps the lock
-  auto s = take_scratch();
-  Cand cur{dist(q, vec(ep)), ep};
-  for (int lc = top_level; lc > level; --lc) cur = descend(*this, q, cur, lc, s->nbuf);
-  std::vector<Cand> eps{cur}, w, chosen;
-  for (int lc = std::min(level, top_level); lc >= 0; --lc) {
-    beam(*this, q, eps, ef_construction, lc, *s);
-    w.assign(s->res.begin(), s->res.end());
-    std::sort(w.begin(), w.end(), CloserFirst{});
-    w.erase(std::remove_if(w.begin(), w.end(), [id](const Cand& c) { return c.id == id; }), w.end());
-    heuristic(*this, w, M, chosen);
-    wire(*this, id, lc, chosen);
-    eps.swap(w);
-  }
-  give_scratch(std::move(s));
-  if (level > top_level) {
-    entry_point = id;
-    max_level = level;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// public construction / mutation API
-// ---------------------------------------------------------------------------
-
-Index::Index(const Params& params) : impl_(std::make_unique<Impl>(params)) {}
-Index::Index(std::unique_ptr<Impl> impl) : impl_(std::move(impl)) {}
-Index::~Index() = default;
-Index::Index(Index&&) noexcept = default;
-Index& Index::operator=(Index&&) noexcept = default;
-
-void Index::add(const float* vec, uint64_t label) { add_batch(vec, &label, 1, 1); }
-
-void Index::add_batch(const float* vecs, const uint64_t* labels, std::size_t n, std::size_t num_threads) {
-  if (n == 0) return;
-  if (vecs == nullptr || labels == nullptr) throw std::invalid_argument("add_batch: null input");
-  std::unique_lock<std::shared_mutex> lk(impl_->api_mutex);
-  Impl& im = *impl_;
-  if (im.read_only) throw std::runtime_error("index is read-only (memory-mapped); load without mmap to modify");
-  if (n > 1) {
-    std::unordered_set<uint64_t> seen;
-    seen.reserve(n);
-    for (std::size_t i = 0; i < n; ++i)
-      if (!seen.insert(labels[i]).second)
-        throw std::invalid_argument("add_batch: duplicate label " + std::to_string(labels[i]) + " in batch");
-  }
-  for (std::size_t i = 0; i < n; ++i)
-    if (im.label_to_id.count(labels[i]) != 0)
-      throw std::invalid_argument("add: label " + std::to_string(labels[i]) + " already exists");
-  const std::size_t need = im.count + n;
-  if (need > im.capacity) {
-    if (im.params.max_elements > 0)
-      throw std::runtime_error("Index is full (max_elements = " + std::to_string(im.params.max_elements) + ")");
-    im.grow(std::max({need, im.capacity * 2, std::size_t{1024}}));
-  }
-  im.label_to_id.reserve(im.count + n);
-  const auto first = static_cast<uint32_t>(im.count);
-  for (std::size_t i = 0; i < n; ++i) im.append(vecs + i * im.dim, labels[i]);
-  parallel_range(n, num_threads, [&](std::size_t i) { im.link(first + static_cast<uint32_t>(i)); });
-  std::lock_guard<std::mutex> g(im.dev_mutex);
-  im.dev_stale = true;
-}
-
-void Index::mark_deleted(uint64_t label) {
-  std::unique_lock<std::shared_mutex> lk(impl_->api_mutex);
-  Impl& im = *impl_;
-  auto it = im.label_to_id.find(label);
-  if (it == im.label_to_id.end()) throw std::invalid_argument("mark_deleted: unknown label " + std::to_string(label));
-  if (im.deleted[it->second] == 0) {
-    im.deleted[it->second] = 1;
-    ++im.num_deleted;
-    std::lock_guard<std::mutex> g(im.dev_mutex);
-    if (im.dev && !im.dev_stale && hgd_graph_set_deleted(im.dev, it->second, 1) != HGD_OK)
-      throw std::runtime_error(std::string("mark_deleted: ") + hgd_last_error());
-  }
-}
-
-bool Index::is_deleted(uint64_t label) const {
-  std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
-  auto it = impl_->label_to_id.find(label);
-  return it != impl_->label_to_id.end() && impl_->deleted[it->second] != 0;
-}
-
-bool Index::contains(uint64_t label) const {
-  std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
-  return impl_->label_to_id.count(label) != 0;
-}
-
-std::size_t Index::size() const {
-  std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
-  return impl_->count;
-}
-std::size_t Index::dim() const noexcept { return impl_->dim; }
-Metric Index::metric() const noexcept { return impl_->params.metric; }
-const Params& Index::params() const noexcept { return impl_->params; }
-std::size_t Index::capacity() const {
-  std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
-  return impl_->capacity;
-}
-std::size_t Index::ef() const {
-  std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
-  return impl_->ef_search;
-}
-void Index::set_ef(std::size_t ef) {
-  if (ef == 0) throw std::invalid_argument("set_ef: ef must be > 0");
-  std::unique_lock<std::shared_mutex> lk(impl_->api_mutex);
-  impl_->ef_search = ef;
-}
-int Index::max_level() const {
-  std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
-  return impl_->max_level;
-}
-bool Index::read_only() const noexcept { return impl_->read_only; }
-
-std::size_t Index::memory_usage() const {
-  std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
-  const Impl& im = *impl_;
-  return im.count * (im.padded_dim * sizeof(float) + im.l0_stride * sizeof(uint32_t) + sizeof(uint64_t) * 2 + 2) +
-         im.upper_used * sizeof(uint32_t);
-}
-
-std::vector<float> Index::get_vector(uint64_t label) const {
-  std::shared_lock<std::shared_mutex> lk(impl_->api_mutex);
-  auto it = impl_->label_to_id.find(label);
-  if (it == impl_->label_to_id.end()) throw std::invalid_argument("get_vector: unknown label");
-  const float* v = impl_->vec(it->second);
-  return std::vector<float>(v, v + impl_->dim);
-}
-
-namespace tuning {
-namespace {
-std::atomic<bool> g_prefetch{true};
-}
-void set_prefetch(bool enabled) noexcept { g_prefetch.store(enabled); }
-bool prefetch_enabled() noexcept { return g_prefetch.load(); }
-}  // namespace tuning
-
-}  // namespace hnsw
+}  // namespace hnsw::gb

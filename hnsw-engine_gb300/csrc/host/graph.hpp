@@ -85,24 +85,6 @@ class Mapping {
   std::size_t size_ = 0;
 };
 
-/// Per-thread scratch of the CPU builder (the graph search during insertion).
-struct BuildScratch {
-  std::vector<uint32_t> mark;
-  uint32_t epoch = 0;
-  std::vector<Cand> cand, res, tmp;
-  std::vector<uint32_t> nbuf;
-  void begin(std::size_t n) {
-    if (mark.size() < n) {
-      mark.assign(n, 0);
-      epoch = 0;
-    }
-    if (++epoch == 0) {
-      std::fill(mark.begin(), mark.end(), 0u);
-      epoch = 1;
-    }
-  }
-};
-
 }  // namespace hnsw::gb
 
 namespace hnsw {
@@ -139,10 +121,8 @@ struct Index::Impl {
   bool read_only = false;
 
   mutable std::shared_mutex api_mutex;
-  std::mutex top_mutex;
+  std::mutex top_mutex;  // entry point and top level during construction
   std::unique_ptr<std::mutex[]> stripes{new std::mutex[gb::kStripes]};
-  std::mutex scratch_mutex;
-  std::vector<std::unique_ptr<gb::BuildScratch>> scratch_free;
 
   // GPU mirror (rebuilt lazily after add; tombstones are patched in place)
   int device = 0;
@@ -168,13 +148,6 @@ struct Index::Impl {
   std::mutex& lock_of(uint32_t id) const noexcept { return stripes[id & (gb::kStripes - 1)]; }
   void bind_pointers();
   void grow(std::size_t n);
-
-  // construction (build.cpp)
-  int draw_level();
-  uint32_t append(const float* v, uint64_t label);
-  void link(uint32_t id);
-  std::unique_ptr<gb::BuildScratch> take_scratch();
-  void give_scratch(std::unique_ptr<gb::BuildScratch> s);
 
   // device mirror (index.cpp)
   hgd_graph* device_graph() const;
@@ -211,6 +184,10 @@ inline void to_bits(const Index::Impl& im, const Filter* f, FilterBits& out) {
 }  // namespace hnsw::gb
 
 namespace hnsw::gb {
+
+// CPU graph construction (build.cpp): stores a validated batch and links it
+// into the graph with `threads` workers (0 = all hardware threads)
+void insert_batch(Index::Impl& g, const float* vecs, const uint64_t* labels, std::size_t n, std::size_t threads);
 
 // launch-shape autotuner (tune.cpp): times candidate shapes per ef bucket on
 // a sample of queries, installs the fastest and returns the table as JSON
