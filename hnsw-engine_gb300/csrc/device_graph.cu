@@ -30,16 +30,16 @@ namespace hg {
 int slots_for(uint32_t pd);
 cudaError_t launch_inv_norm(const float* qs, uint32_t nq, uint32_t dim, float* out, cudaStream_t st);
 cudaError_t launch_search(const SearchParams& P, const float* inv, int blocks, int warps_per_block, cudaStream_t st);
-int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, uint32_t R, uint32_t C);
+int search_occupancy(uint32_t pd, int metric, int order, int warps_per_block, uint32_t H, uint32_t R, uint32_t C);
 cudaError_t launch_search_approx(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st);
-int occupancy_approx(uint32_t pdc, int metric, int prec, int wpb, size_t smem);
+int occupancy_approx(uint32_t pdc, int metric, int prec, int order, int wpb, size_t smem);
 cudaError_t launch_search_wide(const SearchParams& P, const float* inv, int blocks, cudaStream_t st);
-int occupancy_wide(int metric, int prec, uint32_t R);
+int occupancy_wide(int metric, int prec, int order, uint32_t R);
 cudaError_t launch_encode(const float* vecs, uint32_t n, uint32_t pd, uint32_t pdc, int prec, void* out,
                           float* scale, float* aux, cudaStream_t st);
 cudaError_t launch_search_beam(const SearchParams& P, const float* inv, int blocks, int wpb, bool filt,
                                cudaStream_t st);
-int occupancy_beam(int metric, int prec, int wpb, size_t smem, bool filt);
+int occupancy_beam(int metric, int prec, int order, int wpb, size_t smem, bool filt);
 cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, uint32_t ef_all, uint32_t ef_default,
                           uint32_t k_all, const BucketSpec& spec, uint32_t* counts, uint32_t* lists, cudaStream_t st,
                           const uint8_t* skip);
@@ -298,8 +298,8 @@ const char* hgd_last_error(void) { return g_err.c_str(); }
 
 int hgd_graph_upload(const hgd_graph_view* v, int device, int order, hgd_graph** out) {
   if (!v || !out) return fail(HGD_EINVAL, "hgd_graph_upload: null argument");
-  if (order != HGD_ORDER_AVX512)
-    return fail(HGD_EINVAL, "hgd_graph_upload: only the AVX-512 summation order is implemented on the GPU");
+  if (order != HGD_ORDER_AVX512 && order != HGD_ORDER_NEON)
+    return fail(HGD_EINVAL, "hgd_graph_upload: the GPU implements the AVX-512 and NEON summation orders only");
   if (v->count >= 0xFFFFFFFFull) return fail(HGD_EINVAL, "hgd_graph_upload: count exceeds 32-bit ids");
   if (v->padded_dim % 16 != 0 || v->padded_dim < v->dim || v->dim == 0)
     return fail(HGD_EINVAL, "hgd_graph_upload: padded_dim must be dim rounded up to 16");
@@ -395,8 +395,8 @@ int hgd_graph_upload(const hgd_graph_view* v, int device, int order, hgd_graph**
 
 int hgd_graph_set_order(hgd_graph* g, int order) {
   if (!g) return fail(HGD_EINVAL, "hgd_graph_set_order: null graph");
-  if (order != HGD_ORDER_AVX512)
-    return fail(HGD_EINVAL, "hgd_graph_set_order: only the AVX-512 summation order is implemented on the GPU");
+  if (order != HGD_ORDER_AVX512 && order != HGD_ORDER_NEON)
+    return fail(HGD_EINVAL, "hgd_graph_set_order: the GPU implements the AVX-512 and NEON summation orders only");
   g->order = order;
   return HGD_OK;
 }
@@ -689,6 +689,7 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   P.tagged = g->n < (1ull << 24) ? 1 : 0;
   P.dedup = g->dedup ? 1 : 0;
   P.deleted_any = g->num_deleted > 0 ? 1 : 0;
+  P.order = g->order == HGD_ORDER_NEON ? 1 : 0;
   P.queries = d_q;
   P.nq = static_cast<uint32_t>(nq);
   P.efq = d_ef;
@@ -799,8 +800,9 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     if (want_wpb) sh.wpb = std::min<int>(sh.wpb, static_cast<int>(want_wpb));
     if (sh.wpb < 1) return fail(HGD_EINVAL, "hgd_search: ef too large for shared memory");
     const int occ = prec == HGD_PREC_FP32
-                        ? hg::search_occupancy(static_cast<uint32_t>(g->pd), g->metric, sh.wpb, sh.H, sh.R, sh.C)
-                        : hg::occupancy_approx(P.pdc, g->metric, prec, sh.wpb,
+                        ? hg::search_occupancy(static_cast<uint32_t>(g->pd), g->metric, P.order, sh.wpb, sh.H, sh.R,
+                                               sh.C)
+                        : hg::occupancy_approx(P.pdc, g->metric, prec, P.order, sh.wpb,
                                                static_cast<size_t>(sh.wpb) * hg::warp_smem_bytes(sh.H, sh.R, sh.C));
     if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the search kernel cannot be resident with this shape");
     const uint64_t want = (nq + sh.wpb - 1) / sh.wpb;
@@ -942,7 +944,7 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     const int wpb = 4;
     const size_t smem = static_cast<size_t>(wpb) * hg::beam_warp_bytes(B.H, B.R, filt);
     if (smem > 227u * 1024u) return fail(HGD_EINVAL, "hgd_search: ef too large for the beam walk's shared memory");
-    const int occ = hg::occupancy_beam(g->metric, prec, wpb, smem, filt);
+    const int occ = hg::occupancy_beam(g->metric, prec, P.order, wpb, smem, filt);
     if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the beam kernel cannot be resident");
     const uint64_t want = (nq + wpb - 1) / wpb;
     const int blocks = static_cast<int>(std::min<uint64_t>(want, static_cast<uint64_t>(g->sms) * occ));
@@ -957,7 +959,7 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     B.lpt_stride = static_cast<uint32_t>(nq);
     B.work = work + 8;
     B.slot_base = 0;
-    const int occ = hg::occupancy_wide(g->metric, prec, B.R);
+    const int occ = hg::occupancy_wide(g->metric, prec, P.order, B.R);
     if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the several-warps kernel cannot be resident");
     const int blocks = static_cast<int>(std::min<uint64_t>(nq, static_cast<uint64_t>(g->sms) * occ));
     cudaError_t e = hg::launch_search_wide(B, d_inv, blocks, st);
@@ -1140,6 +1142,7 @@ int search_noalloc(hgd_graph* g, const float* d_queries, uint64_t nq, uint32_t k
   P.tagged = g->n < (1ull << 24) ? 1 : 0;
   P.dedup = g->dedup ? 1 : 0;
   P.deleted_any = g->num_deleted > 0 ? 1 : 0;
+  P.order = g->order == HGD_ORDER_NEON ? 1 : 0;
   P.queries = d_queries;
   P.nq = static_cast<uint32_t>(nq);
   P.ef_all = e;

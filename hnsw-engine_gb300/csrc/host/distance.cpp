@@ -140,8 +140,15 @@ constexpr Kernels kTable[4] = {
     {Isa::NEON, &k_neon<true>, &k_neon<false>},
 };
 
+// The order the reference picks on this host: NEON on Arm (its only SIMD
+// kernels there), AVX-512 on x86-64 (the widest; the GPU implements those
+// two).  HNSW_SIMD names another, as it does for the reference.
 const Kernels* initial() noexcept {
+#if defined(__aarch64__)
+  const Kernels* k = &kTable[3];
+#else
   const Kernels* k = &kTable[2];
+#endif
   if (const char* env = std::getenv("HNSW_SIMD"); env && *env) {  // NOLINT(concurrency-mt-unsafe)
     try {
       k = &kTable[static_cast<int>(parse_isa(env))];

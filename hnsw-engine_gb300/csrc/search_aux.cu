@@ -14,6 +14,10 @@ cudaError_t launch_search_l2(const SearchParams& P, const float* inv, int blocks
 cudaError_t launch_search_dot(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st);
 int occupancy_l2(uint32_t pd, int wpb, size_t smem);
 int occupancy_dot(uint32_t pd, int wpb, size_t smem);
+cudaError_t launch_search_l2_neon(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st);
+cudaError_t launch_search_dot_neon(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st);
+int occupancy_l2_neon(uint32_t pd, int wpb, size_t smem);
+int occupancy_dot_neon(uint32_t pd, int wpb, size_t smem);
 
 namespace {
 
@@ -96,13 +100,18 @@ cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bi
 // Returns cudaErrorInvalidValue for a padded dimension beyond the register layouts.
 cudaError_t launch_search(const SearchParams& P, const float* inv, int blocks, int warps_per_block,
                           cudaStream_t st) {
+  if (P.order == 1)
+    return P.metric == 0 ? launch_search_l2_neon(P, inv, blocks, warps_per_block, st)
+                         : launch_search_dot_neon(P, inv, blocks, warps_per_block, st);
   return P.metric == 0 ? launch_search_l2(P, inv, blocks, warps_per_block, st)
                        : launch_search_dot(P, inv, blocks, warps_per_block, st);
 }
 
 // Resident blocks per SM of the search kernel for this shape (0 on error).
-int search_occupancy(uint32_t pd, int metric, int warps_per_block, uint32_t H, uint32_t R, uint32_t C) {
+int search_occupancy(uint32_t pd, int metric, int order, int warps_per_block, uint32_t H, uint32_t R, uint32_t C) {
   const size_t smem = static_cast<size_t>(warps_per_block) * warp_smem_bytes(H, R, C);
+  if (order == 1)
+    return metric == 0 ? occupancy_l2_neon(pd, warps_per_block, smem) : occupancy_dot_neon(pd, warps_per_block, smem);
   return metric == 0 ? occupancy_l2(pd, warps_per_block, smem) : occupancy_dot(pd, warps_per_block, smem);
 }
 

@@ -285,7 +285,7 @@ __device__ __forceinline__ int merge_keys(uint64_t*& cur, uint64_t*& oth, int le
 
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-template <int PREC, bool L2, bool FILT>
+template <int PREC, bool L2, bool FILT, int ORD>
 __global__ void __launch_bounds__(128, 6) beam_kernel(SearchParams P, const float* __restrict__ inv_norm) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(128, 6) beam_kernel(SearchParams P, const floa
     for (int j = lane; j < s; j += 32) prow[j] = wkey_id(rarr[j]);
     if (lane == 0) P.pool_n[q] = static_cast<uint32_t>(s);
     __syncwarp();
-    fused_rerank<typename ApproxDist<4, 16, PREC>::Exact, L2>(
+    fused_rerank<typename ApproxDist<4, 16, PREC, ORD>::Exact, L2>(
         P.vecs, P.pd, P.dim, P.queries + static_cast<size_t>(q) * P.dim, inv_norm ? inv_norm[q] : 1.0f,
         inv_norm != nullptr, prow, s, oth, stage, static_cast<int>(P.R), lane);
     const int mk = s < static_cast<int>(k) ? s : static_cast<int>(k);
@@ -589,22 +589,50 @@ __global__ void __launch_bounds__(128, 6) beam_kernel(SearchParams P, const floa
   }
 }
 
-template <int PREC, bool L2, bool FILT>
+template <int PREC, bool L2, bool FILT, int ORD>
 cudaError_t beam_launch_t(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st) {
-  auto* fn = beam_kernel<PREC, L2, FILT>;
+  auto* fn = beam_kernel<PREC, L2, FILT, ORD>;
   cudaError_t e = open_smem_limit(reinterpret_cast<const void*>(fn));
   if (e != cudaSuccess) return e;
   fn<<<blocks, 32 * wpb, static_cast<size_t>(wpb) * beam_warp_bytes(P.H, P.R, FILT), st>>>(P, inv);
   return cudaGetLastError();
 }
 
-template <int PREC, bool L2, bool FILT>
+template <int PREC, bool L2, bool FILT, int ORD>
 int beam_occupancy_t(int wpb, size_t smem) {
   int blocks = 0;
-  auto* fn = beam_kernel<PREC, L2, FILT>;
+  auto* fn = beam_kernel<PREC, L2, FILT, ORD>;
   if (open_smem_limit(reinterpret_cast<const void*>(fn)) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 32 * wpb, smem) != cudaSuccess) return 0;
   return blocks;
+}
+
+template <int ORD>
+cudaError_t beam_launch(const SearchParams& P, const float* inv, int blocks, int wpb, bool filt, cudaStream_t st) {
+  if (P.pdc != 128) return cudaErrorInvalidValue;
+  const bool fp8 = P.vscale != nullptr;
+  if (P.metric == 0) {
+    if (fp8) return filt ? beam_launch_t<2, true, true, ORD>(P, inv, blocks, wpb, st)
+                         : beam_launch_t<2, true, false, ORD>(P, inv, blocks, wpb, st);
+    return filt ? beam_launch_t<1, true, true, ORD>(P, inv, blocks, wpb, st)
+                : beam_launch_t<1, true, false, ORD>(P, inv, blocks, wpb, st);
+  }
+  if (fp8) return filt ? beam_launch_t<2, false, true, ORD>(P, inv, blocks, wpb, st)
+                       : beam_launch_t<2, false, false, ORD>(P, inv, blocks, wpb, st);
+  return filt ? beam_launch_t<1, false, true, ORD>(P, inv, blocks, wpb, st)
+              : beam_launch_t<1, false, false, ORD>(P, inv, blocks, wpb, st);
+}
+
+template <int ORD>
+int beam_occupancy(int metric, int prec, int wpb, size_t smem, bool filt) {
+  if (metric == 0) {
+    if (prec == 2) return filt ? beam_occupancy_t<2, true, true, ORD>(wpb, smem)
+                               : beam_occupancy_t<2, true, false, ORD>(wpb, smem);
+    return filt ? beam_occupancy_t<1, true, true, ORD>(wpb, smem) : beam_occupancy_t<1, true, false, ORD>(wpb, smem);
+  }
+  if (prec == 2) return filt ? beam_occupancy_t<2, false, true, ORD>(wpb, smem)
+                             : beam_occupancy_t<2, false, false, ORD>(wpb, smem);
+  return filt ? beam_occupancy_t<1, false, true, ORD>(wpb, smem) : beam_occupancy_t<1, false, false, ORD>(wpb, smem);
 }
 
 }  // namespace sk

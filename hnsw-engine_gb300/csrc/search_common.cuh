@@ -27,6 +27,7 @@ struct SearchParams {
   int32_t tagged;           // n < 2^24: visited hash slots carry an 8-bit epoch
   int32_t dedup;            // some neighbour list repeats an id
   int32_t deleted_any;      // num_deleted > 0 (reference switches to the filtered variant)
+  int32_t order;            // FP32 summation order: 0 the AVX-512 kernel's, 1 the NEON kernel's
   // ---- batch ----
   const float* queries;     // nq x dim raw
   uint32_t nq;

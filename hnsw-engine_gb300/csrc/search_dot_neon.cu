@@ -1,0 +1,19 @@
+// search_dot_neon.cu -- instantiations of the query kernel for the inner-product / cosine metrics (1 - dot),
+// distances in the NEON kernel's summation order (indexes loaded on Arm
+// hosts, where the reference dispatches to its NEON kernels).
+#include "search_kernel.cuh"
+
+namespace hg {
+
+cudaError_t launch_search_dot_neon(const SearchParams& P, const float* inv, int blocks, int wpb, cudaStream_t st) {
+  const uint32_t pd = P.pd;
+  HG_SEARCH_DISPATCH_NEON(sk::launch_t, false, P, inv, blocks, wpb, st)
+  return cudaErrorInvalidValue;
+}
+
+int occupancy_dot_neon(uint32_t pd, int wpb, size_t smem) {
+  HG_SEARCH_DISPATCH_NEON(sk::occupancy_t, false, wpb, smem)
+  return 0;
+}
+
+}  // namespace hg

@@ -415,31 +415,142 @@ template <int NB, int NT, int S, int G>
 struct ExactDist {
   static constexpr bool kApprox = false;
   static constexpr int kMinBlocks = S >= 16 ? 4 : 6;  // (128, 7) measured 9% slower
-  static constexpr int kSlots = S;
-  template <bool L2>
-  __device__ __forceinline__ static float rows(const Layout<NB, NT, S>& L, const float* __restrict__ vecs, uint32_t pd,
-                                               uint32_t id, uint32_t mask, const float (&qr)[S], int lane) {
-    return lane_dists<NB, NT, S, G, L2>(L, vecs, pd, id, mask, qr, lane);
-  }
   Layout<NB, NT, S> L;
   float qr[S];
-  __device__ __forceinline__ void init(const SearchParams& P) {
-    L.nb_rt = static_cast<int>(P.pd / 64);
-    L.nt_rt = static_cast<int>((P.pd % 64) / 16);
+  __device__ __forceinline__ void setup(uint32_t pd) {
+    L.nb_rt = static_cast<int>(pd / 64);
+    L.nt_rt = static_cast<int>((pd % 64) / 16);
   }
-  __device__ __forceinline__ void load_query(const SearchParams& P, const float* raw, const float* inv_norm,
-                                             uint32_t q, int lane) {
-    const float inv = inv_norm ? inv_norm[q] : 1.0f;
+  // the prepared query (cosine: scaled by inv) in this lane's slots
+  __device__ __forceinline__ void load_raw(const float* raw, uint32_t dim, float inv, bool cosine, int lane) {
 #pragma unroll
     for (int i = 0; i < S; ++i) {
       const int e = L.elem(i, lane);
-      const float v = (e >= 0 && e < static_cast<int>(P.dim)) ? __ldg(raw + e) : 0.0f;
-      qr[i] = inv_norm ? __fmul_rn(v, inv) : v;
+      const float v = (e >= 0 && e < static_cast<int>(dim)) ? __ldg(raw + e) : 0.0f;
+      qr[i] = cosine ? __fmul_rn(v, inv) : v;
     }
   }
   template <bool L2>
+  __device__ __forceinline__ float rows(const float* __restrict__ vecs, uint32_t pd, uint32_t id, uint32_t mask,
+                                        int lane) const {
+    return lane_dists<NB, NT, S, G, L2>(L, vecs, pd, id, mask, qr, lane);
+  }
+  __device__ __forceinline__ void init(const SearchParams& P) { setup(P.pd); }
+  __device__ __forceinline__ void load_query(const SearchParams& P, const float* raw, const float* inv_norm,
+                                             uint32_t q, int lane) {
+    load_raw(raw, P.dim, inv_norm ? inv_norm[q] : 1.0f, inv_norm != nullptr, lane);
+  }
+  template <bool L2>
   __device__ __forceinline__ float dists(const SearchParams& P, uint32_t id, uint32_t mask, int lane) const {
-    return lane_dists<NB, NT, S, G, L2>(L, P.vecs, P.pd, id, mask, qr, lane);
+    return rows<L2>(P.vecs, P.pd, id, mask, lane);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// distances in the NEON kernel's order (src/kernels_neon.cpp:10-54): four
+// 4-lane accumulators over 16-float blocks, so element 16 i + 4 a + b feeds
+// accumulator a, lane b, as a fused chain over i; then (acc0 + acc1) +
+// (acc2 + acc3) per lane and vaddvq_f32's (v0 + v1) + (v2 + v3).  (The
+// 4-float and scalar tails never run: rows are padded to 16 floats.)  On a
+// warp, lane c of each half-warp runs chain c = 4 a + b of one row, so a pass
+// computes two rows; the sums are a 4 / 8 / 1 / 2 xor butterfly inside the
+// half.  NC > 0 fixes the chain length (pd / 16) at compile time, NC < 0
+// reads it at run time with -NC slots; G rows are in flight.  QREG: the
+// query's chain elements live in registers (chains up to 32); otherwise
+// they are re-read from the query row, which stays in L1.
+// ---------------------------------------------------------------------------
+template <int NC, int G, bool QREG = true>
+struct NeonDist {
+  static_assert(G % 2 == 0, "rows go in pairs, one per half-warp");
+  static constexpr bool kApprox = false;
+  static constexpr int kSlots = NC > 0 ? NC : -NC;
+  static constexpr int kMinBlocks = kSlots > 8 ? 4 : 6;
+  int nc_rt;
+  float qr[QREG ? kSlots : 1];
+  const float* qraw;
+  uint32_t qdim;
+  float qinv;
+  bool qcos;
+  __device__ __forceinline__ int nc() const { return NC > 0 ? NC : nc_rt; }
+  __device__ __forceinline__ void setup(uint32_t pd) { nc_rt = static_cast<int>(pd / 16); }
+  __device__ __forceinline__ void load_raw(const float* raw, uint32_t dim, float inv, bool cosine, int lane) {
+    qraw = raw;
+    qdim = dim;
+    qinv = inv;
+    qcos = cosine;
+    if (QREG) {
+      const int c = lane & 15;
+#pragma unroll
+      for (int i = 0; i < kSlots; ++i) qr[QREG ? i : 0] = qelem(16 * i + c, i);
+    }
+  }
+  __device__ __forceinline__ float qelem(int e, int i) const {
+    if (i >= nc() || e >= static_cast<int>(qdim)) return 0.0f;
+    const float v = __ldg(qraw + e);
+    return qcos ? __fmul_rn(v, qinv) : v;
+  }
+  template <bool L2>
+  __device__ __forceinline__ float rows(const float* __restrict__ vecs, uint32_t pd, uint32_t id, uint32_t mask,
+                                        int lane) const {
+    constexpr int S = kSlots;
+    const int c = lane & 15;
+    const int half = lane >> 4;
+    float mine = 0.0f;
+    while (mask) {
+      int gl[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        gl[g] = mask ? __ffs(mask) - 1 : -1;
+        if (mask) mask &= mask - 1;
+      }
+      const float* rp[G / 2];
+#pragma unroll
+      for (int p = 0; p < G / 2; ++p) {
+        const int src = gl[2 * p + half];  // this half-warp's row of pass p
+        const uint32_t rid = __shfl_sync(kFull, id, src < 0 ? 0 : src);
+        rp[p] = src < 0 ? nullptr : vecs + static_cast<size_t>(rid) * pd;
+      }
+      float x[G / 2][S];
+#pragma unroll
+      for (int p = 0; p < G / 2; ++p)
+#pragma unroll
+        for (int i = 0; i < S; ++i) x[p][i] = (rp[p] != nullptr && i < nc()) ? __ldg(rp[p] + 16 * i + c) : 0.0f;
+#pragma unroll
+      for (int p = 0; p < G / 2; ++p) {
+        if (gl[2 * p] < 0) break;  // warp-uniform: rows fill in order
+        float acc = 0.0f;
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+          if (i < nc()) {
+            const float qv = QREG ? qr[QREG ? i : 0] : qelem(16 * i + c, i);
+            if (L2) {
+              const float d = __fsub_rn(qv, x[p][i]);
+              acc = __fmaf_rn(d, d, acc);
+            } else {
+              acc = __fmaf_rn(qv, x[p][i], acc);
+            }
+          }
+        }
+        acc = __fadd_rn(acc, __shfl_xor_sync(kFull, acc, 4));  // acc0+acc1 | acc2+acc3
+        acc = __fadd_rn(acc, __shfl_xor_sync(kFull, acc, 8));  // v[b]
+        acc = __fadd_rn(acc, __shfl_xor_sync(kFull, acc, 1));  // v0+v1 | v2+v3
+        acc = __fadd_rn(acc, __shfl_xor_sync(kFull, acc, 2));  // (v0+v1)+(v2+v3)
+        if (!L2) acc = __fsub_rn(1.0f, acc);
+        const float r0 = __shfl_sync(kFull, acc, 0), r1 = __shfl_sync(kFull, acc, 16);
+        if (gl[2 * p] == lane) mine = r0;
+        if (gl[2 * p + 1] == lane) mine = r1;
+      }
+    }
+    return mine;
+  }
+  __device__ __forceinline__ void init(const SearchParams& P) { setup(P.pd); }
+  __device__ __forceinline__ void load_query(const SearchParams& P, const float* raw, const float* inv_norm,
+                                             uint32_t q, int lane) {
+    load_raw(raw, P.dim, inv_norm ? inv_norm[q] : 1.0f, inv_norm != nullptr, lane);
+  }
+  template <bool L2>
+  __device__ __forceinline__ float dists(const SearchParams& P, uint32_t id, uint32_t mask, int lane) const {
+    return rows<L2>(P.vecs, P.pd, id, mask, lane);
   }
 };
 
@@ -500,16 +611,27 @@ __device__ __forceinline__ float approx_partial(const SearchParams& P, uint32_t 
   return acc;
 }
 
-template <int RPP, int E, int PREC>
+// The exact FP32 policy (the index's summation order, runtime lengths) of a
+// compressed padded-width class pdc: ORD 0 the AVX-512 order, 1 the NEON order.
+template <int PDC, int ORD>
+struct ExactFor {
+  using type = ExactDist<-1, 0, PDC == 128 ? 5 : (PDC == 256 ? 9 : (PDC == 512 ? 17 : 33)),
+                         PDC == 128 ? 4 : (PDC <= 512 ? 2 : 1)>;
+};
+template <int PDC>
+struct ExactFor<PDC, 1> {
+  using type = NeonDist<-(PDC <= 512 ? PDC / 16 : 64), PDC == 128 ? 4 : 2, (PDC <= 512)>;
+};
+
+template <int RPP, int E, int PREC, int ORD = 0>
 struct ApproxDist {
   static constexpr bool kApprox = true;
   static constexpr int kMinBlocks = 5;  // (128, 6) measured 8% slower on the 1M FP8 walk
   static constexpr int LPR = 32 / RPP;
-  // the exact FP32 layout (reference order, runtime block counts) of the same
-  // padded-width class: the fused rerank computes the pool's exact distances
+  // the exact FP32 policy of the same padded-width class: the fused rerank
+  // computes the pool's exact distances
   static constexpr int kPdc = LPR * E;
-  using Exact = ExactDist<-1, 0, kPdc == 128 ? 5 : (kPdc == 256 ? 9 : (kPdc == 512 ? 17 : 33)),
-                          kPdc == 128 ? 4 : (kPdc <= 512 ? 2 : 1)>;
+  using Exact = typename ExactFor<kPdc, ORD>::type;
   float qa[E];
   __device__ __forceinline__ void init(const SearchParams&) {}
   __device__ __forceinline__ void load_query(const SearchParams& P, const float* raw, const float* inv_norm,
@@ -983,20 +1105,14 @@ static __device__ __noinline__ void fused_rerank(const float* __restrict__ vecs,
                                                  const uint32_t* prow, int s, uint64_t* res, uint64_t* stE, int R,
                                                  int lane) {
   EX ex;
-  ex.L.nb_rt = static_cast<int>(pd / 64);
-  ex.L.nt_rt = static_cast<int>((pd % 64) / 16);
-#pragma unroll
-  for (int i = 0; i < EX::kSlots; ++i) {
-    const int e = ex.L.elem(i, lane);
-    const float v = (e >= 0 && e < static_cast<int>(dim)) ? __ldg(raw + e) : 0.0f;
-    ex.qr[i] = cosine ? __fmul_rn(v, inv) : v;
-  }
+  ex.setup(pd);
+  ex.load_raw(raw, dim, inv, cosine, lane);
   int n = 0;
   for (int c0 = 0; c0 < s; c0 += 32) {
     const bool live = c0 + lane < s;
     const uint32_t id = live ? prow[c0 + lane] : kNoId;
     const uint32_t mask = __ballot_sync(kFull, live);
-    const float d = EX::template rows<L2>(ex.L, vecs, pd, id, mask, ex.qr, lane);
+    const float d = ex.template rows<L2>(vecs, pd, id, mask, lane);
     const uint64_t v = warp_sort32(live ? mkkey(d, id) : kMaxKey, lane);
     const int mm = __popc(mask);
     if (lane < mm) stE[lane] = v;
@@ -1436,14 +1552,37 @@ int occupancy_t(int wpb, size_t smem) {
     if (S_ <= 33) return FN<sk::ExactDist<-1, 0, 33, 1>, L2>(__VA_ARGS__);                          \
   }
 
-// compressed-precision traversal layouts per padded width (rows of pdc elements)
-#define HG_SEARCH_APPROX_DISPATCH(FN, PREC, L2, ...)                      \
-  switch (pdc) {                                                           \
-    case 128: return FN<sk::ApproxDist<4, 16, PREC>, L2>(__VA_ARGS__);    \
-    case 256: return FN<sk::ApproxDist<4, 32, PREC>, L2>(__VA_ARGS__);    \
-    case 512: return FN<sk::ApproxDist<2, 32, PREC>, L2>(__VA_ARGS__);    \
-    case 1024: return FN<sk::ApproxDist<1, 32, PREC>, L2>(__VA_ARGS__);   \
-    default: break;                                                        \
+// The same in the NEON order: chain length pd / 16, rows in pairs.
+#define HG_SEARCH_DISPATCH_NEON(FN, L2, ...)                                      \
+  switch (pd) {                                                                  \
+    case 16: return FN<sk::NeonDist<1, 8>, L2>(__VA_ARGS__);                     \
+    case 32: return FN<sk::NeonDist<2, 8>, L2>(__VA_ARGS__);                     \
+    case 64: return FN<sk::NeonDist<4, 8>, L2>(__VA_ARGS__);                     \
+    case 96: return FN<sk::NeonDist<6, 4>, L2>(__VA_ARGS__);                     \
+    case 112: return FN<sk::NeonDist<7, 4>, L2>(__VA_ARGS__);                    \
+    case 128: return FN<sk::NeonDist<8, 4>, L2>(__VA_ARGS__);                    \
+    case 256: return FN<sk::NeonDist<16, 2>, L2>(__VA_ARGS__);                   \
+    case 512: return FN<sk::NeonDist<32, 2>, L2>(__VA_ARGS__);                   \
+    case 960: return FN<sk::NeonDist<60, 2, false>, L2>(__VA_ARGS__);            \
+    default: break;                                                              \
+  }                                                                              \
+  {                                                                              \
+    const int NC_ = static_cast<int>(pd / 16);                                   \
+    if (NC_ <= 8) return FN<sk::NeonDist<-8, 4>, L2>(__VA_ARGS__);               \
+    if (NC_ <= 16) return FN<sk::NeonDist<-16, 2>, L2>(__VA_ARGS__);             \
+    if (NC_ <= 32) return FN<sk::NeonDist<-32, 2>, L2>(__VA_ARGS__);             \
+    if (NC_ <= 66) return FN<sk::NeonDist<-66, 2, false>, L2>(__VA_ARGS__);      \
+  }
+
+// compressed-precision traversal layouts per padded width (rows of pdc
+// elements); ORD is the summation order of the exact rerank
+#define HG_SEARCH_APPROX_DISPATCH(FN, PREC, L2, ORD, ...)                       \
+  switch (pdc) {                                                                 \
+    case 128: return FN<sk::ApproxDist<4, 16, PREC, ORD>, L2>(__VA_ARGS__);     \
+    case 256: return FN<sk::ApproxDist<4, 32, PREC, ORD>, L2>(__VA_ARGS__);     \
+    case 512: return FN<sk::ApproxDist<2, 32, PREC, ORD>, L2>(__VA_ARGS__);     \
+    case 1024: return FN<sk::ApproxDist<1, 32, PREC, ORD>, L2>(__VA_ARGS__);    \
+    default: break;                                                              \
   }
 
 }  // namespace sk

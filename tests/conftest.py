@@ -27,12 +27,18 @@ def sha256(path) -> str:
 
 @pytest.fixture(scope="session")
 def hg():
-    """The hnswgpu module with libhnswgpu.so built (incrementally) in-tree."""
+    """The hnswgpu module with libhnswgpu.so built (incrementally) in-tree.
+
+    The golden fixtures were recorded by the reference on an x86-64 host in
+    its AVX-512 order, so indexes start in that order on every host (an Arm
+    host would otherwise default to NEON); tests of the NEON order set it
+    themselves."""
     import build as gpubuild  # hnsw-engine_gb300/build.py
 
     gpubuild.build()
     import hnswgpu
 
+    hnswgpu.set_distance_order("avx512")
     return hnswgpu
 
 

@@ -1,0 +1,156 @@
+"""The NEON summation order on the GPU.
+
+On an Arm host the reference dispatches to its NEON kernels
+(src/kernels_neon.cpp:10-54): 4 x 4-lane FMA accumulators over 16-float
+blocks, (acc0 + acc1) + (acc2 + acc3), then vaddvq_f32.  Indexes loaded in
+that order walk with NeonDist, so float distances -- and hence ids -- equal
+a reference run on the same host bit for bit.
+
+* everywhere: the GPU's NEON-order search equals the oracle's NEON-order
+  search bitwise (cosine with filters and deletes, d = 960, inner product),
+  and the compressed forms' reranked distances equal NEON-order exact
+  distances;
+* on an Arm host with the reference built here: the oracle's NEON kernels
+  equal the reference's own, and the GPU equals the reference's
+  search_batch on graphs the reference built on this host;
+* across orders (the benchmark spec's tolerance rule): the AVX-512-order GPU path
+  against the NEON reference -- ids equal except at distance ties within
+  1e-6 relative, distances within 1e-5 relative.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ARM = os.uname().machine in ("aarch64", "arm64")
+
+
+@pytest.fixture
+def neon(hg):
+    hg.set_distance_order("neon")
+    yield hg
+    hg.set_distance_order("avx512")
+
+
+def _eq_oracle(rec, ol, od, what=""):
+    np.testing.assert_array_equal(rec["label"], ol, err_msg=f"labels {what}")
+    assert rec["distance"].tobytes() == od.tobytes(), f"distances {what}"
+
+
+def test_cosine_filters_deletes_vs_oracle(neon, oracle, graphs):
+    import workloads
+
+    _, q, *_ = graphs.data("c3s")
+    p = graphs.path("c3s", deleted=True)
+    ix = neon.Index.load(p)
+    ox = oracle.OracleIndex(p, isa="neon")
+    fw = workloads.label_filter_bits(4000, lambda l: l % 10 == 0)
+    for k, ef, filt in ((10, 40, False), (100, 400, True), (10, 160, True), (100, 100, False)):
+        rec = ix.search_raw(q, k, ef, filter=neon.Bitset(fw, 4000) if filt else None)
+        ol, od = ox.search_batch(q, k, ef, filters=[(fw, 4000)] if filt else None,
+                                 fsel=np.zeros(q.shape[0], np.int32) if filt else None)
+        _eq_oracle(rec, ol, od, f"k={k} ef={ef} filtered={filt}")
+
+
+@pytest.mark.parametrize("name,metric", [("c4s", "l2"), ("ip", "ip"), ("c1", "l2")])
+def test_float_and_ip_vs_oracle(neon, oracle, graphs, name, metric):
+    _, q, *_ = graphs.data(name)
+    p = graphs.path(name)
+    ix = neon.Index.load(p)
+    ox = oracle.OracleIndex(p, isa="neon")
+    for ef in (20, 100):
+        rec = ix.search_raw(q[:200], 10, ef)
+        ol, od = ox.search_batch(q[:200], 10, ef)
+        _eq_oracle(rec, ol, od, f"{name} ef={ef}")
+
+
+@pytest.mark.parametrize("opts", [dict(precision=1), dict(precision=2, rerank_factor=4),
+                                  dict(precision=1, lists_per_step=2), dict(precision=2, warps_per_query=4)])
+def test_compressed_forms_rerank_in_neon_order(neon, oracle, graphs, opts):
+    base, q, *_ = graphs.data("c3s")
+    ix = neon.Index.load(graphs.path("c3s"))
+    rec = ix.search_batch_ex(q[:100], 10, 80, **opts)
+    pdim = 112
+    for i in range(100):
+        a = np.zeros(pdim, np.float32)
+        a[:100] = oracle.prepare_vector("cosine", q[i])
+        for j in range(10):
+            b = np.zeros(pdim, np.float32)
+            b[:100] = oracle.prepare_vector("cosine", base[int(rec["label"][i, j])])
+            want = oracle.lib().orc_distance(oracle.ISAS["neon"], oracle.METRICS["cosine"], a.ctypes.data,
+                                             b.ctypes.data, pdim)
+            assert np.float32(want).tobytes() == rec["distance"][i, j].tobytes(), (opts, i, j)
+
+
+@pytest.mark.skipif(not ARM, reason="the reference's NEON kernels exist only on an Arm host")
+def test_oracle_neon_kernels_equal_the_reference():
+    import refcore
+
+    if not refcore.available():
+        pytest.skip("reference library not built on this host")
+    import pyoracle
+
+    r = np.random.default_rng(11)
+    for dim in (1, 3, 4, 15, 16, 17, 33, 100, 112, 128, 960):
+        a = r.normal(size=(64, dim)).astype(np.float32)
+        b = r.normal(size=(64, dim)).astype(np.float32)
+        l2, dot = refcore.kernels("neon", a, b)
+        for i in range(64):
+            assert pyoracle.kernel("neon", True, a[i], b[i]).tobytes() == l2[i].tobytes(), (dim, i)
+            assert pyoracle.kernel("neon", False, a[i], b[i]).tobytes() == dot[i].tobytes(), (dim, i)
+
+
+def _reference_graph(tmp_path, base, metric):
+    import refcore
+
+    if not refcore.available():
+        pytest.skip("reference library not built on this host")
+    p = tmp_path / f"ref_{metric}.idx"
+    refcore.build(base, p, metric=metric, M=16, ef_construction=200, threads=0)
+    return p
+
+
+@pytest.mark.skipif(not ARM, reason="the reference runs its NEON kernels only on an Arm host")
+def test_gpu_equals_the_reference_on_this_host(neon, tmp_path):
+    """Cosine with filters and deletes on a graph the reference built here:
+    the GPU in NEON order equals the reference's search_batch bit for bit."""
+    import refcore
+    import workloads
+
+    base, q = workloads.unit_mixture(20000, 100, 200, 500)
+    p = _reference_graph(tmp_path, base, "cosine")
+    rx = refcore.RefIndex(p)
+    for lab in workloads.random_deletes(20000, 0.01, seed=2):
+        rx.mark_deleted(int(lab))
+    pd = tmp_path / "ref_cosine_del.idx"
+    rx.save(pd)
+    ix = neon.Index.load(pd)
+    fw = workloads.label_filter_bits(20000, lambda l: l % 10 == 0)
+    for k, ef, filt in ((10, 40, False), (100, 400, True), (10, 100, True)):
+        want = rx.search_batch(q, k, ef, filt=refcore.Bitset(fw, 20000) if filt else None)
+        got = ix.search_raw(q, k, ef, filter=neon.Bitset(fw, 20000) if filt else None)
+        np.testing.assert_array_equal(got["label"], want["label"], err_msg=f"k={k} ef={ef} f={filt}")
+        assert got["distance"].tobytes() == want["distance"].tobytes(), (k, ef, filt)
+
+
+@pytest.mark.skipif(not ARM, reason="the reference runs its NEON kernels only on an Arm host")
+def test_other_order_within_tolerance_of_the_reference(hg, tmp_path):
+    """The AVX-512-order GPU path against the NEON reference: ids equal
+    except where distances tie within 1e-6 relative, distances within 1e-5."""
+    import refcore
+    import workloads
+
+    base, q = workloads.scaled_abs_normal(20000, 128, 300)
+    p = _reference_graph(tmp_path, base, "l2")
+    want = refcore.RefIndex(p).search_batch(q, 10, 80)
+    got = hg.Index.load(p).search_raw(q, 10, 80)  # AVX-512 order (the session default)
+    wd = want["distance"].astype(np.float64)
+    gd = got["distance"].astype(np.float64)
+    assert np.all(np.abs(gd - wd) <= 1e-5 * np.abs(wd) + 1e-30)
+    differ = got["label"] != want["label"]
+    # where the ids differ, the two distances at that rank tie within 1e-6
+    assert np.all(np.abs(gd - wd)[differ] <= 1e-6 * np.abs(wd)[differ]), np.argwhere(differ)[:5]
