@@ -62,9 +62,10 @@ FORMS = [
     ("fp8_walk", dict(precision=2, rerank_factor=4)),
     ("fp8_4warps", dict(precision=2, rerank_factor=4, warps_per_query=4)),
 ]
-# DRAM bytes (read + write) of one launch of the headline kernel over the
-# batch, from an ncu capture (null until profiled)
-HEAD_DRAM_BYTES = None
+# DRAM bytes (read + write) of one launch of the headline kernel (the FP16
+# beam walk at ef 48) over the 100,000-query batch, from an ncu capture:
+# 18.052 GB read + 0.143 GB written
+HEAD_DRAM_BYTES = 18_195_270_000
 
 
 def dist_env():
@@ -269,12 +270,15 @@ def run_ours(args, rank, world, local):
     out_d = torch.empty((HEAD_NQ, HEAD_K, 4), dtype=torch.int32, device=dev)  # 16-byte records
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
 
-    def step(kw, ef, graph=True):
-        ix.search_device(q_d.data_ptr(), HEAD_NQ, HEAD_K, ef, out_d.data_ptr(), stream.cuda_stream, graph=graph,
-                         **kw)
+    use_graph = args.launch == "graph"
 
-    def timed(kw, ef, warmup, steps, clocks=None):
-        """Per-step device milliseconds (CUDA events on the launch stream)."""
+    def step(kw, ef):
+        ix.search_device(q_d.data_ptr(), HEAD_NQ, HEAD_K, ef, out_d.data_ptr(), stream.cuda_stream,
+                         graph=use_graph, **kw)
+
+    def timed(kw, ef, warmup, steps, clocks=None, nvtx=None):
+        """Per-step device milliseconds (CUDA events on the launch stream);
+        nvtx names a range around the timed steps (for a profiler's filter)."""
         with torch.cuda.stream(stream):
             for _ in range(warmup):
                 flush.zero_()
@@ -286,12 +290,16 @@ def run_ours(args, rank, world, local):
             ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
             if clocks:
                 clocks.__enter__()
+            if nvtx:
+                torch.cuda.nvtx.range_push(nvtx)
             for i in range(steps):
                 flush.zero_()
                 ev[i][0].record(stream)
                 step(kw, ef)
                 ev[i][1].record(stream)
             torch.cuda.synchronize()
+            if nvtx:
+                torch.cuda.nvtx.range_pop()
             if clocks:
                 clocks.__exit__()
         return [a.elapsed_time(b) for a, b in ev]
@@ -311,8 +319,8 @@ def run_ours(args, rank, world, local):
     plain_ef = table["fp32_plain"]["ef"]
 
     clocks = Clocks(local)
-    head_ms = timed(head_kw, head_ef, args.warmup, args.steps, clocks)
-    plain_ms = timed(plain_kw, plain_ef, args.warmup, args.steps)
+    head_ms = timed(head_kw, head_ef, args.warmup, args.steps, clocks, nvtx="head_timed")
+    plain_ms = timed(plain_kw, plain_ef, args.warmup, args.steps, nvtx="plain_timed")
     dev_ms = sum(head_ms)
     plain_dev_ms = sum(plain_ms)
 
@@ -369,7 +377,8 @@ def run_ours(args, rank, world, local):
                    "compressed_over_plain": round(qps / plain_qps, 3),
                    "forms": table, "l2_flush": "256 MiB write before every timed step (the graph and rows "
                                                 "also exceed the 129 MB L2)",
-                   "launch": "one CUDA-graph replay per step: bucket kernel, one persistent walk, rerun pass",
+                   "launch": ("one CUDA-graph replay" if use_graph else "kernel launches") +
+                             " per step: bucket kernel, one persistent walk, rerun pass",
                    "parallelism": f"replicas x{world} (queries per replica fixed)",
                    "graph": {"source": "reference add_batch (all host threads), FORMAT v1 file",
                              "seconds": round(build_s, 1), "how": build_how},
@@ -392,7 +401,7 @@ def run_ours(args, rank, world, local):
         result["cpu_baseline"] = cpu_baseline(ix, gpath, queries, plain_ef)
         del ix
         if not args.no_batched:
-            result["batched_200k"] = run_batched_200k(local)
+            result["batched_200k"] = run_batched_200k(local, use_graph)
         if not args.no_serving:
             result["serving"] = run_serving(local, gpath)
         if not args.no_precision:
@@ -427,7 +436,7 @@ B2_N, B2_CLUSTERS, B2_NQ = 200_000, 256, 10_000
 B2_EFS = (10, 20, 40, 80, 160, 320)
 
 
-def run_batched_200k(local):
+def run_batched_200k(local, use_graph=True):
     """200,000 x 128 (256 clusters), 10,000 queries with ef drawn per query from
     {10..320}, k = 10: one persistent launch on the GPU (plain FP32) against the
     reference's search_batch grouped per ef; ids and distances compared."""
@@ -455,14 +464,17 @@ def run_batched_200k(local):
     with torch.cuda.stream(stream):
         for i in range(8):
             flush.zero_()
+            if i == 3:
+                torch.cuda.nvtx.range_push("b200_timed")
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
             ix.search_device(q_d.data_ptr(), B2_NQ, HEAD_K, int(efs.max()), out_d.data_ptr(), stream.cuda_stream,
-                             ef_ptr=ef_d.data_ptr(), graph=True)
+                             ef_ptr=ef_d.data_ptr(), graph=use_graph)
             b.record(stream)
             torch.cuda.synchronize()
             if i >= 3:
                 ms.append(a.elapsed_time(b))
+        torch.cuda.nvtx.range_pop()
     gpu = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(B2_NQ, HEAD_K)
     bf = hnswgpu.BruteForceIndex(HEAD_DIM, "l2")
     bf.add(base)
@@ -773,6 +785,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 200k mixed-ef block")
     ap.add_argument("--no-serving", action="store_true", help="skip the 1M serving block")
     ap.add_argument("--no-precision", action="store_true", help="skip the d=960 precision block")
+    ap.add_argument("--launch", choices=["graph", "streams"], default="graph",
+                    help="timed steps: one CUDA-graph replay, or kernel launches (for a profiler)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
