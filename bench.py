@@ -476,6 +476,20 @@ def run_batched_200k(local, use_graph=True):
                 ms.append(a.elapsed_time(b))
         torch.cuda.nvtx.range_pop()
     gpu = out_d.cpu().numpy().view(hnswgpu.NEIGHBOR).reshape(B2_NQ, HEAD_K)
+    # the allocation-free entry point beside the allocating one (one ef, 80)
+    noalloc = {}
+    for name, call in (("search_batch", ix.search_device), ("noalloc", ix.search_noalloc)):
+        t = []
+        with torch.cuda.stream(stream):
+            for i in range(5):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                call(q_d.data_ptr(), B2_NQ, HEAD_K, 80, out_d.data_ptr(), stream.cuda_stream)
+                b.record(stream)
+                torch.cuda.synchronize()
+                if i >= 2:
+                    t.append(a.elapsed_time(b))
+        noalloc[name + "_qps"] = round(B2_NQ / (statistics.median(t) / 1e3), 1)
     bf = hnswgpu.BruteForceIndex(HEAD_DIM, "l2")
     bf.add(base)
     gt = bf.search_raw(queries, HEAD_K)["label"].astype(np.int64)
@@ -495,6 +509,8 @@ def run_batched_200k(local, use_graph=True):
             "qps": round(B2_NQ / (statistics.median(ms) / 1e3), 1), "ms_per_batch": round(statistics.median(ms), 4),
             "recall_at_10": round(workloads.recall_at_k(gpu["label"].astype(np.int64), gt), 4),
             "reference_qps": round(B2_NQ / el, 1),
+            "noalloc": {**noalloc, "ef": 80, "note": "device-resident batch; the allocation-free call runs on a "
+                                                      "fixed 48 warps"},
             "reference": f"search_batch per ef group, {threads} threads, simd {refcore.isa()}",
             "parity_vs_reference": {"queries": B2_NQ, **parity(gpu, ref)}}
 

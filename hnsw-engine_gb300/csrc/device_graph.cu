@@ -927,29 +927,54 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   const bool beamwalk = !wide && a->lists_per_step >= 1 && prec != HGD_PREC_FP32 && P.pdc == 128 && g->n > 0 &&
                         g->n < (1ull << 24) && P.M0 <= 32;
   if (beamwalk) {
-    hg::SearchParams B = P;
-    B.R = round_up(ef_max, 32);
-    // visited hash slots: each query uses the size its own ef calls for
-    // (beam_hash_slots); the launch reserves the largest
-    B.H = hg::beam_hash_slots(ef_max);
-    B.lists_per_step = std::min<uint32_t>(a->lists_per_step, hg::kBeamMaxE);
-    B.qidx = w->lists.as<uint32_t>();
-    B.lpt_sizes = work + 32;
-    B.lpt_buckets = spec.n;
-    B.lpt_stride = static_cast<uint32_t>(nq);
-    B.work = work + 8;
-    B.slot_base = 0;
     // filters or deletes: the variant that keeps a separate result list
     const bool filt = a->num_filters > 0 || g->num_deleted > 0;
     const int wpb = 4;
-    const size_t smem = static_cast<size_t>(wpb) * hg::beam_warp_bytes(B.H, B.R, filt);
-    if (smem > 227u * 1024u) return fail(HGD_EINVAL, "hgd_search: ef too large for the beam walk's shared memory");
-    const int occ = hg::occupancy_beam(g->metric, prec, P.order, wpb, smem, filt);
-    if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the beam kernel cannot be resident");
-    const uint64_t want = (nq + wpb - 1) / wpb;
-    const int blocks = static_cast<int>(std::min<uint64_t>(want, static_cast<uint64_t>(g->sms) * occ));
-    cudaError_t e = hg::launch_search_beam(B, d_inv, blocks, wpb, filt, st);
-    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("beam kernel launch: ") + cudaGetErrorString(e));
+    // one launch over every query with the largest bucket's shape, or --
+    // per-query ef spread over several buckets -- one launch per bucket with
+    // its own shape (the beam and hash of a large ef would otherwise cut the
+    // occupancy of every query), concurrent on the workspace's forked
+    // streams, larger ef first.  A query walks the same in either: its hash
+    // size and beam capacity follow its own ef.
+    const bool per_bucket = a->ef_per_query != nullptr && spec.n > 1;
+    if (per_bucket) HG_CUDA(cudaEventRecord(w->ev_fork, st));
+    for (int b = per_bucket ? static_cast<int>(spec.n) - 1 : 0; b >= 0; --b) {
+      const uint32_t hi = per_bucket ? spec.hi[b] : ef_max;
+      hg::SearchParams B = P;
+      B.R = round_up(hi, 32);
+      // visited hash slots: each query uses the size its own ef calls for
+      // (beam_hash_slots); the launch reserves the largest
+      B.H = hg::beam_hash_slots(hi);
+      B.lists_per_step = std::min<uint32_t>(a->lists_per_step, hg::kBeamMaxE);
+      B.slot_base = 0;
+      if (per_bucket) {
+        B.nq_dev = work + 32 + b;
+        B.qidx = w->lists.as<uint32_t>() + static_cast<uint64_t>(b) * nq;
+        B.work = work + 8 + b;
+      } else {
+        B.qidx = w->lists.as<uint32_t>();
+        B.lpt_sizes = work + 32;
+        B.lpt_buckets = spec.n;
+        B.lpt_stride = static_cast<uint32_t>(nq);
+        B.work = work + 8;
+      }
+      const size_t smem = static_cast<size_t>(wpb) * hg::beam_warp_bytes(B.H, B.R, filt);
+      if (smem > 227u * 1024u) return fail(HGD_EINVAL, "hgd_search: ef too large for the beam walk's shared memory");
+      const int occ = hg::occupancy_beam(g->metric, prec, P.order, wpb, smem, filt);
+      if (occ < 1) return fail(HGD_ECUDA, "hgd_search: the beam kernel cannot be resident");
+      const uint64_t want = (nq + wpb - 1) / wpb;
+      const int blocks = static_cast<int>(std::min<uint64_t>(want, static_cast<uint64_t>(g->sms) * occ));
+      cudaStream_t sb = st;
+      if (per_bucket) {
+        sb = w->aux[b];
+        HG_CUDA(cudaStreamWaitEvent(sb, w->ev_fork, 0));
+      }
+      cudaError_t e = hg::launch_search_beam(B, d_inv, blocks, wpb, filt, sb);
+      if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("beam kernel launch: ") + cudaGetErrorString(e));
+      if (per_bucket) HG_CUDA(cudaEventRecord(w->ev_join[b], sb));
+    }
+    if (per_bucket)
+      for (uint32_t b = 0; b < spec.n; ++b) HG_CUDA(cudaStreamWaitEvent(st, w->ev_join[b], 0));
   } else if (wide) {
     hg::SearchParams B = P;
     B.R = round_up(ef_max, 32);

@@ -136,10 +136,15 @@ namespace {
 constexpr uint32_t kNaMaxNodes = 1u << 20;    // largest graph
 constexpr uint32_t kNaMaxQueries = 1u << 16;  // largest batch
 constexpr uint32_t kNaMaxEf = 512;            // largest ef (after max(ef, k))
+// A fixed 48 warps walk every batch, whatever the GPU: the per-warp scratch
+// below is sized for them, so a batch runs at a fraction of the allocating
+// path's throughput (which fills every SM).
 constexpr int kNaWarpsPerBlock = 4;
 constexpr int kNaBlocks = 12;
 constexpr uint64_t kNaSlots = static_cast<uint64_t>(kNaWarpsPerBlock) * kNaBlocks;
-constexpr uint64_t kNaPoolCap = 2048;                    // spill keys per warp before the rerun pass
+// spill keys per warp; a query that needs more goes to the rerun pass, which
+// one warp runs, so such queries are finished one after another
+constexpr uint64_t kNaPoolCap = 2048;
 constexpr uint64_t kNaBitmapWords = kNaMaxNodes / 32 + 1;
 
 // byte layout of the array
@@ -159,7 +164,9 @@ std::mutex g_na_mutex;
 void* g_na_address[64] = {};
 
 // Device address of the array on the current device, looked up once per
-// device (host code cannot use the symbol itself as a device pointer).
+// device (host code cannot use the symbol itself as a device pointer) and
+// kept for the process: after a device reset the kept address would be
+// stale, so a reset after the first call is not supported.
 cudaError_t noalloc_scratch(int device, unsigned char** out) {
   if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_na_mutex);
@@ -202,6 +209,10 @@ cudaError_t launch_search_noalloc(SearchParams P, int device, bool cosine, cudaS
   P.work = ctr;
   P.ovf_count = ctr + 1;
   P.ovf_list = reinterpret_cast<uint32_t*>(base + kNaOffOvf);
+  // The kernel raises ctr[4] for a query whose ef or k exceeds the launch's
+  // capacity.  The host checks (one ef and k per batch, R >= max(ef, k))
+  // make that impossible here, so the flag is not read back; a change that
+  // allowed per-query ef or k would have to read it.
   P.err = ctr + 4;
   P.nq_dev = nullptr;
   P.qidx = nullptr;

@@ -170,7 +170,13 @@ int hg_bruteforce_last_path(const hg_bruteforce* bf);
  * array's device address; make it before any stream capture.  The graph must
  * already be mirrored on the GPU (any earlier allocating search does it).
  * Limits: nq <= 65536, index size <= 2^20 nodes, max(ef, k) <= 512; larger
- * requests return HG_EINVAL.  No counterpart in the reference. */
+ * requests return HG_EINVAL.  Cost: the walk runs on a fixed 48 warps (12
+ * blocks of 4) whatever the GPU, so a large batch takes several times as
+ * long as through the allocating calls, and queries that outgrow its
+ * 2,048-key spill pool are finished one after another by a single warp.
+ * The array's device address is looked up once per device and kept: a
+ * device reset after the first call is not supported.  No counterpart in
+ * the reference. */
 int hg_index_search_batch_noalloc(const hg_index* idx, const float* queries, size_t nq, size_t k, size_t ef,
                                   hg_neighbor* out, void* stream);
 

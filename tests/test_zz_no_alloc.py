@@ -46,6 +46,25 @@ def test_no_alloc_cosine_with_deletes_and_limits(hg, graphs):
         _run(hg, ix, q[:2], 10, 600, torch)
 
 
+def test_no_alloc_overflow_reruns_match(hg, graphs):
+    """Nine in ten nodes deleted and ef = 512: the filtered walk's candidate
+    queue outgrows the 2,048-key spill pool, so queries go to the one-warp
+    rerun pass; answers still equal the allocating path's bit for bit."""
+    torch = pytest.importorskip("torch")
+    _, q, *_ = graphs.data("c1")
+    ix = hg.Index.load(graphs.path("c1"))
+    for lab in range(20000):
+        if lab % 10:
+            ix.mark_deleted(lab)
+    want = ix.search_raw(q[:64], 10, 512)
+    for _ in range(2):
+        got = _run(hg, ix, q[:64], 10, 512, torch)
+        np.testing.assert_array_equal(got["label"], want["label"])
+        assert got["distance"].tobytes() == want["distance"].tobytes()
+    _, cnt = ix.search_batch_ex(q[:64], 10, 512, counters=True, pool_cap=2048)
+    assert (cnt[:, 7] & 4).any(), "no query needed the rerun pass with a 2,048-key pool"
+
+
 def test_no_alloc_needs_a_mirrored_graph(hg, graphs):
     torch = pytest.importorskip("torch")
     _, q, *_ = graphs.data("c1")
