@@ -784,18 +784,18 @@ __global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ r
                                                      uint32_t nq, uint32_t dim, uint32_t dp, uint32_t k,
                                                      const uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t p2max,
                                                      const uint32_t* __restrict__ pool_n, Rec* __restrict__ out,
-                                                     OutMap om) {
+                                                     OutMap om, int neon) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint64_t* keys = reinterpret_cast<uint64_t*>(smem) + static_cast<size_t>(w) * p2max;
   const uint32_t q = blockIdx.x * 4u + static_cast<uint32_t>(w);
   if (q >= nq) return;
-  const int nb = static_cast<int>(dim / 64), nt = static_cast<int>((dim % 64) / 16), rem = static_cast<int>(dim % 16);
+  const BfOrder o = bf_order(dim, neon != 0);
   float qr[S];
   const float iv = inv ? inv[q] : 1.0f;
 #pragma unroll
   for (int i = 0; i < S; ++i) {
-    const int e = bslot(i, nb, nt, rem, lane);
+    const int e = bslot(o, i, lane);
     const float v = e >= 0 ? queries[static_cast<size_t>(q) * dim + e] : 0.0f;
     qr[i] = inv ? __fmul_rn(v, iv) : v;
   }
@@ -806,10 +806,10 @@ __global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ r
     float x[S];
 #pragma unroll
     for (int i = 0; i < S; ++i) {
-      const int e = bslot(i, nb, nt, rem, lane);
+      const int e = bslot(o, i, lane);
       x[i] = e >= 0 ? __ldg(rows + static_cast<size_t>(r) * dp + e) : 0.0f;
     }
-    const float d = bdist<S, L2>(x, qr, nb, nt, rem, lane);
+    const float d = bdist<S, L2>(x, qr, o, lane);
     if (lane == 0) keys[c] = (static_cast<uint64_t>(okey(d)) << 32) | r;
   }
   int p2 = 1;
@@ -842,25 +842,24 @@ __global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ r
   }
 }
 
-int slots_of(uint32_t dim) {
-  return 2 * static_cast<int>(dim / 64) + static_cast<int>((dim % 64) / 16) + 1;
-}
 
 template <bool L2>
 cudaError_t launch_rerank(int S, dim3 grid, size_t smem, cudaStream_t st, const float* rows, const uint64_t* labels,
                           const float* queries, const float* inv, uint32_t nq, uint32_t dim, uint32_t dp, uint32_t k,
                           const uint32_t* pool, uint32_t pool_cap, uint32_t p2max, const uint32_t* pool_n, Rec* out,
-                          OutMap om = OutMap{nullptr, nullptr, 0, nullptr}) {
+                          OutMap om, bool neon) {
   auto go = [&](auto fn) {
     cudaError_t e = open_smem_limit(reinterpret_cast<const void*>(fn));
     if (e != cudaSuccess) return e;
-    fn<<<grid, 128, smem, st>>>(rows, labels, queries, inv, nq, dim, dp, k, pool, pool_cap, p2max, pool_n, out, om);
+    fn<<<grid, 128, smem, st>>>(rows, labels, queries, inv, nq, dim, dp, k, pool, pool_cap, p2max, pool_n, out, om,
+                                neon ? 1 : 0);
     return cudaGetLastError();
   };
   if (S <= 6) return go(rerank_kernel<6, L2>);
   if (S <= 10) return go(rerank_kernel<10, L2>);
   if (S <= 18) return go(rerank_kernel<18, L2>);
   if (S <= 34) return go(rerank_kernel<34, L2>);
+  if (S <= 70) return go(rerank_kernel<70, L2>);  // the NEON order of rows above 512 elements
   return cudaErrorInvalidValue;
 }
 
@@ -1103,14 +1102,16 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
                                                   0);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
-    const int S = slots_of(r.dim);
+    const int S = bf_slots(r.dim, r.neon != 0);
     const dim3 rgrid((nq + 3) / 4);
     const size_t rsmem = 4ull * p2max * 8;
     e = r.metric == HGD_METRIC_L2
             ? launch_rerank<true>(S, rgrid, rsmem, st, r.rows, r.labels, queries, inv, nq, r.dim, r.dp, k, pool,
-                                  pool_cap, p2max, pool_n, static_cast<Rec*>(out))
+                                  pool_cap, p2max, pool_n, static_cast<Rec*>(out), OutMap{nullptr, nullptr, 0, nullptr},
+                                  r.neon != 0)
             : launch_rerank<false>(S, rgrid, rsmem, st, r.rows, r.labels, queries, inv, nq, r.dim, r.dp, k, pool,
-                                   pool_cap, p2max, pool_n, static_cast<Rec*>(out));
+                                   pool_cap, p2max, pool_n, static_cast<Rec*>(out),
+                                   OutMap{nullptr, nullptr, 0, nullptr}, r.neon != 0);
     if (e != cudaSuccess) break;
     uint32_t herr[4] = {0, 0, 0, 0};
     what = "status";
@@ -1231,17 +1232,17 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
                                                    sc->qq.as<float>(), n_r, splits, cap, k, sc->pool.as<uint32_t>(),
                                                    pool_cap, sc->pool_n.as<uint32_t>(), sc->err.as<uint32_t>(), 1);    if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
-    const int S = slots_of(r.dim);
+    const int S = bf_slots(r.dim, r.neon != 0);
     const dim3 rgrid((n_r + 3) / 4);
     const size_t rsmem = 4ull * p2max * 8;
     const OutMap om{a.qlist, a.kq, a.k_stride, a.done};
     e = r.metric == HGD_METRIC_L2
             ? launch_rerank<true>(S, rgrid, rsmem, st, r.rows, r.labels, sc->qp.as<float>(), nullptr, n_r, r.dim,
                                   r.dp, k, sc->pool.as<uint32_t>(), pool_cap, p2max, sc->pool_n.as<uint32_t>(),
-                                  static_cast<Rec*>(a.out), om)
+                                  static_cast<Rec*>(a.out), om, r.neon != 0)
             : launch_rerank<false>(S, rgrid, rsmem, st, r.rows, r.labels, sc->qp.as<float>(), nullptr, n_r, r.dim,
                                    r.dp, k, sc->pool.as<uint32_t>(), pool_cap, p2max, sc->pool_n.as<uint32_t>(),
-                                   static_cast<Rec*>(a.out), om);
+                                   static_cast<Rec*>(a.out), om, r.neon != 0);
   } while (false);
   if (e != cudaSuccess && err) *err = std::string("tensor scan: ") + what + ": " + cudaGetErrorString(e);
   return e;

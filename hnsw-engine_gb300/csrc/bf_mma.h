@@ -17,6 +17,7 @@ struct Rows {
   const uint64_t* labels;  // n (device), sorted
   uint32_t n, dim, dp;
   int metric;              // HGD_METRIC_*
+  int neon;                // 1: exact distances in the NEON kernel's order, 0: the AVX-512 kernel's
 };
 
 // Whether the tensor path handles this shape (dim <= 1024, k <= 256).

@@ -2,9 +2,11 @@
 //
 // Rows are stored sorted by label, so the key (order-preserving distance
 // bits << 32 | row) orders exactly like the reference's (distance, label)
-// heap.  Distances use the reference kernel's AVX-512 order over `dim`
-// (not the padded dimension): 64-float blocks into acc0..acc3, 16-float
-// blocks into acc0, the masked remainder into acc1.
+// heap.  Distances use the reference kernel's order over `dim` (not the
+// padded dimension), the host's as the reference picks it: AVX-512 (64-float
+// blocks into acc0..acc3, 16-float blocks into acc0, the masked remainder
+// into acc1) or NEON (16-float blocks into four 4-lane accumulators, 4-float
+// blocks into acc0, a fused scalar tail); see bf_common.cuh.
 //
 // One block = 16 warps x QT queries.  Each warp scans an interleaved share
 // of the rows with the QT queries held in registers and keeps, per query, a
@@ -40,6 +42,7 @@ struct BfParams {
   const float* queries;    // nq x dim raw
   const float* inv;        // cosine: per query 1/||q|| or null
   uint32_t n, dim, dp, nq, k;
+  int32_t neon;            // distance order: 1 NEON, 0 AVX-512
   void* out;
 };
 
@@ -49,8 +52,7 @@ __global__ void __launch_bounds__(kWarps * 32) bf_kernel(BfParams P) {
   uint64_t* lists = reinterpret_cast<uint64_t*>(smem);  // [warp][QT][k]
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t q0 = blockIdx.x * QT;
-  const int nb = static_cast<int>(P.dim / 64), nt = static_cast<int>((P.dim % 64) / 16);
-  const int rem = static_cast<int>(P.dim % 16);
+  const BfOrder o = bf_order(P.dim, P.neon != 0);
   const uint32_t k = P.k;
   float qr[QT][S];
 #pragma unroll
@@ -60,7 +62,7 @@ __global__ void __launch_bounds__(kWarps * 32) bf_kernel(BfParams P) {
     const float inv = P.inv ? P.inv[q] : 1.0f;
 #pragma unroll
     for (int i = 0; i < S; ++i) {
-      const int e = bslot(i, nb, nt, rem, lane);
+      const int e = bslot(o, i, lane);
       const float v = e >= 0 ? raw[e] : 0.0f;
       qr[t][i] = P.inv ? __fmul_rn(v, inv) : v;
     }
@@ -75,12 +77,12 @@ __global__ void __launch_bounds__(kWarps * 32) bf_kernel(BfParams P) {
     float x[S];
 #pragma unroll
     for (int i = 0; i < S; ++i) {
-      const int e = bslot(i, nb, nt, rem, lane);
+      const int e = bslot(o, i, lane);
       x[i] = e >= 0 ? __ldg(row + e) : 0.0f;
     }
 #pragma unroll
     for (int t = 0; t < QT; ++t) {
-      const float d = bdist<S, L2>(x, qr[t], nb, nt, rem, lane);
+      const float d = bdist<S, L2>(x, qr[t], o, lane);
       const uint64_t key = (static_cast<uint64_t>(okey(d)) << 32) | r;
       uint64_t* L = my + static_cast<size_t>(t) * k;
       const int c = cnt[t];
@@ -181,10 +183,6 @@ __global__ void bf_translate(const uint64_t* words, uint64_t num_bits, const uin
   out[wd] = bits;
 }
 
-int bf_slots(uint32_t dim) {
-  return 2 * static_cast<int>(dim / 64) + static_cast<int>((dim % 64) / 16) + 1;
-}
-
 template <int S, int QT, bool L2>
 cudaError_t bf_launch(const BfParams& P, cudaStream_t st) {
   int p2 = 1;
@@ -199,12 +197,13 @@ cudaError_t bf_launch(const BfParams& P, cudaStream_t st) {
 
 template <bool L2>
 cudaError_t bf_dispatch(const BfParams& P, cudaStream_t st) {
-  const int S = bf_slots(P.dim);
+  const int S = bf_slots(P.dim, P.neon != 0);
   const bool big_k = P.k > 64;
   if (S <= 6) return big_k ? bf_launch<6, 1, L2>(P, st) : bf_launch<6, 4, L2>(P, st);
   if (S <= 10) return big_k ? bf_launch<10, 1, L2>(P, st) : bf_launch<10, 2, L2>(P, st);
   if (S <= 18) return bf_launch<18, 1, L2>(P, st);
   if (S <= 34) return bf_launch<34, 1, L2>(P, st);
+  if (S <= 70) return bf_launch<70, 1, L2>(P, st);  // the NEON order of rows above 512 elements
   return cudaErrorInvalidValue;
 }
 
@@ -220,6 +219,7 @@ struct hgd_flat {
   hg::bfm::Store* tensor = nullptr;  // FP16 copy for the tensor-core path (built on first use)
   int path = HGD_BF_AUTO;
   int last_path = 0;
+  bool neon = false;  // distance order
 };
 
 extern "C" {
@@ -227,8 +227,9 @@ extern "C" {
 int hgd_flat_upload(const float* prepared, const uint64_t* labels, uint64_t n, uint64_t dim, int metric, int device,
                     int order, hgd_flat** out) {
   if (!out || (n && (!prepared || !labels))) return (hg::set_last_error("hgd_flat_upload: null argument"), HGD_EINVAL);
-  if (order != HGD_ORDER_AVX512) return (hg::set_last_error("brute force: only the AVX-512 order is implemented"), HGD_EINVAL);
-  if (n >= 0xFFFFFFFFull || dim == 0 || bf_slots(static_cast<uint32_t>(dim)) > 34)
+  if (order != HGD_ORDER_AVX512 && order != HGD_ORDER_NEON)
+    return (hg::set_last_error("brute force: the GPU implements the AVX-512 and NEON orders only"), HGD_EINVAL);
+  if (n >= 0xFFFFFFFFull || dim == 0 || dim > 1056)
     return (hg::set_last_error("brute force: unsupported size"), HGD_EINVAL);
   auto* f = new hgd_flat();
   f->device = device;
@@ -236,6 +237,7 @@ int hgd_flat_upload(const float* prepared, const uint64_t* labels, uint64_t n, u
   f->n = static_cast<uint32_t>(n);
   f->dim = static_cast<uint32_t>(dim);
   f->dp = (f->dim + 15) / 16 * 16;
+  f->neon = order == HGD_ORDER_NEON;
   std::vector<uint64_t> order_idx(n);
   std::iota(order_idx.begin(), order_idx.end(), 0);
   std::stable_sort(order_idx.begin(), order_idx.end(), [&](uint64_t a, uint64_t b) { return labels[a] < labels[b]; });
@@ -337,7 +339,7 @@ int hgd_bruteforce(hgd_flat* f, const float* queries, uint64_t nq, uint32_t k, c
       }
     }
     if (use_tensor) {
-      hg::bfm::Rows R{f->rows, f->labels, f->n, f->dim, f->dp, f->metric};
+      hg::bfm::Rows R{f->rows, f->labels, f->n, f->dim, f->dp, f->metric, f->neon ? 1 : 0};
       std::string err;
       if (!f->tensor && !check(hg::bfm::store_create(R, st, &f->tensor, &err))) {
         hg::set_last_error(err);
@@ -371,6 +373,7 @@ int hgd_bruteforce(hgd_flat* f, const float* queries, uint64_t nq, uint32_t k, c
     P.dp = f->dp;
     P.nq = static_cast<uint32_t>(nq);
     P.k = k;
+    P.neon = f->neon ? 1 : 0;
     P.out = dout;
     if (!check(f->metric == HGD_METRIC_L2 ? bf_dispatch<true>(P, st) : bf_dispatch<false>(P, st))) break;
     if (!check(cudaMemcpyAsync(out, dout, nq * k * 16, cudaMemcpyDeviceToHost, st))) break;

@@ -884,7 +884,8 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   const bool scanning = !r_qlist.empty();
   if (scanning) {
     hg::bfm::Rows rows{g->vecs.as<float>(), g->labels.as<uint64_t>(), static_cast<uint32_t>(g->n),
-                       static_cast<uint32_t>(g->pd), static_cast<uint32_t>(g->pd), g->metric};
+                       static_cast<uint32_t>(g->pd), static_cast<uint32_t>(g->pd), g->metric,
+                       g->order == HGD_ORDER_NEON ? 1 : 0};
     {
       std::lock_guard<std::mutex> build_lock(g->mu);
       if (!g->scan) {

@@ -154,3 +154,40 @@ def test_other_order_within_tolerance_of_the_reference(hg, tmp_path):
     differ = got["label"] != want["label"]
     # where the ids differ, the two distances at that rank tie within 1e-6
     assert np.all(np.abs(gd - wd)[differ] <= 1e-6 * np.abs(wd)[differ]), np.argwhere(differ)[:5]
+
+
+@pytest.mark.parametrize("dim,metric", [(100, "cosine"), (33, "l2"), (960, "l2"), (7, "ip")])
+@pytest.mark.parametrize("path", [1, 2])
+def test_bruteforce_neon_vs_oracle(neon, oracle, dim, metric, path):
+    """Brute force over dim (not the padded width) in the NEON order: 16-float
+    blocks, 4-float blocks into acc0, the fused scalar tail -- both GPU
+    kernels (1: CUDA-core scan, 2: tensor-core GEMM + exact rerank)."""
+    r = np.random.default_rng(dim)
+    base = r.normal(size=(3000, dim)).astype(np.float32)
+    q = r.normal(size=(40, dim)).astype(np.float32)
+    bf = neon.BruteForceIndex(dim, metric)
+    bf.add(base)
+    bf.set_path(path)
+    got = bf.search_raw(q, 10)
+    assert bf.last_path == path
+    ol, od = oracle.bruteforce(base, q, 10, metric=metric, isa="neon")
+    np.testing.assert_array_equal(got["label"], ol)
+    assert got["distance"].tobytes() == od.tobytes()
+
+
+@pytest.mark.skipif(not ARM, reason="the reference runs its NEON kernels only on an Arm host")
+def test_bruteforce_equals_the_reference_on_this_host(neon):
+    import refcore
+
+    if not refcore.available():
+        pytest.skip("reference library not built on this host")
+    r = np.random.default_rng(9)
+    for dim, metric in ((100, "cosine"), (37, "l2"), (128, "ip")):
+        base = r.normal(size=(5000, dim)).astype(np.float32)
+        q = r.normal(size=(30, dim)).astype(np.float32)
+        want = refcore.bruteforce(base, q, 10, metric=metric)
+        bf = neon.BruteForceIndex(dim, metric)
+        bf.add(base)
+        got = bf.search_raw(q, 10)
+        np.testing.assert_array_equal(got["label"], want["label"], err_msg=f"{dim} {metric}")
+        assert got["distance"].tobytes() == want["distance"].tobytes(), (dim, metric)
