@@ -524,10 +524,13 @@ SERVE_FILTERS = 16  # pool of distinct random 10%-density bitsets
 SERVE_RECALL_REQUESTS = 2000
 SERVE_PLAIN_REQUESTS = 500
 SERVE_FORMS = (
-    # name, server options
+    # name, server options (batch slots and batch size: 4 x 8,192 queries
+    # unless given; smaller batches trade peak for latency)
     ("fp32", dict(precision=0)),
-    ("fp16_beam2_scan", dict(precision=1, filter_scan=0.15, rerank_factor=4, lists_per_step=2)),
+    ("fp16_beam4_scan", dict(precision=1, filter_scan=0.15, rerank_factor=4, lists_per_step=4)),
     ("fp8_4warps_scan", dict(precision=2, filter_scan=0.15, rerank_factor=4, warps_per_query=4)),
+    ("fp8_4warps_scan_12x1024", dict(precision=2, filter_scan=0.15, rerank_factor=4, warps_per_query=4,
+                                     max_inflight=12, max_batch_queries=1024)),
 )
 
 
@@ -625,7 +628,7 @@ def run_serving(local, gpath):
            "batched_fp32_search_batch_ex": {"qps": round(plain_qps, 1), "recall_at_k": plain_recall[0],
                                             "recall_at_10": plain_recall[1], "queries_per_call": chunk}}
     for name, opts in SERVE_FORMS:
-        srv = hnswgpu.Server(ix, max_inflight=4, max_batch_queries=8192, **opts)
+        srv = hnswgpu.Server(ix, **{"max_inflight": 4, "max_batch_queries": 8192, **opts})
         srv.replay(requests[:2000], np.zeros(2000))  # warm-up: encodes the copy, sizes the staging
         peak, outs = srv.replay(requests, np.zeros(SERVE_REQUESTS))
         same = all(np.array_equal(outs[i]["label"], plain[offs[i]:offs[i + 1], :ks[i]]["label"])

@@ -334,9 +334,14 @@ int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_ms) {
 
 int hg_server_replay(hg_server* s, const hg_request* reqs, const double* arrival_s, size_t n,
                      hg_server_stats* stats) {
+  return hg_server_replay_latencies(s, reqs, arrival_s, n, stats, nullptr);
+}
+
+int hg_server_replay_latencies(hg_server* s, const hg_request* reqs, const double* arrival_s, size_t n,
+                               hg_server_stats* stats, double* latency_ms) {
   return guarded([&] {
     if (!s || (n && (!reqs || !arrival_s)) || !stats) throw std::invalid_argument("server replay: null argument");
-    hnsw::gb::server_replay(s->s, reqs, arrival_s, n, stats);
+    hnsw::gb::server_replay(s->s, reqs, arrival_s, n, stats, latency_ms);
   });
 }
 

@@ -203,7 +203,8 @@ Server* server_new(const Index::Impl& im, const hg_server_config& cfg);
 void server_delete(Server* s);
 uint64_t server_submit(Server* s, const hg_request& r);
 void server_wait(Server* s, uint64_t ticket, double* latency_ms);
-void server_replay(Server* s, const hg_request* reqs, const double* arrival_s, size_t n, hg_server_stats* out);
+void server_replay(Server* s, const hg_request* reqs, const double* arrival_s, size_t n, hg_server_stats* out,
+                   double* latency_ms);
 void server_stats(Server* s, hg_server_stats* out);
 
 }  // namespace hnsw::gb

@@ -464,7 +464,7 @@ class Server {
  public:
   // Submit each request at its arrival time (seconds from the call), wait for
   // all, and report the stats of exactly these requests.
-  void replay(const hg_request* reqs, const double* arrival_s, size_t n, hg_server_stats* out) {
+  void replay(const hg_request* reqs, const double* arrival_s, size_t n, hg_server_stats* out, double* latency_ms) {
     reset_stats();
     std::vector<uint64_t> tickets(n);
     const auto t0 = Clock::now();
@@ -479,7 +479,7 @@ class Server {
     for (size_t i = 0; i < n; ++i) {
       int st = HG_OK;
       std::string err;
-      wait(tickets[i], nullptr, &st, &err);
+      wait(tickets[i], latency_ms ? latency_ms + i : nullptr, &st, &err);
       if (st != HG_OK) throw std::runtime_error("server replay: request failed: " + err);
     }
     stats(out);
@@ -503,8 +503,9 @@ void server_wait(Server* s, uint64_t ticket, double* latency_ms) {
   if (st == HG_EINVAL) throw std::invalid_argument(err);
   if (st != HG_OK) throw std::runtime_error(err);
 }
-void server_replay(Server* s, const hg_request* reqs, const double* arrival_s, size_t n, hg_server_stats* out) {
-  s->replay(reqs, arrival_s, n, out);
+void server_replay(Server* s, const hg_request* reqs, const double* arrival_s, size_t n, hg_server_stats* out,
+                   double* latency_ms) {
+  s->replay(reqs, arrival_s, n, out, latency_ms);
 }
 void server_stats(Server* s, hg_server_stats* out) { s->stats(out); }
 

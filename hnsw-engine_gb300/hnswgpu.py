@@ -109,6 +109,7 @@ def lib():
         L.hg_server_submit.argtypes = [vp, C.POINTER(_Request), C.POINTER(C.c_uint64)]
         L.hg_server_wait.argtypes = [vp, C.c_uint64, C.POINTER(C.c_double)]
         L.hg_server_replay.argtypes = [vp, C.POINTER(_Request), vp, sz, C.POINTER(_ServerStats)]
+        L.hg_server_replay_latencies.argtypes = [vp, C.POINTER(_Request), vp, sz, C.POINTER(_ServerStats), vp]
         L.hg_server_stats_get.argtypes = [vp, C.POINTER(_ServerStats)]
         L.hg_server_destroy.argtypes = [vp]
         L.hg_set_distance_order.argtypes = [i32]
@@ -648,9 +649,10 @@ class Server:
             keep, out, k = self._live.pop(ticket, (None, None, 1))
         return out.reshape(-1, k), lat.value
 
-    def replay(self, requests, arrivals_s):
+    def replay(self, requests, arrivals_s, latencies=False):
         """requests: list of (queries, k, ef, filter); arrivals_s: seconds from the
-        call.  Returns (stats dict, list of result record arrays)."""
+        call.  Returns (stats dict, list of result record arrays) and, with
+        latencies=True, each request's latency in ms as a third item."""
         keep, outs = [], []
         arr = (_Request * len(requests))()
         for i, (q, k, ef, f) in enumerate(requests):
@@ -659,7 +661,10 @@ class Server:
             outs.append((out, k))
         at = np.ascontiguousarray(arrivals_s, dtype=np.float64)
         st = _ServerStats()
-        _check(lib().hg_server_replay(self._h, arr, at.ctypes.data, len(requests), C.byref(st)))
+        lat = np.zeros(len(requests), dtype=np.float64)
+        _check(lib().hg_server_replay_latencies(self._h, arr, at.ctypes.data, len(requests), C.byref(st),
+                                                lat.ctypes.data))
         stats = {f: getattr(st, f) for f, _ in _ServerStats._fields_}
-        return stats, [o.reshape(-1, k) for o, k in outs]
+        res = [o.reshape(-1, k) for o, k in outs]
+        return (stats, res, lat) if latencies else (stats, res)
 

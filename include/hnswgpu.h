@@ -226,6 +226,10 @@ int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_ms);
  * load), waits for all and reports these requests' statistics. */
 int hg_server_replay(hg_server* s, const hg_request* reqs, const double* arrival_s, size_t n,
                      hg_server_stats* stats);
+/* The same, also writing each request's latency (arrival to completion, ms)
+ * into latency_ms[i] (n entries; NULL: none). */
+int hg_server_replay_latencies(hg_server* s, const hg_request* reqs, const double* arrival_s, size_t n,
+                               hg_server_stats* stats, double* latency_ms);
 int hg_server_stats_get(hg_server* s, hg_server_stats* out);
 void hg_server_destroy(hg_server* s);
 
