@@ -181,6 +181,15 @@ __device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
                : "memory");
 }
 
+__device__ __forceinline__ void sp_mma(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                       uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
 __device__ __forceinline__ float dist_of_key_bits(uint32_t kb) {
   const uint32_t u = (kb & 0x80000000u) ? (kb & 0x7FFFFFFFu) : ~kb;
   return __uint_as_float(u);
@@ -630,51 +639,117 @@ __global__ void prep_queries_kernel(const float* __restrict__ raw, const float* 
 // the margin.  The pool's order does not matter (the rerank sorts it).  The
 // candidates are read 5-7 times by 256 threads; a warp bisecting the key
 // bits read them about 34 times, which dominated scans split many ways
-// (few queries over many rows).
+// (few queries over many rows).  The splits' counts are turned into offsets
+// in shared memory first, so each pass walks the candidates of all splits
+// as one flat range (a split is found by binary search) instead of one
+// split after another.
 // ---------------------------------------------------------------------------
 constexpr int kSelThreads = 256;
+constexpr uint32_t kSelMaxSplits = 1024;
 
+// kq: per-query k (indexed through qlist when given), or null for k.
+// bound_out (non-null): only the bound -- the order-preserving key of the
+// k-th smallest score plus the margin, or +inf's key with at most k
+// candidates -- is written per query; no pool.
 __global__ void __launch_bounds__(kSelThreads) select_cta_kernel(
     const uint64_t* __restrict__ buf, const uint32_t* __restrict__ cnt, const float* __restrict__ qm,
     const float* __restrict__ qq, uint32_t nq, uint32_t splits, uint32_t cap, uint32_t k,
     uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t* __restrict__ pool_n, uint32_t* __restrict__ err,
-    int lenient) {
+    int lenient, const uint32_t* __restrict__ kq, const uint32_t* __restrict__ qlist,
+    uint32_t* __restrict__ bound_out) {
   __shared__ uint32_t hist[256];
   __shared__ uint32_t wsum[kSelThreads / 32];
-  __shared__ uint32_t sh_over, sh_total, sh_bucket, sh_before, sh_count, sh_w;
+  __shared__ uint32_t soff[kSelMaxSplits + 1];
+  __shared__ uint32_t sh_over, sh_bucket, sh_before, sh_count, sh_w;
   const uint32_t q = blockIdx.x;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (kq) k = kq[qlist ? qlist[q] : q];
   if (t == 0) {
     sh_over = 0u;
-    sh_total = 0u;
     sh_w = 0u;
   }
   __syncthreads();
   {
-    uint32_t tot = 0;
+    // thread t owns splits 4t .. 4t + 3: counts, then an exclusive scan
+    constexpr int kPer = kSelMaxSplits / kSelThreads;
+    uint32_t c[kPer], sum = 0;
     bool ov = false;
-    for (uint32_t sp = t; sp < splits; sp += kSelThreads) {
-      const uint32_t c = cnt[static_cast<size_t>(sp) * nq + q];
-      if (c == kOver) ov = true;
-      else tot += min(c, cap);
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const uint32_t sp = static_cast<uint32_t>(kPer * t + i);
+      c[i] = 0u;
+      if (sp < splits) {
+        const uint32_t v = cnt[static_cast<size_t>(sp) * nq + q];
+        if (v == kOver) ov = true;
+        else c[i] = min(v, cap);
+      }
+      sum += c[i];
     }
     if (ov) atomicOr(&sh_over, 1u);
-    if (tot) atomicAdd(&sh_total, tot);
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0;
+    for (int w2 = 0; w2 < warp; ++w2) base += wsum[w2];
+    uint32_t run = base + incl - sum;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      soff[kPer * t + i] = run;
+      run += c[i];
+    }
+    if (t == kSelThreads - 1) soff[kSelMaxSplits] = run;
   }
   __syncthreads();
   if (sh_over) {
     if (t == 0) {
-      pool_n[q] = 0;
-      atomicAdd(err + 1, 1u);
+      if (bound_out) {
+        bound_out[q] = okey(__int_as_float(0x7f800000));
+      } else {
+        pool_n[q] = 0;
+        atomicAdd(err + 1, 1u);
+      }
     }
     return;
   }
-  const uint32_t total = sh_total;
+  const uint32_t total = soff[kSelMaxSplits];
+  // Up to kSelThreads * kSelReg candidates are read once into registers
+  // (thread t holds candidates t, t + 256, ...), and every pass runs over
+  // those; more are re-read from the buffers by each pass.
+  constexpr int kSelReg = 16;
+  const bool in_regs = total <= static_cast<uint32_t>(kSelThreads * kSelReg);
+  uint64_t kv[kSelReg];
+  if (in_regs) {
+    uint32_t sp = 0;  // the split holding candidate i: soff[sp] <= i < soff[sp + 1]
+#pragma unroll
+    for (int j = 0; j < kSelReg; ++j) {
+      const uint32_t i = static_cast<uint32_t>(t + j * kSelThreads);
+      kv[j] = ~0ull;
+      if (i < total) {
+        while (soff[sp + 1] <= i) ++sp;
+        kv[j] = buf[(static_cast<size_t>(sp) * nq + q) * cap + (i - soff[sp])];
+      }
+    }
+  }
   auto for_each = [&](auto&& f) {
-    for (uint32_t sp = 0; sp < splits; ++sp) {
-      const uint32_t m = min(cnt[static_cast<size_t>(sp) * nq + q], cap);
-      const uint64_t* b = buf + (static_cast<size_t>(sp) * nq + q) * cap;
-      for (uint32_t i = t; i < m; i += kSelThreads) f(b[i]);
+    if (in_regs) {
+#pragma unroll
+      for (int j = 0; j < kSelReg; ++j)
+        if (static_cast<uint32_t>(t + j * kSelThreads) < total) f(kv[j]);
+      return;
+    }
+    for (uint32_t i = t; i < total; i += kSelThreads) {
+      uint32_t lo = 0, hi = splits;  // the split sp with soff[sp] <= i < soff[sp + 1]
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (soff[mid] <= i) lo = mid;
+        else hi = mid;
+      }
+      f(buf[(static_cast<size_t>(lo) * nq + q) * cap + (i - soff[lo])]);
     }
   };
   // block-wide count of keys whose bits are <= kb
@@ -726,6 +801,11 @@ __global__ void __launch_bounds__(kSelThreads) select_cta_kernel(
     return prefix;
   };
   float thr = __int_as_float(0x7f800000);
+  if (bound_out) {
+    if (total > k) thr = __fadd_ru(dist_of_key_bits(radix_select(k)), qm[q]);
+    if (t == 0) bound_out[q] = okey(thr);
+    return;
+  }
   if (total > k) {
     const float T = dist_of_key_bits(radix_select(k));
     thr = __fadd_ru(T, qm[q]);
@@ -778,56 +858,186 @@ struct OutMap {
   uint32_t* done;
 };
 
-template <int S, bool L2>
-__global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ rows, const uint64_t* __restrict__ labels,
-                                                     const float* __restrict__ queries, const float* __restrict__ inv,
-                                                     uint32_t nq, uint32_t dim, uint32_t dp, uint32_t k,
-                                                     const uint32_t* __restrict__ pool, uint32_t pool_cap, uint32_t p2max,
-                                                     const uint32_t* __restrict__ pool_n, Rec* __restrict__ out,
-                                                     OutMap om, int neon) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint64_t* keys = reinterpret_cast<uint64_t*>(smem) + static_cast<size_t>(w) * p2max;
-  const uint32_t q = blockIdx.x * 4u + static_cast<uint32_t>(w);
-  if (q >= nq) return;
-  const BfOrder o = bf_order(dim, neon != 0);
-  float qr[S];
-  const float iv = inv ? inv[q] : 1.0f;
-#pragma unroll
-  for (int i = 0; i < S; ++i) {
-    const int e = bslot(o, i, lane);
-    const float v = e >= 0 ? queries[static_cast<size_t>(q) * dim + e] : 0.0f;
-    qr[i] = inv ? __fmul_rn(v, iv) : v;
+// One thread computes one candidate's exact distance in the host kernel's
+// summation order, with that kernel's SIMD lanes as separate accumulators in
+// registers (the warp-per-row forms, bdist / bdist_neon, reduce the same
+// lanes across threads by the same tree), so a query's candidates are all
+// in flight at once instead of one row per round trip.
+//   NEON: 16 chains (element 16i + l into chain l; 4-blocks continue chains
+//   0..3), the tree ((c0+c4)+(c8+c12))+((c1+c5)+(c9+c13)) + ... of the
+//   4 / 8 / 1 / 2 butterfly, then the scalar tail fused in order.
+//   AVX-512: chains A0..A31 and B0..B31 (64-blocks: 64i + l into A_l,
+//   64i + 32 + l into B_l; 16-blocks into A0..A15; the masked remainder into
+//   A16..), s_l = (A_l + A_l+16) + (B_l + B_l+16), then the 8 / 4 / 2 / 1
+//   butterfly over s_0..s_15.
+template <bool L2>
+__device__ __forceinline__ float ex_term(float q, float x, float acc) {
+  if (L2) {
+    const float d = __fsub_rn(q, x);
+    return __fmaf_rn(d, d, acc);
   }
+  return __fmaf_rn(q, x, acc);
+}
+
+template <bool L2>
+__device__ float exact_dist_neon(const float* __restrict__ x, const float* q, uint32_t dim) {
+  const uint32_t n16 = dim / 16, n4 = (dim % 16) / 4, tail = dim % 4;
+  float c[16];
+#pragma unroll
+  for (int l = 0; l < 16; ++l) c[l] = 0.0f;
+  const float4* xv = reinterpret_cast<const float4*>(x);
+  for (uint32_t i = 0; i < n16; ++i) {
+    float4 v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = __ldg(xv + 4 * i + j);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      c[4 * j] = ex_term<L2>(q[16 * i + 4 * j], v[j].x, c[4 * j]);
+      c[4 * j + 1] = ex_term<L2>(q[16 * i + 4 * j + 1], v[j].y, c[4 * j + 1]);
+      c[4 * j + 2] = ex_term<L2>(q[16 * i + 4 * j + 2], v[j].z, c[4 * j + 2]);
+      c[4 * j + 3] = ex_term<L2>(q[16 * i + 4 * j + 3], v[j].w, c[4 * j + 3]);
+    }
+  }
+  for (uint32_t j = 0; j < n4; ++j) {
+    const uint32_t e = 16 * n16 + 4 * j;
+    const float4 v = __ldg(xv + e / 4);
+    c[0] = ex_term<L2>(q[e], v.x, c[0]);
+    c[1] = ex_term<L2>(q[e + 1], v.y, c[1]);
+    c[2] = ex_term<L2>(q[e + 2], v.z, c[2]);
+    c[3] = ex_term<L2>(q[e + 3], v.w, c[3]);
+  }
+  float r2[4];  // lanes 0..3 after the 4 and 8 levels
+#pragma unroll
+  for (int l = 0; l < 4; ++l)
+    r2[l] = __fadd_rn(__fadd_rn(c[l], c[l + 4]), __fadd_rn(c[l + 8], c[l + 12]));
+  float s = __fadd_rn(__fadd_rn(r2[0], r2[1]), __fadd_rn(r2[2], r2[3]));
+  for (uint32_t t = 0; t < tail; ++t) {
+    const uint32_t e = 16 * n16 + 4 * n4 + t;
+    s = ex_term<L2>(q[e], __ldg(x + e), s);
+  }
+  return L2 ? s : __fsub_rn(1.0f, s);
+}
+
+template <bool L2>
+__device__ float exact_dist_avx512(const float* __restrict__ x, const float* q, uint32_t dim) {
+  const uint32_t nb = dim / 64, nt = (dim % 64) / 16, rem = dim % 16;
+  float a[32], b[32];
+#pragma unroll
+  for (int l = 0; l < 32; ++l) a[l] = b[l] = 0.0f;
+  const float4* xv = reinterpret_cast<const float4*>(x);
+  for (uint32_t i = 0; i < nb; ++i) {
+    float4 v[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __ldg(xv + 16 * i + j);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t e = 64 * i + 4 * j;
+      a[4 * j] = ex_term<L2>(q[e], v[j].x, a[4 * j]);
+      a[4 * j + 1] = ex_term<L2>(q[e + 1], v[j].y, a[4 * j + 1]);
+      a[4 * j + 2] = ex_term<L2>(q[e + 2], v[j].z, a[4 * j + 2]);
+      a[4 * j + 3] = ex_term<L2>(q[e + 3], v[j].w, a[4 * j + 3]);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t e = 64 * i + 32 + 4 * j;
+      b[4 * j] = ex_term<L2>(q[e], v[8 + j].x, b[4 * j]);
+      b[4 * j + 1] = ex_term<L2>(q[e + 1], v[8 + j].y, b[4 * j + 1]);
+      b[4 * j + 2] = ex_term<L2>(q[e + 2], v[8 + j].z, b[4 * j + 2]);
+      b[4 * j + 3] = ex_term<L2>(q[e + 3], v[8 + j].w, b[4 * j + 3]);
+    }
+  }
+  for (uint32_t u = 0; u < nt; ++u) {
+    const uint32_t e0 = 64 * nb + 16 * u;
+    float4 v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = __ldg(xv + e0 / 4 + j);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      a[4 * j] = ex_term<L2>(q[e0 + 4 * j], v[j].x, a[4 * j]);
+      a[4 * j + 1] = ex_term<L2>(q[e0 + 4 * j + 1], v[j].y, a[4 * j + 1]);
+      a[4 * j + 2] = ex_term<L2>(q[e0 + 4 * j + 2], v[j].z, a[4 * j + 2]);
+      a[4 * j + 3] = ex_term<L2>(q[e0 + 4 * j + 3], v[j].w, a[4 * j + 3]);
+    }
+  }
+  if (rem) {
+    const uint32_t e0 = 64 * nb + 16 * nt;
+#pragma unroll
+    for (int l = 0; l < 16; ++l)
+      if (static_cast<uint32_t>(l) < rem) a[16 + l] = ex_term<L2>(q[e0 + l], __ldg(x + e0 + l), a[16 + l]);
+  }
+  float sv[16];
+#pragma unroll
+  for (int l = 0; l < 16; ++l) sv[l] = __fadd_rn(__fadd_rn(a[l], a[l + 16]), __fadd_rn(b[l], b[l + 16]));
+  float t8[8];
+#pragma unroll
+  for (int l = 0; l < 8; ++l) t8[l] = __fadd_rn(sv[l], sv[l + 8]);
+  const float s = __fadd_rn(__fadd_rn(__fadd_rn(t8[0], t8[4]), __fadd_rn(t8[2], t8[6])),
+                            __fadd_rn(__fadd_rn(t8[1], t8[5]), __fadd_rn(t8[3], t8[7])));
+  return L2 ? s : __fsub_rn(1.0f, s);
+}
+
+// One CTA per query: the exact distances of the pool, a block bitonic sort,
+// the first k written.  Queries: row q at queries + q * qstride (cosine: times
+// inv[q] when inv is given).  Shared memory: the query (dim rounded up to 4)
+// and p2max keys.
+constexpr int kRerankThreads = 128;
+
+template <bool L2, bool NEON>
+__global__ void __launch_bounds__(kRerankThreads) rerank_kernel(
+    const float* __restrict__ rows, const uint64_t* __restrict__ labels, const float* __restrict__ queries,
+    uint32_t qstride, const float* __restrict__ inv, uint32_t dim, uint32_t dp, uint32_t k,
+    const uint32_t* __restrict__ pool, uint32_t pool_cap, const uint32_t* __restrict__ pool_n, Rec* __restrict__ out,
+    OutMap om) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t dq = (dim + 3u) & ~3u;
+  float* qsm = reinterpret_cast<float*>(smem);
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smem + ((dq * 4u + 15u) & ~15u));
+  const uint32_t q = blockIdx.x;
+  const int t = threadIdx.x;
+  const float iv = inv ? inv[q] : 1.0f;
+  for (uint32_t i = t; i < dq; i += kRerankThreads) {
+    const float v = i < dim ? queries[static_cast<size_t>(q) * qstride + i] : 0.0f;
+    qsm[i] = inv ? __fmul_rn(v, iv) : v;
+  }
+  __syncthreads();
   const uint32_t m = pool_n[q];
   const uint32_t* ids = pool + static_cast<size_t>(q) * pool_cap;
-  for (uint32_t c = 0; c < m; ++c) {
+  for (uint32_t c = t; c < m; c += kRerankThreads) {
     const uint32_t r = ids[c];
-    float x[S];
-#pragma unroll
-    for (int i = 0; i < S; ++i) {
-      const int e = bslot(o, i, lane);
-      x[i] = e >= 0 ? __ldg(rows + static_cast<size_t>(r) * dp + e) : 0.0f;
-    }
-    const float d = bdist<S, L2>(x, qr, o, lane);
-    if (lane == 0) keys[c] = (static_cast<uint64_t>(okey(d)) << 32) | r;
+    const float* x = rows + static_cast<size_t>(r) * dp;
+    const float d = NEON ? exact_dist_neon<L2>(x, qsm, dim) : exact_dist_avx512<L2>(x, qsm, dim);
+    keys[c] = (static_cast<uint64_t>(okey(d)) << 32) | r;
   }
-  int p2 = 1;
-  while (p2 < static_cast<int>(m)) p2 <<= 1;
-  for (int i = static_cast<int>(m) + lane; i < p2; i += 32) keys[i] = ~0ull;
-  __syncwarp();
-  warp_sort(keys, p2, lane);
+  uint32_t p2 = 1;
+  while (p2 < m) p2 <<= 1;
+  for (uint32_t i = m + t; i < p2; i += kRerankThreads) keys[i] = ~0ull;
+  __syncthreads();
+  for (uint32_t kk = 2; kk <= p2; kk <<= 1) {
+    for (uint32_t j = kk >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = t; i < p2; i += kRerankThreads) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const uint64_t x0 = keys[i], x1 = keys[l];
+          if ((x0 > x1) == ((i & kk) == 0)) {
+            keys[i] = x1;
+            keys[l] = x0;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
   const uint32_t orow = om.out_index ? om.out_index[q] : q;
   const uint32_t stride = om.k_stride ? om.k_stride : k;
   const uint32_t kk_row = om.kq ? om.kq[orow] : k;
   const uint32_t mv = m < kk_row ? m : kk_row;
   Rec* row = out + static_cast<size_t>(orow) * stride;
-  for (uint32_t j = lane; j < stride; j += 32) {
+  for (uint32_t j = t; j < stride; j += kRerankThreads) {
     Rec o;
     if (j < mv) {
-      const uint64_t kk = keys[j];
-      o.label = labels[static_cast<uint32_t>(kk)];
-      o.dist = key_dist(kk);
+      const uint64_t kv = keys[j];
+      o.label = labels[static_cast<uint32_t>(kv)];
+      o.dist = key_dist(kv);
     } else {
       o.label = ~0ull;
       o.dist = __int_as_float(0x7f800000);
@@ -837,30 +1047,27 @@ __global__ void __launch_bounds__(128) rerank_kernel(const float* __restrict__ r
   }
   if (om.done) {
     __threadfence_system();
-    __syncwarp();
-    if (lane == 0) *reinterpret_cast<volatile uint32_t*>(om.done + orow) = 1u;
+    __syncthreads();
+    if (t == 0) *reinterpret_cast<volatile uint32_t*>(om.done + orow) = 1u;
   }
 }
 
-
+// nq queries, one CTA each; p2max = the pool capacity rounded up to a power of two
 template <bool L2>
-cudaError_t launch_rerank(int S, dim3 grid, size_t smem, cudaStream_t st, const float* rows, const uint64_t* labels,
-                          const float* queries, const float* inv, uint32_t nq, uint32_t dim, uint32_t dp, uint32_t k,
-                          const uint32_t* pool, uint32_t pool_cap, uint32_t p2max, const uint32_t* pool_n, Rec* out,
-                          OutMap om, bool neon) {
+cudaError_t launch_rerank(uint32_t nq, uint32_t p2max, bool neon, cudaStream_t st, const float* rows,
+                          const uint64_t* labels, const float* queries, uint32_t qstride, const float* inv,
+                          uint32_t dim, uint32_t dp, uint32_t k, const uint32_t* pool, uint32_t pool_cap,
+                          const uint32_t* pool_n, Rec* out, OutMap om) {
+  if (nq == 0) return cudaSuccess;
+  const size_t smem = ((((dim + 3u) & ~3u) * 4u + 15u) & ~15u) + static_cast<size_t>(p2max) * 8u;
   auto go = [&](auto fn) {
     cudaError_t e = open_smem_limit(reinterpret_cast<const void*>(fn));
     if (e != cudaSuccess) return e;
-    fn<<<grid, 128, smem, st>>>(rows, labels, queries, inv, nq, dim, dp, k, pool, pool_cap, p2max, pool_n, out, om,
-                                neon ? 1 : 0);
+    fn<<<nq, kRerankThreads, smem, st>>>(rows, labels, queries, qstride, inv, dim, dp, k, pool, pool_cap, pool_n, out,
+                                         om);
     return cudaGetLastError();
   };
-  if (S <= 6) return go(rerank_kernel<6, L2>);
-  if (S <= 10) return go(rerank_kernel<10, L2>);
-  if (S <= 18) return go(rerank_kernel<18, L2>);
-  if (S <= 34) return go(rerank_kernel<34, L2>);
-  if (S <= 70) return go(rerank_kernel<70, L2>);  // the NEON order of rows above 512 elements
-  return cudaErrorInvalidValue;
+  return neon ? go(rerank_kernel<L2, true>) : go(rerank_kernel<L2, false>);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -915,7 +1122,7 @@ struct Buf {
 
 // Device buffers of one scan, grown on demand and reused across calls.
 struct Scratch {
-  Buf qp, q16, qc, qm, qq, buf, cnt, pool, pool_n, err;
+  Buf qp, q16, qc, qm, qq, buf, cnt, pool, pool_n, err, tiles, gkey;
 };
 
 struct Store {
@@ -1099,19 +1306,14 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "select kernel";
     select_cta_kernel<<<nq, kSelThreads, 0, st>>>(buf, cnt, qm, qq, nq, splits, cap, k, pool, pool_cap, pool_n, derr,
-                                                  0);
+                                                  0, nullptr, nullptr, nullptr);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
-    const int S = bf_slots(r.dim, r.neon != 0);
-    const dim3 rgrid((nq + 3) / 4);
-    const size_t rsmem = 4ull * p2max * 8;
     e = r.metric == HGD_METRIC_L2
-            ? launch_rerank<true>(S, rgrid, rsmem, st, r.rows, r.labels, queries, inv, nq, r.dim, r.dp, k, pool,
-                                  pool_cap, p2max, pool_n, static_cast<Rec*>(out), OutMap{nullptr, nullptr, 0, nullptr},
-                                  r.neon != 0)
-            : launch_rerank<false>(S, rgrid, rsmem, st, r.rows, r.labels, queries, inv, nq, r.dim, r.dp, k, pool,
-                                   pool_cap, p2max, pool_n, static_cast<Rec*>(out),
-                                   OutMap{nullptr, nullptr, 0, nullptr}, r.neon != 0);
+            ? launch_rerank<true>(nq, p2max, r.neon != 0, st, r.rows, r.labels, queries, r.dim, inv, r.dim, r.dp, k,
+                                  pool, pool_cap, pool_n, static_cast<Rec*>(out), OutMap{nullptr, nullptr, 0, nullptr})
+            : launch_rerank<false>(nq, p2max, r.neon != 0, st, r.rows, r.labels, queries, r.dim, inv, r.dim, r.dp, k,
+                                   pool, pool_cap, pool_n, static_cast<Rec*>(out), OutMap{nullptr, nullptr, 0, nullptr});
     if (e != cudaSuccess) break;
     uint32_t herr[4] = {0, 0, 0, 0};
     what = "status";
@@ -1148,15 +1350,396 @@ __global__ void gather_queries_kernel(const float* __restrict__ raw, const float
 }
 
 
+// ---------------------------------------------------------------------------
+// Routed scans over the allowed rows only
+// ---------------------------------------------------------------------------
+// The routed queries of a graph batch are few per filter, and their filters
+// allow a small share of the rows.  The GEMM above reads every row for a tile
+// of 128 queries and holds an SM's shared memory for the whole scan; this
+// kernel reads only the rows a filter allows, for 8 queries at a time, with
+// 16 KB of shared memory per 4 warps, so it runs beside graph walks.
+//
+// One warp per (tile, segment).  A tile is up to 8 consecutive routed queries
+// with the same filter (the host sorts the routed queries by filter); a
+// segment is a range of 32-row words.  A round turns 32 words of allow and
+// alive bits into row ids (a warp scan of their counts), then scores them 16
+// rows per mma.sync m16n8k16 (rows as A, the tile's queries as B, FP32
+// accumulation) straight from the store's FP16 rows with 16-byte loads: lane
+// (g, t) holds the elements [32t, 32t + 32) of a 128-element chunk of rows g
+// and g + 8 and of query g, and uses elements 32t + 4s .. 32t + 4s + 3 at
+// k-step s.  That permutes the dot product's terms, identically for A and
+// B, so the score is the GEMM's s = |x|^2 + acc * qc (or acc * qc) up to the
+// summation order, which the error bound already covers.
+//
+// Candidates go to the same per-(segment, query) buffers, with the same
+// compaction and margin, as the GEMM's.  A compaction's bound is the k-th
+// smallest score of a subset of the rows plus the margin, never below the
+// bound over all rows, so it is safe for every segment: it is published in a
+// per-query word (atomicMin on the order-preserving key) that every segment
+// reads once per round.
+struct SparseParams {
+  const __half* x16;         // n_pad x kp store rows
+  const float* xn;           // n_pad
+  const __half* q16;         // nq_pad x kp prepared routed queries
+  const float* qc;           // per routed query
+  const float* qm;           // per routed query: selection margin
+  const uint32_t* kq;        // per original query k, or null (k)
+  const uint32_t* qlist;     // routed query -> original query
+  const uint2* tiles;        // {first routed query, queries (1..8)}
+  const uint32_t* const* allow_tab;
+  const int32_t* fsel;       // per routed query
+  const uint32_t* alive;     // or null
+  uint64_t* buf;             // segs x nq x cap
+  uint32_t* cnt;             // segs x nq
+  uint32_t* gkey;            // per routed query: tightest published bound (key bits)
+  uint32_t n, nq, kp, cap, k, segs, wps, words, ntiles;
+  int l2;
+  uint32_t sample;  // > 0: only the first `sample` (<= 16) allowed rows of each segment, every score kept
+};
+
+constexpr int kSpWarps = 4;
+constexpr uint32_t kSpRound = 16;  // words per round: one per lane of the lower half
+constexpr uint32_t kNoId = 0xFFFFFFFFu;
+
+struct SparseQ {  // per tile query, warp-uniform (shared memory)
+  uint32_t cnt, lim, trig, k;
+  float margin;
+  uint32_t over;
+};
+
+// CH = kp / 128 chunks per row.  Shared memory per warp: the round's row ids
+// and the lane's B fragments (uint2 per k-step, lane-major: conflict-free).
+template <int CH>
+__global__ void __launch_bounds__(kSpWarps * 32, 4) sparse_scan_kernel(SparseParams P) {
+  __shared__ uint32_t ids_all[kSpWarps][kSpRound * 32];
+  __shared__ uint2 bfrag_all[kSpWarps][CH * 8][32];
+  __shared__ SparseQ qs_all[kSpWarps][8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t gw = blockIdx.x * kSpWarps + static_cast<uint32_t>(warp);
+  const uint32_t tile = gw / P.segs, seg = gw % P.segs;
+  if (tile >= P.ntiles) return;
+  uint32_t* ids = ids_all[warp];
+  uint2 (*bfrag)[32] = bfrag_all[warp];
+  SparseQ* qs = qs_all[warp];
+  const uint2 td = P.tiles[tile];
+  const uint32_t q0 = td.x, nqt = td.y;
+  const int g = lane >> 2, t = lane & 3;
+  const uint32_t* allow = P.allow_tab[P.fsel[q0]];
+  if (lane < static_cast<int>(nqt)) {
+    const uint32_t q = q0 + static_cast<uint32_t>(lane);
+    SparseQ z;
+    z.k = P.kq ? min(P.kq[P.qlist[q]], P.k) : P.k;
+    z.trig = min(P.cap, max(96u, (2u * z.k + 64u + 31u) / 32u * 32u));
+    z.cnt = 0u;
+    z.lim = z.trig;
+    z.margin = P.qm[q];
+    z.over = 0u;
+    qs[lane] = z;
+  }
+  // query g's words [16t, 16t + 16) of each chunk (zero past the tile), as
+  // the B fragments of the eight k-steps
+#pragma unroll
+  for (int c = 0; c < CH; ++c) {
+    uint32_t w[16];
+    if (static_cast<uint32_t>(g) < nqt) {
+      const uint4* p = reinterpret_cast<const uint4*>(P.q16 + static_cast<size_t>(q0 + g) * P.kp + 128 * c + 32 * t);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint4 u = __ldg(p + i);
+        w[4 * i] = u.x;
+        w[4 * i + 1] = u.y;
+        w[4 * i + 2] = u.z;
+        w[4 * i + 3] = u.w;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) w[i] = 0u;
+    }
+#pragma unroll
+    for (int st = 0; st < 8; ++st) bfrag[8 * c + st][lane] = make_uint2(w[2 * st], w[2 * st + 1]);
+  }
+  // this lane's two query columns 2t, 2t + 1
+  const bool va = 2u * t < nqt, vb = 2u * t + 1u < nqt;
+  const uint32_t qa = q0 + 2u * t, qb = qa + 1u;
+  const float cqa = va ? P.qc[qa] : 0.0f, cqb = vb ? P.qc[qb] : 0.0f;
+  uint32_t lka = va ? 0xFF800000u : 0u, lkb = vb ? 0xFF800000u : 0u;  // pass: key <= lk (+inf: all finite)
+  __syncwarp();
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t w_begin = seg * P.wps, w_end = min(P.words, w_begin + P.wps);
+  for (uint32_t wb = w_begin; wb < w_end; wb += kSpRound) {
+    // the tightest bound published so far
+    if (va) lka = min(lka, *reinterpret_cast<volatile const uint32_t*>(P.gkey + qa));
+    if (vb) lkb = min(lkb, *reinterpret_cast<volatile const uint32_t*>(P.gkey + qb));
+    const uint32_t wi = wb + static_cast<uint32_t>(lane);
+    uint32_t bits = 0u;
+    if (lane < static_cast<int>(kSpRound) && wi < w_end) {
+      bits = __ldg(allow + wi);
+      if (P.alive) bits &= __ldg(P.alive + wi);
+      const uint32_t r0 = wi * 32u;
+      if (r0 + 32u > P.n) bits &= P.n > r0 ? ((1u << (P.n - r0)) - 1u) : 0u;  // P.n - r0 < 32 here
+    }
+    const uint32_t c = static_cast<uint32_t>(__popc(bits));
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += u;
+    }
+    const uint32_t m_all = __shfl_sync(kFull, incl, 31);
+    uint32_t pos = incl - c;
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      bits &= bits - 1u;
+      ids[pos++] = wi * 32u + static_cast<uint32_t>(b);
+    }
+    __syncwarp();
+    const uint32_t m = P.sample ? min(m_all, P.sample) : m_all;
+    for (uint32_t base = 0; base < m; base += 16u) {
+      const uint32_t r0 = base + static_cast<uint32_t>(g), r1 = r0 + 8u;
+      const uint32_t i0 = r0 < m ? ids[r0] : kNoId, i1 = r1 < m ? ids[r1] : kNoId;
+      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int ch = 0; ch < CH; ++ch) {
+        uint32_t a[2][16];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t r = h ? i1 : i0;
+          if (r != kNoId) {
+            const uint4* p = reinterpret_cast<const uint4*>(P.x16 + static_cast<size_t>(r) * P.kp + 128 * ch + 32 * t);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const uint4 u = __ldg(p + i);
+              a[h][4 * i] = u.x;
+              a[h][4 * i + 1] = u.y;
+              a[h][4 * i + 2] = u.z;
+              a[h][4 * i + 3] = u.w;
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) a[h][i] = 0u;
+          }
+        }
+#pragma unroll
+        for (int st = 0; st < 8; ++st) {
+          const uint2 b = bfrag[8 * ch + st][lane];
+          sp_mma(acc, a[0][2 * st], a[1][2 * st], a[0][2 * st + 1], a[1][2 * st + 1], b.x, b.y);
+        }
+      }
+      // acc: (row g, column 2t), (row g, 2t + 1), (row g + 8, 2t), (row g + 8, 2t + 1)
+      const float x0 = (P.l2 && i0 != kNoId) ? __ldg(P.xn + i0) : 0.0f;
+      const float x1 = (P.l2 && i1 != kNoId) ? __ldg(P.xn + i1) : 0.0f;
+      auto score = [&](float d, float cq, float x) { return P.l2 ? __fmaf_rn(d, cq, x) : __fmul_rn(d, cq); };
+      const uint32_t ka0 = okey(score(acc[0], cqa, x0)), kb0 = okey(score(acc[1], cqb, x0));
+      const uint32_t ka1 = okey(score(acc[2], cqa, x1)), kb1 = okey(score(acc[3], cqb, x1));
+      const bool pa0 = i0 != kNoId && ka0 <= lka, pb0 = i0 != kNoId && kb0 <= lkb;
+      const bool pa1 = i1 != kNoId && ka1 <= lka, pb1 = i1 != kNoId && kb1 <= lkb;
+      if (!__any_sync(kFull, pa0 || pb0 || pa1 || pb1)) continue;  // the common case once bounds settle
+#pragma unroll 1
+      for (int j = 0; j < 8; ++j) {
+        const bool mine = t == (j >> 1);
+        const bool p0 = mine && ((j & 1) ? pb0 : pa0), p1 = mine && ((j & 1) ? pb1 : pa1);
+        const uint32_t bal0 = __ballot_sync(kFull, p0), bal1 = __ballot_sync(kFull, p1);
+        if ((bal0 | bal1) == 0u) continue;
+        const uint32_t q = q0 + static_cast<uint32_t>(j);
+        uint64_t* bufp = P.buf + (static_cast<size_t>(seg) * P.nq + q) * P.cap;
+        const uint32_t c0 = qs[j].cnt;
+        const uint32_t n0 = static_cast<uint32_t>(__popc(bal0));
+        if (p0) bufp[c0 + __popc(bal0 & lt_mask)] = (static_cast<uint64_t>((j & 1) ? kb0 : ka0) << 32) | i0;
+        if (p1) bufp[c0 + n0 + __popc(bal1 & lt_mask)] = (static_cast<uint64_t>((j & 1) ? kb1 : ka1) << 32) | i1;
+        const uint32_t c1 = c0 + n0 + static_cast<uint32_t>(__popc(bal1));
+        __syncwarp();
+        if (c1 + 16u <= qs[j].lim) {
+          __syncwarp();
+          if (lane == 0) qs[j].cnt = c1;
+          __syncwarp();
+          continue;
+        }
+        // room for the next group: compact, publish the bound
+        float thr;
+        const uint32_t kept = warp_compact(bufp, c1, qs[j].k, qs[j].margin, lane, &thr);
+        const uint32_t key = okey(thr);
+        const bool over = kept + 16u > P.cap;  // the margin keeps too many rows: stop adding (lenient)
+        if (mine) {
+          if (j & 1) lkb = over ? 0u : min(lkb, key);
+          else lka = over ? 0u : min(lka, key);
+        }
+        __syncwarp();
+        if (lane == 0) {
+          qs[j].cnt = kept;
+          qs[j].lim = min(P.cap, max(qs[j].trig, kept + 64u));
+          qs[j].over = over ? 1u : 0u;
+          if (!over) atomicMin(P.gkey + q, key);
+        }
+        __syncwarp();
+      }
+    }
+    __syncwarp();
+    if (P.sample && m > 0) break;  // the segment's sample is taken
+  }
+  __syncwarp();
+  if (lane < static_cast<int>(nqt)) P.cnt[static_cast<size_t>(seg) * P.nq + q0 + lane] = qs[lane].cnt;
+}
+
 }  // namespace
 
 
 Scratch* scratch_new() { return new Scratch(); }
 void scratch_free(Scratch* s) { delete s; }
 
+namespace {
+
+// Tiles of the sparse scan: runs of routed queries with the same filter
+// (fsel sorted), cut into pieces of at most 8.
+std::vector<uint2> routed_tiles(const int32_t* fsel, uint32_t n_r) {
+  std::vector<uint2> tiles;
+  for (uint32_t i = 0; i < n_r;) {
+    uint32_t j = i + 1;
+    while (j < n_r && j - i < 8 && fsel[j] == fsel[i]) ++j;
+    tiles.push_back(make_uint2(i, j - i));
+    i = j;
+  }
+  return tiles;
+}
+
+cudaError_t routed_sparse(Store* s, const Rows& r, const RoutedArgs& a, Scratch* sc, cudaStream_t st,
+                          const std::vector<uint2>& tiles, const char** what) {
+  const uint32_t n_r = a.n_r;
+  const uint32_t k = a.k_stride;
+  const uint32_t nq_pad = round_up(n_r, BM);
+  const uint32_t T = static_cast<uint32_t>(tiles.size());
+  const uint32_t words = (r.n + 31) / 32;
+  // segments: about 128 allowed rows (8 groups) per warp for the largest
+  // filter, at most 8192 warps in all and kSelMaxSplits per tile.  The
+  // sample pass (16 rows of every segment) bounds each query's scores
+  // before the scan, so the number of segments does not add candidates.
+  uint64_t max_ones = 1;
+  for (const uint2& t : tiles) max_ones = std::max<uint64_t>(max_ones, a.h_ones[a.h_fsel[t.x]]);
+  uint32_t segs = static_cast<uint32_t>(std::min<uint64_t>(kSelMaxSplits, (max_ones + 127) / 128));
+  segs = std::max<uint32_t>(1, std::min<uint32_t>(segs, std::max<uint32_t>(1, 8192 / T)));
+  const uint32_t wps = round_up((words + segs - 1) / segs, kSpRound);
+  segs = std::max<uint32_t>(1, (words + wps - 1) / wps);
+  const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
+  const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(2 * cap, 32));
+  uint32_t p2max = 1;
+  while (p2max < pool_cap) p2max <<= 1;
+  cudaError_t e = cudaSuccess;
+  *what = "alloc";
+  if ((e = sc->qp.ensure(static_cast<size_t>(n_r) * r.dp * 4)) != cudaSuccess) return e;
+  if ((e = sc->q16.ensure(static_cast<size_t>(nq_pad) * s->kp * 2)) != cudaSuccess) return e;
+  if ((e = sc->qc.ensure(nq_pad * 4ull)) != cudaSuccess) return e;
+  if ((e = sc->qm.ensure(nq_pad * 4ull)) != cudaSuccess) return e;
+  if ((e = sc->qq.ensure(nq_pad * 4ull)) != cudaSuccess) return e;
+  if ((e = sc->buf.ensure(static_cast<size_t>(segs) * n_r * cap * 8)) != cudaSuccess) return e;
+  if ((e = sc->cnt.ensure(static_cast<size_t>(segs) * n_r * 4)) != cudaSuccess) return e;
+  if ((e = sc->pool.ensure(static_cast<size_t>(n_r) * pool_cap * 4)) != cudaSuccess) return e;
+  if ((e = sc->pool_n.ensure(n_r * 4ull)) != cudaSuccess) return e;
+  if ((e = sc->err.ensure(16)) != cudaSuccess) return e;
+  if ((e = sc->tiles.ensure(T * sizeof(uint2))) != cudaSuccess) return e;
+  if ((e = sc->gkey.ensure(n_r * 4ull)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(sc->err.p, 0, 16, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(sc->gkey.p, 0xFF, n_r * 4ull, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(sc->tiles.p, tiles.data(), T * sizeof(uint2), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return e;
+  *what = "gather kernel";
+  gather_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(n_r) * 32 + 255) / 256), 256, 0, st>>>(
+      a.queries, a.inv, a.qlist, n_r, a.dim, r.dp, sc->qp.as<float>());
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  *what = "query kernel";
+  prep_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(nq_pad) * 32 + 255) / 256), 256, 0, st>>>(
+      sc->qp.as<float>(), nullptr, n_r, nq_pad, r.dim, s->kp, r.metric == HGD_METRIC_L2 ? 1 : 0, s->db,
+      sc->q16.as<__half>(), sc->qc.as<float>(), sc->qm.as<float>(), sc->qq.as<float>());
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  SparseParams P{};
+  P.x16 = s->x16;
+  P.xn = s->xn;
+  P.q16 = sc->q16.as<__half>();
+  P.qc = sc->qc.as<float>();
+  P.qm = sc->qm.as<float>();
+  P.kq = a.kq;
+  P.qlist = a.qlist;
+  P.tiles = sc->tiles.as<uint2>();
+  P.allow_tab = a.allow_tab;
+  P.fsel = a.fsel;
+  P.alive = a.alive;
+  P.buf = sc->buf.as<uint64_t>();
+  P.cnt = sc->cnt.as<uint32_t>();
+  P.gkey = sc->gkey.as<uint32_t>();
+  P.n = r.n;
+  P.nq = n_r;
+  P.kp = s->kp;
+  P.cap = cap;
+  P.k = k;
+  P.segs = segs;
+  P.wps = wps;
+  P.words = words;
+  P.ntiles = T;
+  P.l2 = r.metric == HGD_METRIC_L2 ? 1 : 0;
+  const unsigned grid = static_cast<unsigned>((static_cast<uint64_t>(T) * segs + kSpWarps - 1) / kSpWarps);
+  auto scan = [&](uint32_t sample) {
+    P.sample = sample;
+    switch (s->kp / 128) {
+      case 1: sparse_scan_kernel<1><<<grid, kSpWarps * 32, 0, st>>>(P); break;
+      case 2: sparse_scan_kernel<2><<<grid, kSpWarps * 32, 0, st>>>(P); break;
+      case 3: sparse_scan_kernel<3><<<grid, kSpWarps * 32, 0, st>>>(P); break;
+      case 4: sparse_scan_kernel<4><<<grid, kSpWarps * 32, 0, st>>>(P); break;
+      default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+  };
+  // the sample (at most 4096 rows per query, held in the bound kernel's
+  // registers) and its bound (the k-th smallest sampled score + the margin
+  // bounds the k-th smallest of all rows from above), then the scan
+  *what = "sample scan kernel";
+  if ((e = scan(std::max<uint32_t>(1, std::min<uint32_t>(16, 4096 / segs)))) != cudaSuccess) return e;
+  *what = "bound kernel";
+  select_cta_kernel<<<n_r, kSelThreads, 0, st>>>(sc->buf.as<uint64_t>(), sc->cnt.as<uint32_t>(), sc->qm.as<float>(),
+                                                 sc->qq.as<float>(), n_r, segs, cap, k, nullptr, 0, nullptr,
+                                                 sc->err.as<uint32_t>(), 1, a.kq, a.qlist, sc->gkey.as<uint32_t>());
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  *what = "sparse scan kernel";
+  if ((e = scan(0)) != cudaSuccess) return e;
+  *what = "select kernel";
+  select_cta_kernel<<<n_r, kSelThreads, 0, st>>>(sc->buf.as<uint64_t>(), sc->cnt.as<uint32_t>(), sc->qm.as<float>(),
+                                                 sc->qq.as<float>(), n_r, segs, cap, k, sc->pool.as<uint32_t>(),
+                                                 pool_cap, sc->pool_n.as<uint32_t>(), sc->err.as<uint32_t>(), 1, a.kq,
+                                                 a.qlist, nullptr);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  *what = "rerank kernel";
+  const OutMap om{a.qlist, a.kq, a.k_stride, a.done};
+  return r.metric == HGD_METRIC_L2
+             ? launch_rerank<true>(n_r, p2max, r.neon != 0, st, r.rows, r.labels, sc->qp.as<float>(), r.dp, nullptr,
+                                   r.dim, r.dp, k, sc->pool.as<uint32_t>(), pool_cap, sc->pool_n.as<uint32_t>(),
+                                   static_cast<Rec*>(a.out), om)
+             : launch_rerank<false>(n_r, p2max, r.neon != 0, st, r.rows, r.labels, sc->qp.as<float>(), r.dp, nullptr,
+                                    r.dim, r.dp, k, sc->pool.as<uint32_t>(), pool_cap, sc->pool_n.as<uint32_t>(),
+                                    static_cast<Rec*>(a.out), om);
+}
+
+// Whether the allowed-rows scan reads fewer bytes than the GEMM (within 2x:
+// it also runs beside the walks, the GEMM holds whole SMs).
+bool routed_prefers_rows(uint32_t kp, const int32_t* fsel, uint32_t n_r, const uint64_t* ones, uint32_t n) {
+  if (kp % 128 != 0 || kp > 512 || n_r == 0) return false;
+  const std::vector<uint2> tiles = routed_tiles(fsel, n_r);
+  uint64_t rows = 0;
+  for (const uint2& t : tiles) rows += ones[fsel[t.x]];
+  const uint64_t tiles_q = (n_r + BM - 1) / BM;
+  return rows <= 2ull * tiles_q * n;
+}
+
+}  // namespace
+
 cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch* sc, cudaStream_t st,
                           std::string* err) {
   if (a.n_r == 0) return cudaSuccess;
+  const char* what = "alloc";
+  bool rows_only = a.h_fsel != nullptr && a.h_ones != nullptr && s->kp % 128 == 0 && s->kp <= 512;
+  if (rows_only && a.mode == HGD_SCAN_AUTO) rows_only = routed_prefers_rows(s->kp, a.h_fsel, a.n_r, a.h_ones, r.n);
+  if (rows_only && a.mode == HGD_SCAN_EVERY_ROW) rows_only = false;
+  if (rows_only) {
+    const cudaError_t e = routed_sparse(s, r, a, sc, st, routed_tiles(a.h_fsel, a.n_r), &what);
+    if (e != cudaSuccess && err) *err = std::string("routed scan: ") + what + ": " + cudaGetErrorString(e);
+    return e;
+  }
   const uint32_t n_r = a.n_r;
   const uint32_t k = a.k_stride;
   const uint32_t nq_pad = round_up(n_r, BM);
@@ -1170,7 +1753,6 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
   uint32_t p2max = 1;
   while (p2max < pool_cap) p2max <<= 1;
   cudaError_t e = cudaSuccess;
-  const char* what = "alloc";
   do {
     if ((e = sc->qp.ensure(static_cast<size_t>(n_r) * r.dp * 4)) != cudaSuccess) break;
     if ((e = sc->q16.ensure(static_cast<size_t>(nq_pad) * s->kp * 2)) != cudaSuccess) break;
@@ -1230,19 +1812,18 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     what = "select kernel";
     select_cta_kernel<<<n_r, kSelThreads, 0, st>>>(sc->buf.as<uint64_t>(), sc->cnt.as<uint32_t>(), sc->qm.as<float>(),
                                                    sc->qq.as<float>(), n_r, splits, cap, k, sc->pool.as<uint32_t>(),
-                                                   pool_cap, sc->pool_n.as<uint32_t>(), sc->err.as<uint32_t>(), 1);    if ((e = cudaGetLastError()) != cudaSuccess) break;
+                                                   pool_cap, sc->pool_n.as<uint32_t>(), sc->err.as<uint32_t>(), 1, a.kq,
+                                                   a.qlist, nullptr);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
-    const int S = bf_slots(r.dim, r.neon != 0);
-    const dim3 rgrid((n_r + 3) / 4);
-    const size_t rsmem = 4ull * p2max * 8;
     const OutMap om{a.qlist, a.kq, a.k_stride, a.done};
     e = r.metric == HGD_METRIC_L2
-            ? launch_rerank<true>(S, rgrid, rsmem, st, r.rows, r.labels, sc->qp.as<float>(), nullptr, n_r, r.dim,
-                                  r.dp, k, sc->pool.as<uint32_t>(), pool_cap, p2max, sc->pool_n.as<uint32_t>(),
-                                  static_cast<Rec*>(a.out), om, r.neon != 0)
-            : launch_rerank<false>(S, rgrid, rsmem, st, r.rows, r.labels, sc->qp.as<float>(), nullptr, n_r, r.dim,
-                                   r.dp, k, sc->pool.as<uint32_t>(), pool_cap, p2max, sc->pool_n.as<uint32_t>(),
-                                   static_cast<Rec*>(a.out), om, r.neon != 0);
+            ? launch_rerank<true>(n_r, p2max, r.neon != 0, st, r.rows, r.labels, sc->qp.as<float>(), r.dp, nullptr,
+                                  r.dim, r.dp, k, sc->pool.as<uint32_t>(), pool_cap, sc->pool_n.as<uint32_t>(),
+                                  static_cast<Rec*>(a.out), om)
+            : launch_rerank<false>(n_r, p2max, r.neon != 0, st, r.rows, r.labels, sc->qp.as<float>(), r.dp, nullptr,
+                                   r.dim, r.dp, k, sc->pool.as<uint32_t>(), pool_cap, sc->pool_n.as<uint32_t>(),
+                                   static_cast<Rec*>(a.out), om);
   } while (false);
   if (e != cudaSuccess && err) *err = std::string("tensor scan: ") + what + ": " + cudaGetErrorString(e);
   return e;

@@ -51,6 +51,12 @@ struct RoutedArgs {
   const uint32_t* kq;                // device per original query k, or null (k_stride)
   void* out;                         // device records, original query rows of k_stride
   uint32_t* done;                    // device per original query done flags or null
+  // Host copies for the choice of scan: per routed query its filter index
+  // (sorted, so queries of one filter are consecutive) and per filter the
+  // number of rows it allows.  Without them the GEMM over every row runs.
+  const int32_t* h_fsel;
+  const uint64_t* h_ones;
+  int mode;                          // HGD_SCAN_*: which scan (auto: fewer bytes)
 };
 struct Scratch;
 Scratch* scratch_new();

@@ -610,16 +610,20 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
   // ---- compressed-precision batches: restrictive filters go to the exact scan ----
   std::vector<uint32_t> r_qlist;
   std::vector<int32_t> r_fsel;
+  std::vector<uint64_t> r_ones;  // per filter: rows it allows
   const uint8_t* d_skip = nullptr;
+  if (a->filter_scan_mode > HGD_SCAN_EVERY_ROW) return fail(HGD_EINVAL, "hgd_search: unknown filter_scan_mode");
   if (a->precision != HGD_PREC_FP32 && a->filter_scan_permille && a->num_filters && !a->nres && !a->counters &&
       hg::bfm::supported(static_cast<uint32_t>(g->pd), a->k)) {
     std::vector<char> routed(a->num_filters, 0);
+    r_ones.assign(a->num_filters, 0);
     bool any = false;
     for (uint32_t f = 0; f < a->num_filters; ++f) {
       const hgd_bitset& bs = a->filters[f];
       uint64_t ones = 0;
       const uint64_t words64 = (bs.num_bits + 63) / 64;
       for (uint64_t i = 0; i < words64; ++i) ones += static_cast<uint64_t>(__builtin_popcountll(bs.words[i]));
+      r_ones[f] = ones;
       routed[f] = ones * 1000 <= static_cast<uint64_t>(a->filter_scan_permille) * g->n;
       any = any || routed[f];
     }
@@ -630,9 +634,14 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
         if (f >= 0 && routed[f]) {
           skip[q] = 1;
           r_qlist.push_back(static_cast<uint32_t>(q));
-          r_fsel.push_back(f);
         }
       }
+      // grouped by filter (the allowed-rows scan tiles the queries of one
+      // filter together), in query order within a filter
+      std::stable_sort(r_qlist.begin(), r_qlist.end(), [&](uint32_t x, uint32_t y) {
+        return (a->filter_of_query ? a->filter_of_query[x] : 0) < (a->filter_of_query ? a->filter_of_query[y] : 0);
+      });
+      for (uint32_t q : r_qlist) r_fsel.push_back(a->filter_of_query ? a->filter_of_query[q] : 0);
       if (!r_qlist.empty()) {
         HG_CUDA(w->scan_route.ensure(nq));
         HG_CUDA(w->scan_qlist.ensure(r_qlist.size() * 4));
@@ -914,6 +923,9 @@ int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStre
     ra.kq = d_k;
     ra.out = d_out;
     ra.done = a->done_flags;
+    ra.h_fsel = r_fsel.data();
+    ra.h_ones = r_ones.data();
+    ra.mode = static_cast<int>(a->filter_scan_mode);
     std::string err;
     if (hg::bfm::search_routed(g->scan, rows, ra, w->scan_sc, w->scan_stream, &err) != cudaSuccess)
       return fail(HGD_ECUDA, err);

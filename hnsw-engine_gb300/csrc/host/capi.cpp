@@ -188,6 +188,7 @@ int hg_index_search_batch_ex(const hg_index* idx, const float* qs, size_t nq, si
       opt.rerank_factor = o->rerank_factor;
       opt.warps_per_query = o->warps_per_query;
       opt.lists_per_step = o->lists_per_step;
+      opt.filter_scan_mode = o->filter_scan_mode;
     }
     idx->index.search_batch_ex(qs, nq, k, ef, reinterpret_cast<hnsw::Neighbor*>(out), opt);
   });

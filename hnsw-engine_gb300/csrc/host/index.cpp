@@ -130,6 +130,7 @@ void Index::search_batch_ex(const float* qs, std::size_t nq, std::size_t k, std:
   a.rerank_factor = opt.rerank_factor;
   a.warps_per_query = opt.warps_per_query;
   a.lists_per_step = opt.lists_per_step;
+  a.filter_scan_mode = opt.filter_scan_mode;
   a.hash_slots = opt.hash_slots;
   a.cand_cap = opt.cand_cap;
   a.warps_per_block = opt.warps_per_block;

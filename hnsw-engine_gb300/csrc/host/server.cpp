@@ -103,6 +103,7 @@ class Server {
     rerank_factor_ = cfg.rerank_factor;
     warps_per_query_ = cfg.warps_per_query;
     lists_per_step_ = cfg.lists_per_step;
+    filter_scan_mode_ = cfg.filter_scan_mode;
     {
       std::shared_lock<std::shared_mutex> lk(im.api_mutex);
       g_ = im.device_graph();
@@ -339,6 +340,7 @@ class Server {
       a.rerank_factor = rerank_factor_;
       a.warps_per_query = warps_per_query_;
       a.lists_per_step = lists_per_step_;
+      a.filter_scan_mode = filter_scan_mode_;
       a.stream = s.stream;
       a.synchronize = 0;
       rc = hgd_search(g_, &a);
@@ -445,6 +447,7 @@ class Server {
   uint32_t rerank_factor_ = 0;
   uint32_t warps_per_query_ = 1;
   uint32_t lists_per_step_ = 0;
+  uint32_t filter_scan_mode_ = 0;
   uint64_t budget_ = 0, inflight_bytes_ = 0;
   std::mutex mu_;
   std::condition_variable cv_, cv_done_;

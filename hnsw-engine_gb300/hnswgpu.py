@@ -41,13 +41,15 @@ class _BatchOptions(C.Structure):
                 ("hash_slots", C.c_uint32), ("cand_cap", C.c_uint32), ("warps_per_block", C.c_uint32),
                 ("pool_cap", C.c_uint32), ("queries_on_device", C.c_int32), ("out_on_device", C.c_int32),
                 ("filter_scan_permille", C.c_uint32), ("rerank_factor", C.c_uint32),
-                ("warps_per_query", C.c_uint32), ("lists_per_step", C.c_uint32)]
+                ("warps_per_query", C.c_uint32), ("lists_per_step", C.c_uint32),
+                ("filter_scan_mode", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class _ServerConfig(C.Structure):
     _fields_ = [("max_inflight", C.c_uint32), ("max_batch_queries", C.c_uint32), ("memory_budget", C.c_uint64),
                 ("precision", C.c_int32), ("filter_scan_permille", C.c_uint32), ("rerank_factor", C.c_uint32),
-                ("warps_per_query", C.c_uint32), ("lists_per_step", C.c_uint32), ("reserved", C.c_uint32)]
+                ("warps_per_query", C.c_uint32), ("lists_per_step", C.c_uint32),
+                ("filter_scan_mode", C.c_uint32)]
 
 
 class _Request(C.Structure):
@@ -166,6 +168,15 @@ def _lists_per_step(v) -> int:
     if not 0 <= v <= 4:
         raise ValueError("lists_per_step must be 0 (the reference's order) or 1..4 (beam search)")
     return v
+
+
+SCAN_MODES = {"auto": 0, "allowed_rows": 1, "every_row": 2}
+
+
+def _scan_mode(v) -> int:
+    if v not in SCAN_MODES:
+        raise ValueError("filter_scan_mode must be 'auto', 'allowed_rows' or 'every_row'")
+    return SCAN_MODES[v]
 
 
 def _float_matrix(x, name: str) -> np.ndarray:
@@ -350,10 +361,12 @@ class Index:
                         filter_of_query=None, stream=None, precision: int = 0, counters: bool = False,
                         hash_slots: int = 0, cand_cap: int = 0, warps_per_block: int = 0, pool_cap: int = 0,
                         out=None, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1,
-                        lists_per_step: int = 0):
+                        lists_per_step: int = 0, filter_scan_mode: str = "auto"):
         """search_batch with per-query ef / k / filter.  filter_scan (FP16 / FP8
         only): queries whose filter allows at most this fraction of the nodes
-        are answered by the exact tensor-core scan instead of a graph walk.
+        are answered by an exact tensor-core scan instead of a graph walk;
+        filter_scan_mode picks it: 'allowed_rows' (only the rows the filter
+        allows), 'every_row' (the GEMM over all rows) or 'auto' (fewer bytes).
         rerank_factor (FP16 / FP8 only): the exact FP32 rerank covers the best
         rerank_factor x k entries of the traversal pool (at least 32); 0 = all.
         warps_per_query=4 (FP16 / FP8, dim <= 128): four warps walk each query
@@ -373,6 +386,7 @@ class Index:
         opt.rerank_factor = _rerank_factor(rerank_factor)
         opt.warps_per_query = _warps_per_query(warps_per_query)
         opt.lists_per_step = _lists_per_step(lists_per_step)
+        opt.filter_scan_mode = _scan_mode(filter_scan_mode)
         keep = []
         if ef_per_query is not None:
             a = np.ascontiguousarray(ef_per_query, dtype=np.uint32)
@@ -598,18 +612,20 @@ class Server:
     with those, filter_scan answers requests whose filter allows at most that
     fraction of the nodes by the exact tensor-core scan, rerank_factor limits
     the rerank to the pool's best rerank_factor x k, warps_per_query=4
-    walks each query with four warps (beam search: lower latency), and
+    walks each query with four warps (beam search: lower latency),
     lists_per_step=1..4 walks it with one warp expanding that many lists per
-    step (beam search, tensor-core distances: throughput)."""
+    step (beam search, tensor-core distances: throughput), and
+    filter_scan_mode picks the exact scan as in Index.search_batch_ex."""
 
     def __init__(self, index: Index, max_inflight: int = 4, max_batch_queries: int = 4096, memory_budget: int = 0,
                  precision: int = 0, filter_scan: float = 0.0, rerank_factor: int = 0, warps_per_query: int = 1,
-                 lists_per_step: int = 0):
+                 lists_per_step: int = 0, filter_scan_mode: str = "auto"):
         self._h = None
         self._index = index  # keep the index alive
         cfg = _ServerConfig(max_inflight, max_batch_queries, memory_budget, precision,
                             int(round(filter_scan * 1000)), _rerank_factor(rerank_factor),
-                            _warps_per_query(warps_per_query), _lists_per_step(lists_per_step), 0)
+                            _warps_per_query(warps_per_query), _lists_per_step(lists_per_step),
+                            _scan_mode(filter_scan_mode))
         h = C.c_void_p()
         _check(lib().hg_server_create(index._h, C.byref(cfg), C.byref(h)))
         self._h = h

@@ -68,6 +68,9 @@ struct SearchOptions {
   /// distances on the tensor cores (throughput; not the reference's visit
   /// order); 0 = the one-warp walk in the reference's order
   uint32_t lists_per_step = 0;
+  /// the exact scan of routed queries: 0 auto (fewer bytes), 1 only the
+  /// rows the filter allows, 2 every row (the tcgen05 GEMM)
+  uint32_t filter_scan_mode = 0;
 };
 
 class Index {

@@ -40,6 +40,11 @@ enum { HG_OK = 0, HG_EINVAL = 1, HG_ERUNTIME = 2, HG_ERANGE = 3 };
 enum { HG_METRIC_L2 = 0, HG_METRIC_IP = 1, HG_METRIC_COSINE = 2 };
 enum { HG_ORDER_SCALAR = 0, HG_ORDER_AVX2 = 1, HG_ORDER_AVX512 = 2, HG_ORDER_NEON = 3 };
 enum { HG_FILTER_NONE = 0, HG_FILTER_BITSET = 1, HG_FILTER_PREDICATE = 2 };
+/* The exact scan of routed filtered queries: AUTO = the one that reads fewer
+ * bytes; ALLOWED_ROWS = only the rows the filter allows (tensor-core tiles
+ * of 8 queries; padded row width a multiple of 128, at most 512); EVERY_ROW
+ * = the tcgen05 GEMM over all rows (tiles of 128 queries). */
+enum { HG_SCAN_AUTO = 0, HG_SCAN_ALLOWED_ROWS = 1, HG_SCAN_EVERY_ROW = 2 };
 
 #define HG_INVALID_LABEL (~(uint64_t)0)
 
@@ -97,6 +102,8 @@ typedef struct {
                                       warp walks each query as a beam search expanding this many
                                       lists per step, distances on the tensor cores; 0 = the
                                       one-warp walk in the reference's order */
+  uint32_t filter_scan_mode;       /* HG_SCAN_*: the exact scan of routed queries */
+  uint32_t reserved;
 } hg_batch_options;
 
 const char* hg_last_error(void);
@@ -201,7 +208,7 @@ typedef struct {
                                     (beam search, lower latency); 0 / 1 = one warp */
   uint32_t lists_per_step;       /* precision 1 / 2, dim <= 128: one warp per query, a beam search
                                     expanding this many lists per step (1..4); 0 = off */
-  uint32_t reserved;
+  uint32_t filter_scan_mode;     /* HG_SCAN_*: the exact scan of routed requests */
 } hg_server_config;
 typedef struct {
   const float* queries;        /* nq x dim */

@@ -42,6 +42,13 @@ enum { HGD_ORDER_SCALAR = 0, HGD_ORDER_AVX2 = 1, HGD_ORDER_AVX512 = 2, HGD_ORDER
  * vectors and rerank the final pool in exact FP32. */
 enum { HGD_PREC_FP32 = 0, HGD_PREC_FP16 = 1, HGD_PREC_FP8 = 2 };
 
+/* The exact scan that answers routed filtered queries (filter_scan_permille):
+ * AUTO picks the one that reads fewer bytes; ALLOWED_ROWS reads only the rows
+ * the query's filter allows, 8 queries per tensor-core tile (rows of <= 512
+ * padded elements, a multiple of 128); EVERY_ROW is the tcgen05 GEMM over all
+ * rows, 128 queries per tile, with the filter applied to its scores. */
+enum { HGD_SCAN_AUTO = 0, HGD_SCAN_ALLOWED_ROWS = 1, HGD_SCAN_EVERY_ROW = 2 };
+
 #define HGD_NCOUNTERS 8 /* per query: upper lists, upper distances, layer-0 lists,
                            layer-0 distances, visited, peak candidates, results,
                            tier flags (1 global visited set, 2 spill pool, 4 rerun) */
@@ -93,7 +100,7 @@ typedef struct {
   const uint32_t* k_per_query;   /* nullable */
   const hgd_bitset* filters;     /* host array of num_filters bitsets */
   uint32_t num_filters;
-  uint32_t reserved;
+  uint32_t filter_scan_mode;     /* HGD_SCAN_*: the scan of routed queries (see filter_scan_permille) */
   const int32_t* filter_of_query; /* host, nq entries, -1 = unfiltered; NULL: filter 0 for all if any */
   void* out;                     /* nq*k records */
   uint32_t* nres;                /* nullable: per-query result count (no padding) */
