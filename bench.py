@@ -527,10 +527,13 @@ SERVE_FORMS = (
     # name, server options (batch slots and batch size: 4 x 8,192 queries
     # unless given; smaller batches trade peak for latency)
     ("fp32", dict(precision=0)),
-    ("fp16_beam4_scan", dict(precision=1, filter_scan=0.15, rerank_factor=4, lists_per_step=4)),
+    ("fp16_beam4_scan_8x2048", dict(precision=1, filter_scan=0.15, rerank_factor=4, lists_per_step=4,
+                                    max_inflight=8, max_batch_queries=2048)),
     ("fp8_4warps_scan", dict(precision=2, filter_scan=0.15, rerank_factor=4, warps_per_query=4)),
-    ("fp8_4warps_scan_12x1024", dict(precision=2, filter_scan=0.15, rerank_factor=4, warps_per_query=4,
-                                     max_inflight=12, max_batch_queries=1024)),
+    ("fp8_4warps_scan_8x2048", dict(precision=2, filter_scan=0.15, rerank_factor=4, warps_per_query=4,
+                                    max_inflight=8, max_batch_queries=2048)),
+    ("fp8_4warps_scan_15x256", dict(precision=2, filter_scan=0.15, rerank_factor=4, warps_per_query=4,
+                                    max_inflight=15, max_batch_queries=256)),
 )
 
 
@@ -654,6 +657,12 @@ def run_serving(local, gpath):
     out["served_compressed_form"] = best
     out["served_compressed_over_batched_fp32"] = round(out[best]["peak_qps"] / plain_qps, 3)
     out["served_compressed_over_served_fp32"] = round(out[best]["peak_qps"] / out["fp32"]["peak_qps"], 3)
+    # the compressed form with the lowest p99 at half of its own peak
+    half = {n: next(x for x in out[n]["loads"] if x["offered"] == 0.5) for n, o in SERVE_FORMS if o["precision"]}
+    low = min(half, key=lambda n: half[n]["p99_ms"])
+    out["lowest_p99_at_half_load"] = {"form": low, "p99_ms": half[low]["p99_ms"], "p50_ms": half[low]["p50_ms"],
+                                      "peak_qps": out[low]["peak_qps"],
+                                      "peak_over_batched_fp32": round(out[low]["peak_qps"] / plain_qps, 3)}
     return out
 
 

@@ -131,6 +131,7 @@ class Server {
       stop_ = true;
     }
     cv_.notify_all();
+    cv_launched_.notify_all();
     dispatcher_.join();
     completer_.join();
     for (auto& s : slots_) {
@@ -367,6 +368,7 @@ class Server {
       return;
     }
     launched_.push_back(&s);
+    cv_launched_.notify_one();
   }
 
   // Returns every request of a launched batch whose done flags are all up,
@@ -377,7 +379,9 @@ class Server {
     std::vector<ServerRequest*> finished;
     for (;;) {
       {
-        std::lock_guard<std::mutex> lk(mu_);
+        std::unique_lock<std::mutex> lk(mu_);
+        // nothing in flight: sleep until a batch is launched (or the server stops)
+        cv_launched_.wait(lk, [&] { return stop_ || !launched_.empty(); });
         if (stop_ && launched_.empty() && pending_.empty()) {
           bool any = false;
           for (auto& s : slots_) any = any || s.inflight;
@@ -434,7 +438,9 @@ class Server {
         }
         cv_done_.notify_all();
       }
-      if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(10));
+      // batches in flight: poll their done flags without sleeping (a sleep's
+      // timer slack, tens of microseconds, would add to every request)
+      if (!progress) std::this_thread::yield();
     }
   }
 
@@ -450,7 +456,7 @@ class Server {
   uint32_t filter_scan_mode_ = 0;
   uint64_t budget_ = 0, inflight_bytes_ = 0;
   std::mutex mu_;
-  std::condition_variable cv_, cv_done_;
+  std::condition_variable cv_, cv_done_, cv_launched_;
   std::deque<ServerRequest*> pending_;
   std::unordered_map<uint64_t, std::unique_ptr<ServerRequest>> reqs_;
   std::vector<BatchSlot> slots_;
