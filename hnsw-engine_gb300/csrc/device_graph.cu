@@ -45,6 +45,8 @@ cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, 
                           const uint8_t* skip);
 cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bits, const uint64_t* labels, uint32_t n,
                                     uint32_t* out, cudaStream_t st);
+cudaError_t launch_relayout_l0(const uint32_t* raw, uint64_t n, uint32_t M0, uint32_t* l0, uint32_t l0s, uint32_t* dup,
+                               cudaStream_t st);
 }  // namespace hg
 
 namespace {
@@ -290,51 +292,61 @@ std::string graph_key_of(const hgd_search_args* a, bool any_deleted, uint64_t tu
 
 int enqueue_batch(hgd_graph* g, const hgd_search_args* a, Workspace* w, cudaStream_t st);
 
-}  // namespace
-
-extern "C" {
-
-const char* hgd_last_error(void) { return g_err.c_str(); }
-
-int hgd_graph_upload(const hgd_graph_view* v, int device, int order, hgd_graph** out) {
-  if (!v || !out) return fail(HGD_EINVAL, "hgd_graph_upload: null argument");
+int check_view(const hgd_graph_view* v, int order, const char* who) {
+  const std::string w(who);
   if (order != HGD_ORDER_AVX512 && order != HGD_ORDER_NEON)
-    return fail(HGD_EINVAL, "hgd_graph_upload: the GPU implements the AVX-512 and NEON summation orders only");
-  if (v->count >= 0xFFFFFFFFull) return fail(HGD_EINVAL, "hgd_graph_upload: count exceeds 32-bit ids");
+    return fail(HGD_EINVAL, w + ": the GPU implements the AVX-512 and NEON summation orders only");
+  if (v->count >= 0xFFFFFFFFull) return fail(HGD_EINVAL, w + ": count exceeds 32-bit ids");
   if (v->padded_dim % 16 != 0 || v->padded_dim < v->dim || v->dim == 0)
-    return fail(HGD_EINVAL, "hgd_graph_upload: padded_dim must be dim rounded up to 16");
+    return fail(HGD_EINVAL, w + ": padded_dim must be dim rounded up to 16");
   if (hg::slots_for(static_cast<uint32_t>(v->padded_dim)) > 33)
-    return fail(HGD_EINVAL, "hgd_graph_upload: padded dimension above 1024 is not supported on the GPU");
-  if (v->M < 2 || v->M > 2048) return fail(HGD_EINVAL, "hgd_graph_upload: invalid M");
+    return fail(HGD_EINVAL, w + ": padded dimension above 1024 is not supported on the GPU");
+  if (v->M < 2 || v->M > 2048) return fail(HGD_EINVAL, w + ": invalid M");
+  return HGD_OK;
+}
+
+// A graph with its sizes, device and stream set, no arrays yet.
+int graph_begin(const hgd_graph_view* v, int device, int order, hgd_graph** out) {
   auto* g = new hgd_graph();
   g->device = device;
   g->order = order;
-  auto cleanup = [&](int code) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
     hgd_graph_free(g);
-    return code;
-  };
-  {
-    cudaError_t e = cudaSetDevice(device);
-    if (e != cudaSuccess) return cleanup(fail(HGD_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
-    e = cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, device);
-    if (e != cudaSuccess) return cleanup(fail(HGD_ECUDA, cudaGetErrorString(e)));
-    e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return cleanup(fail(HGD_ECUDA, cudaGetErrorString(e)));
+    return fail(HGD_ECUDA, std::string("graph setup: ") + cudaGetErrorString(e));
   }
-  const uint64_t n = v->count;
-  g->n = n;
+  g->n = v->count;
   g->dim = v->dim;
   g->pd = v->padded_dim;
   g->M = v->M;
   g->metric = v->metric;
   g->max_level = v->max_level;
   g->entry = v->entry_point;
-  const uint32_t M0 = static_cast<uint32_t>(2 * v->M);
-  g->l0s = round_up(M0, 16);
+  g->l0s = round_up(static_cast<uint32_t>(2 * v->M), 16);
   g->ups = round_up(static_cast<uint32_t>(v->M), 16);
+  *out = g;
+  return HGD_OK;
+}
 
-  // host re-layout
-  std::vector<uint32_t> l0(static_cast<size_t>(n) * g->l0s, hg::kNoId);
+int up_copy(DBuf& d, const void* src, size_t bytes) {
+  cudaError_t e = d.ensure(std::max<size_t>(bytes, 16));
+  if (e != cudaSuccess) return fail(HGD_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  if (bytes) {
+    e = cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+  }
+  return HGD_OK;
+}
+
+// The small parts, built on the host from the view and uploaded: the upper
+// layers in blocks of ups ids per (node, level) with each node's first
+// block, the alive bits, whether labels are the ids, and whether a list
+// holds an id twice (layer 0 too when check_l0).
+int graph_small_parts(hgd_graph* g, const hgd_graph_view* v, bool check_l0) {
+  const uint64_t n = v->count;
+  const uint32_t M0 = static_cast<uint32_t>(2 * v->M);
   std::vector<uint32_t> mark(n, hg::kNoId);
   uint64_t list_no = 0;
   auto dup_check = [&](const uint32_t* ids, uint32_t cnt) {
@@ -344,12 +356,11 @@ int hgd_graph_upload(const hgd_graph_view* v, int device, int order, hgd_graph**
     }
     ++list_no;
   };
-  for (uint64_t i = 0; i < n; ++i) {
-    const uint32_t* src = v->level0 + i * (1 + M0);
-    const uint32_t cnt = std::min(src[0], M0);
-    std::memcpy(&l0[i * g->l0s], src + 1, cnt * 4);
-    dup_check(src + 1, cnt);
-  }
+  if (check_l0)
+    for (uint64_t i = 0; i < n; ++i) {
+      const uint32_t* src = v->level0 + i * (1 + M0);
+      dup_check(src + 1, std::min(src[0], M0));
+    }
   std::vector<uint32_t> up_blk(n, hg::kNoId);
   uint64_t blocks = 0;
   for (uint64_t i = 0; i < n; ++i) blocks += v->levels[i];
@@ -366,31 +377,191 @@ int hgd_graph_upload(const hgd_graph_view* v, int device, int order, hgd_graph**
       dup_check(src + 1, cnt);
     }
   }
+  g->identity_labels = true;
   for (uint64_t i = 0; i < n && g->identity_labels; ++i) g->identity_labels = v->labels[i] == i;
   g->alive_host.assign((n + 31) / 32 + 1, 0u);
+  g->num_deleted = 0;
   for (uint64_t i = 0; i < n; ++i) {
     if (v->deleted[i] == 0) g->alive_host[i >> 5] |= 1u << (i & 31);
     else ++g->num_deleted;
   }
-
-  auto up_copy = [&](DBuf& d, const void* src, size_t bytes) -> int {
-    cudaError_t e = d.ensure(std::max<size_t>(bytes, 16));
-    if (e != cudaSuccess) return fail(HGD_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    if (bytes) {
-      e = cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
-      if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
-    }
-    return HGD_OK;
-  };
   int rc;
+  if ((rc = up_copy(g->up, up.data(), up.size() * 4)) != HGD_OK) return rc;
+  if ((rc = up_copy(g->up_blk, up_blk.data(), up_blk.size() * 4)) != HGD_OK) return rc;
+  return up_copy(g->alive, g->alive_host.data(), g->alive_host.size() * 4);
+}
+
+}  // namespace
+
+// Streamed upload state: the graph under construction, a ring of pinned
+// staging buffers with the event of each one's last copy, and layer 0 in the
+// file's layout until it is re-laid on the device.
+constexpr int kStreamBuffers = 4;
+struct hgd_stream {
+  hgd_graph* g = nullptr;
+  uint32_t M0 = 0;
+  uint64_t chunk = 0;
+  uint64_t sec_bytes[3] = {0, 0, 0};
+  uint64_t submitted[3] = {0, 0, 0};
+  std::vector<PinnedBuf> ring;
+  std::vector<cudaEvent_t> ev;
+  int cur = kStreamBuffers - 1;
+  bool handed = false;
+  DBuf raw_l0, flag;
+};
+
+extern "C" {
+
+const char* hgd_last_error(void) { return g_err.c_str(); }
+
+int hgd_graph_upload(const hgd_graph_view* v, int device, int order, hgd_graph** out) {
+  if (!v || !out) return fail(HGD_EINVAL, "hgd_graph_upload: null argument");
+  int rc = check_view(v, order, "hgd_graph_upload");
+  if (rc != HGD_OK) return rc;
+  hgd_graph* g = nullptr;
+  if ((rc = graph_begin(v, device, order, &g)) != HGD_OK) return rc;
+  auto cleanup = [&](int code) {
+    hgd_graph_free(g);
+    return code;
+  };
+  const uint64_t n = v->count;
+  const uint32_t M0 = static_cast<uint32_t>(2 * v->M);
+  // host re-layout of layer 0
+  std::vector<uint32_t> l0(static_cast<size_t>(n) * g->l0s, hg::kNoId);
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint32_t* src = v->level0 + i * (1 + M0);
+    const uint32_t cnt = std::min(src[0], M0);
+    std::memcpy(&l0[i * g->l0s], src + 1, cnt * 4);
+  }
+  if ((rc = graph_small_parts(g, v, true)) != HGD_OK) return cleanup(rc);
   if ((rc = up_copy(g->vecs, v->vectors, n * g->pd * 4)) != HGD_OK) return cleanup(rc);
   if ((rc = up_copy(g->l0, l0.data(), l0.size() * 4)) != HGD_OK) return cleanup(rc);
-  if ((rc = up_copy(g->up, up.data(), up.size() * 4)) != HGD_OK) return cleanup(rc);
-  if ((rc = up_copy(g->up_blk, up_blk.data(), up_blk.size() * 4)) != HGD_OK) return cleanup(rc);
   if ((rc = up_copy(g->labels, v->labels, n * 8)) != HGD_OK) return cleanup(rc);
-  if ((rc = up_copy(g->alive, g->alive_host.data(), g->alive_host.size() * 4)) != HGD_OK) return cleanup(rc);
   *out = g;
   return HGD_OK;
+}
+
+// ---- streamed upload -------------------------------------------------------
+int hgd_stream_begin(const hgd_graph_view* v, int device, int order, uint64_t chunk_bytes, hgd_stream** out) {
+  if (!v || !out) return fail(HGD_EINVAL, "hgd_stream_begin: null argument");
+  int rc = check_view(v, order, "hgd_stream_begin");
+  if (rc != HGD_OK) return rc;
+  if (v->count > 0xFFFFFFFFull - 64) return fail(HGD_EINVAL, "hgd_stream_begin: count exceeds 32-bit ids");
+  if (chunk_bytes < 4096 || chunk_bytes % 16 != 0)
+    return fail(HGD_EINVAL, "hgd_stream_begin: chunk_bytes must be a multiple of 16, at least 4096");
+  auto* s = new hgd_stream();
+  if ((rc = graph_begin(v, device, order, &s->g)) != HGD_OK) {
+    delete s;
+    return rc;
+  }
+  auto cleanup = [&](int code) {
+    hgd_stream_abort(s);
+    return code;
+  };
+  const uint64_t n = v->count;
+  s->M0 = static_cast<uint32_t>(2 * v->M);
+  s->sec_bytes[0] = n * s->g->pd * 4;
+  s->sec_bytes[1] = n * (1 + static_cast<uint64_t>(s->M0)) * 4;
+  s->sec_bytes[2] = n * 8;
+  DBuf* dst[3] = {&s->g->vecs, &s->raw_l0, &s->g->labels};
+  for (int i = 0; i < 3; ++i) {
+    const cudaError_t e = dst[i]->ensure(std::max<uint64_t>(s->sec_bytes[i], 16));
+    if (e != cudaSuccess) return cleanup(fail(HGD_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e)));
+  }
+  s->ring.resize(kStreamBuffers);
+  s->ev.assign(kStreamBuffers, nullptr);
+  for (int i = 0; i < kStreamBuffers; ++i) {
+    cudaError_t e = s->ring[i].ensure(chunk_bytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) return cleanup(fail(HGD_ENOMEM, std::string("pinned staging: ") + cudaGetErrorString(e)));
+  }
+  s->chunk = chunk_bytes;
+  *out = s;
+  return HGD_OK;
+}
+
+int hgd_stream_buffer(hgd_stream* s, void** buf, uint64_t* cap) {
+  if (!s || !buf || !cap) return fail(HGD_EINVAL, "hgd_stream_buffer: null argument");
+  const int next = (s->cur + 1) % kStreamBuffers;
+  const cudaError_t e = cudaEventSynchronize(s->ev[next]);  // its previous copy (none yet: returns at once)
+  if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("hgd_stream_buffer: ") + cudaGetErrorString(e));
+  s->cur = next;
+  s->handed = true;
+  *buf = s->ring[next].p;
+  *cap = s->chunk;
+  return HGD_OK;
+}
+
+int hgd_stream_submit(hgd_stream* s, int section, uint64_t offset, uint64_t bytes) {
+  if (!s) return fail(HGD_EINVAL, "hgd_stream_submit: null stream");
+  if (!s->handed) return fail(HGD_EINVAL, "hgd_stream_submit: no buffer taken");
+  if (section < 0 || section > 2) return fail(HGD_EINVAL, "hgd_stream_submit: section must be 0, 1 or 2");
+  if (bytes > s->chunk || offset > s->sec_bytes[section] || bytes > s->sec_bytes[section] - offset)
+    return fail(HGD_EINVAL, "hgd_stream_submit: chunk outside the section");
+  s->handed = false;
+  if (bytes == 0) return HGD_OK;
+  void* dst = section == 0 ? s->g->vecs.p : (section == 1 ? s->raw_l0.p : s->g->labels.p);
+  cudaError_t e = cudaMemcpyAsync(static_cast<char*>(dst) + offset, s->ring[s->cur].p, bytes, cudaMemcpyHostToDevice,
+                                  s->g->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(s->ev[s->cur], s->g->stream);
+  if (e != cudaSuccess) return fail(HGD_ECUDA, std::string("hgd_stream_submit: ") + cudaGetErrorString(e));
+  s->submitted[section] += bytes;
+  return HGD_OK;
+}
+
+int hgd_stream_finish(hgd_stream* s, const hgd_graph_view* v, hgd_graph** out) {
+  if (!s || !v || !out) return fail(HGD_EINVAL, "hgd_stream_finish: null argument");
+  auto cleanup = [&](int code) {
+    hgd_stream_abort(s);
+    return code;
+  };
+  hgd_graph* g = s->g;
+  if (v->count != g->n || v->padded_dim != g->pd || v->M != g->M)
+    return cleanup(fail(HGD_EINVAL, "hgd_stream_finish: the view does not match hgd_stream_begin's"));
+  for (int i = 0; i < 3; ++i)
+    if (s->submitted[i] != s->sec_bytes[i])
+      return cleanup(fail(HGD_EINVAL, "hgd_stream_finish: a section was not streamed in full"));
+  const uint64_t n = g->n;
+  cudaError_t e = g->l0.ensure(std::max<uint64_t>(n * g->l0s * 4, 16));
+  if (e != cudaSuccess) return cleanup(fail(HGD_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e)));
+  // layer 0 into the padded stride on the device; duplicate ids in a list
+  // (M0 <= 32: one warp compare per list) raise the flag
+  const bool dev_dups = s->M0 <= 32;
+  int rc = graph_small_parts(g, v, !dev_dups);
+  if (rc != HGD_OK) return cleanup(rc);
+  if ((e = s->flag.ensure(16)) != cudaSuccess) return cleanup(fail(HGD_ENOMEM, cudaGetErrorString(e)));
+  if ((e = cudaMemsetAsync(s->flag.p, 0, 16, g->stream)) != cudaSuccess)
+    return cleanup(fail(HGD_ECUDA, cudaGetErrorString(e)));
+  if (n > 0) {
+    if ((e = hg::launch_relayout_l0(s->raw_l0.as<uint32_t>(), n, s->M0, g->l0.as<uint32_t>(), g->l0s,
+                                    dev_dups ? s->flag.as<uint32_t>() : nullptr, g->stream)) != cudaSuccess)
+      return cleanup(fail(HGD_ECUDA, std::string("layer-0 re-layout: ") + cudaGetErrorString(e)));
+  }
+  uint32_t dup = 0;
+  if ((e = cudaMemcpyAsync(&dup, s->flag.p, 4, cudaMemcpyDeviceToHost, g->stream)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(g->stream)) != cudaSuccess)
+    return cleanup(fail(HGD_ECUDA, std::string("hgd_stream_finish: ") + cudaGetErrorString(e)));
+  if (dup) g->dedup = true;
+  s->g = nullptr;
+  hgd_stream_abort(s);  // frees the staging, not the graph
+  *out = g;
+  return HGD_OK;
+}
+
+void hgd_stream_abort(hgd_stream* s) {
+  if (!s) return;
+  if (s->g) {
+    hgd_graph_free(s->g);  // synchronises the stream first
+  } else {
+    for (cudaEvent_t e : s->ev)
+      if (e) cudaEventSynchronize(e);
+  }
+  for (cudaEvent_t e : s->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& b : s->ring) b.release();
+  s->raw_l0.release();
+  s->flag.release();
+  delete s;
 }
 
 int hgd_graph_set_order(hgd_graph* g, int order) {

@@ -119,6 +119,13 @@ int hg_index_load(const char* path, int mmap, hg_index** out) {
   });
 }
 
+int hg_index_load_device(const char* path, int mmap, int device, hg_index** out) {
+  return guarded([&] {
+    if (!path || !out) throw std::invalid_argument("hg_index_load_device: null argument");
+    *out = new hg_index{hnsw::Index::load_to_device(path, device, mmap != 0)};
+  });
+}
+
 int hg_index_save(const hg_index* idx, const char* path) {
   return guarded([&] {
     if (!idx || !path) throw std::invalid_argument("hg_index_save: null argument");

@@ -151,6 +151,8 @@ struct Index::Impl {
 
   // device mirror (index.cpp)
   hgd_graph* device_graph() const;
+  hgd_graph_view device_view() const;  // the host arrays, as the device upload reads them
+  int device_order() const;            // HGD_ORDER_* of the distance kernel in use
 };
 
 }  // namespace hnsw

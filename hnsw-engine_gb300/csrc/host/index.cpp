@@ -43,13 +43,7 @@ int order_of(simd::Isa isa) {
 
 }  // namespace
 
-hgd_graph* Index::Impl::device_graph() const {
-  std::lock_guard<std::mutex> g(dev_mutex);
-  if (dev && !dev_stale) return dev;
-  if (dev) {
-    hgd_graph_free(dev);
-    dev = nullptr;
-  }
+hgd_graph_view Index::Impl::device_view() const {
   hgd_graph_view v{};
   v.count = count;
   v.dim = dim;
@@ -66,6 +60,19 @@ hgd_graph* Index::Impl::device_graph() const {
   v.labels = labels;
   v.levels = levels;
   v.deleted = deleted.data();
+  return v;
+}
+
+int Index::Impl::device_order() const { return order_of(isa); }
+
+hgd_graph* Index::Impl::device_graph() const {
+  std::lock_guard<std::mutex> g(dev_mutex);
+  if (dev && !dev_stale) return dev;
+  if (dev) {
+    hgd_graph_free(dev);
+    dev = nullptr;
+  }
+  const hgd_graph_view v = device_view();
   hgd_graph* out = nullptr;
   const int rc = hgd_graph_upload(&v, device, order_of(isa), &out);
   if (rc != HGD_OK) rethrow(rc, "upload to GPU");

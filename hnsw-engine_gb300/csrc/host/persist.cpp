@@ -110,7 +110,12 @@ uint64_t header_sum(const unsigned char* hdr) noexcept {
 /// FORMAT v1 payload hash (FORMAT.md "Payload checksum").
 class SectionHash {
  public:
-  void feed(const void* data, std::size_t n) noexcept {
+  // one whole section
+  void feed(const void* data, std::size_t n) noexcept { feed_part(data, n, true, n); }
+  // a section in consecutive parts: every part but the last a multiple of 8
+  // bytes long; `last` closes the section of `total` bytes (the same value
+  // as one feed of the whole section)
+  void feed_part(const void* data, std::size_t n, bool last, std::size_t total) noexcept {
     const auto* p = static_cast<const unsigned char*>(data);
     std::size_t i = 0;
     for (; i + 8 <= n; i += 8) {
@@ -118,8 +123,9 @@ class SectionHash {
       std::memcpy(&w, p + i, 8);
       step(w);
     }
+    if (!last) return;
     for (; i < n; ++i) step(0x100ULL | p[i]);
-    step(n);
+    step(total);
   }
   uint64_t value() const noexcept { return h_; }
 
@@ -226,6 +232,35 @@ Params params_of(const Fields& f) {
   return p;
 }
 
+/// The state of a read-only index whose arrays stay in the file mapping b.
+void bind_mapped(Index::Impl& im, const Fields& f, const unsigned char* b) {
+  im.params.max_elements = f.max_elements;
+  im.count = im.capacity = f.count;
+  im.ef_search = f.ef_search;
+  im.upper_used = f.upper_used;
+  im.entry_point = f.entry;
+  im.max_level = f.max_level;
+  im.rng_state = f.rng;
+  im.vecs = reinterpret_cast<const float*>(b + f.off[0]);
+  im.l0 = const_cast<uint32_t*>(reinterpret_cast<const uint32_t*>(b + f.off[1]));
+  im.labels = reinterpret_cast<const uint64_t*>(b + f.off[2]);
+  im.levels = b + f.off[3];
+  im.upper = const_cast<uint32_t*>(reinterpret_cast<const uint32_t*>(b + f.off[5]));
+}
+
+/// pread until `n` bytes are in or the file ends; false on a short read.
+bool pread_full(int fd, void* dst, uint64_t n, uint64_t at) {
+  auto* p = static_cast<unsigned char*>(dst);
+  while (n > 0) {
+    const ssize_t r = ::pread(fd, p, static_cast<std::size_t>(std::min<uint64_t>(n, 1ull << 30)), static_cast<off_t>(at));
+    if (r <= 0) return false;
+    p += r;
+    at += static_cast<uint64_t>(r);
+    n -= static_cast<uint64_t>(r);
+  }
+  return true;
+}
+
 /// Graph checks and derived state (reference persist.cpp:321-365).
 void check_graph(Index::Impl& im, const Fields& f, const uint8_t* tomb, const std::string& path) {
   const std::size_t n = f.count;
@@ -330,18 +365,7 @@ Index Index::load(const std::string& path, bool mmap) {
     const unsigned char* b = file.data();
     const Fields f = parse_header(b, file.size(), path);
     auto im = std::make_unique<Impl>(params_of(f));
-    im->params.max_elements = f.max_elements;
-    im->count = im->capacity = f.count;
-    im->ef_search = f.ef_search;
-    im->upper_used = f.upper_used;
-    im->entry_point = f.entry;
-    im->max_level = f.max_level;
-    im->rng_state = f.rng;
-    im->vecs = reinterpret_cast<const float*>(b + f.off[0]);
-    im->l0 = const_cast<uint32_t*>(reinterpret_cast<const uint32_t*>(b + f.off[1]));
-    im->labels = reinterpret_cast<const uint64_t*>(b + f.off[2]);
-    im->levels = b + f.off[3];
-    im->upper = const_cast<uint32_t*>(reinterpret_cast<const uint32_t*>(b + f.off[5]));
+    bind_mapped(*im, f, b);
     const Sizes s = section_bytes(f.count, f.padded_dim, f.M, f.upper_used);
     SectionHash hash;
     uint64_t pos = kHeaderBytes;
@@ -397,6 +421,133 @@ Index Index::load(const std::string& path, bool mmap) {
   im->rng_state = f.rng;
   check_graph(*im, f, tomb.data(), path);
   im->deleted.resize(im->capacity, 0);
+  return Index(std::move(im));
+}
+
+Index Index::load_to_device(const std::string& path, int device, bool mmap) {
+  // The checks and their order are load()'s; the reads go through the
+  // stream's pinned buffers for sections 0-2 (hashed there, copied to the
+  // host arrays unless mapped, and sent to the device), directly for the
+  // small sections 3-5.
+  gb::Mapping file;
+  const unsigned char* base = nullptr;
+  int fd = -1;
+  struct FdGuard {
+    int& fd;
+    ~FdGuard() {
+      if (fd >= 0) ::close(fd);
+    }
+  } fd_guard{fd};
+  uint64_t actual = 0;
+  unsigned char hdr[kHeaderBytes];
+  if (mmap) {
+    file = gb::Mapping(path);
+    base = file.data();
+    actual = file.size();
+  } else {
+    fd = ::open(path.c_str(), O_RDONLY);
+    if (fd < 0) throw std::runtime_error("cannot open " + path);
+    struct stat st {};
+    if (::fstat(fd, &st) != 0) throw std::runtime_error("cannot stat " + path);
+    actual = static_cast<uint64_t>(st.st_size);
+    if (actual < kHeaderBytes) corrupt(path, "file too small for header");
+    if (!pread_full(fd, hdr, kHeaderBytes, 0)) corrupt(path, "short read");
+  }
+  const Fields f = parse_header(mmap ? base : hdr, static_cast<std::size_t>(actual), path);
+  auto im = std::make_unique<Impl>(params_of(f));
+  im->params.max_elements = f.max_elements;
+  const Sizes s = section_bytes(f.count, f.padded_dim, f.M, f.upper_used);
+  std::vector<uint8_t> tomb;
+  void* dst[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  if (!mmap) {
+    if (f.count > 0) im->grow(std::max<std::size_t>(f.count, f.max_elements));
+    tomb.resize(f.count);
+    im->upper_store.assign(f.upper_used, 0u);
+    void* d[6] = {im->vec_store.data(), im->l0_store.data(), im->label_store.data(), im->level_store.data(),
+                  tomb.data(), im->upper_store.data()};
+    std::copy(d, d + 6, dst);
+  }
+  hgd_graph_view sizes{};
+  sizes.count = f.count;
+  sizes.dim = f.dim;
+  sizes.padded_dim = f.padded_dim;
+  sizes.M = f.M;
+  sizes.metric = static_cast<int32_t>(im->params.metric);
+  sizes.max_level = f.max_level;
+  sizes.entry_point = f.entry;
+  constexpr uint64_t kChunk = 32ull << 20;
+  hgd_stream* stream = nullptr;
+  if (hgd_stream_begin(&sizes, device, im->device_order(), kChunk, &stream) != HGD_OK)
+    throw std::runtime_error(std::string("load_to_device: ") + hgd_last_error());
+  struct StreamGuard {
+    hgd_stream*& s;
+    ~StreamGuard() { hgd_stream_abort(s); }
+  } stream_guard{stream};
+  SectionHash hash;
+  uint64_t pos = kHeaderBytes;
+  for (int i = 0; i < 6; ++i) {
+    unsigned char pad[kSectionAlign];
+    const uint64_t gap = f.off[i] - pos;
+    if (gap > sizeof pad) corrupt(path, "short read");
+    if (mmap) {
+      std::memcpy(pad, base + pos, gap);
+    } else if (gap && !pread_full(fd, pad, gap, pos)) {
+      corrupt(path, "short read");
+    }
+    for (uint64_t p = 0; p < gap; ++p)
+      if (pad[p] != 0) corrupt(path, "non-zero padding");
+    for (uint64_t o = 0; o < s.bytes[i]; o += kChunk) {
+      const uint64_t len = std::min<uint64_t>(kChunk, s.bytes[i] - o);
+      const uint64_t at = f.off[i] + o;
+      if (i <= 2) {
+        void* buf = nullptr;
+        uint64_t cap = 0;
+        if (hgd_stream_buffer(stream, &buf, &cap) != HGD_OK)
+          throw std::runtime_error(std::string("load_to_device: ") + hgd_last_error());
+        if (mmap) std::memcpy(buf, base + at, len);
+        else if (!pread_full(fd, buf, len, at)) corrupt(path, "short read");
+        hash.feed_part(buf, len, o + len == s.bytes[i], s.bytes[i]);
+        if (!mmap) std::memcpy(static_cast<unsigned char*>(dst[i]) + o, buf, len);
+        if (hgd_stream_submit(stream, i, o, len) != HGD_OK)
+          throw std::runtime_error(std::string("load_to_device: ") + hgd_last_error());
+      } else if (mmap) {
+        hash.feed_part(base + at, len, o + len == s.bytes[i], s.bytes[i]);
+      } else {
+        unsigned char* d = static_cast<unsigned char*>(dst[i]) + o;
+        if (!pread_full(fd, d, len, at)) corrupt(path, "short read");
+        hash.feed_part(d, len, o + len == s.bytes[i], s.bytes[i]);
+      }
+    }
+    if (s.bytes[i] == 0) hash.feed(nullptr, 0);  // an empty section still closes
+    pos = f.off[i] + s.bytes[i];
+  }
+  if (hash.value() != f.payload) corrupt(path, "payload checksum mismatch");
+  if (mmap) {
+    bind_mapped(*im, f, base);
+    check_graph(*im, f, base + f.off[4], path);
+    im->mapping = std::move(file);
+    im->read_only = true;
+  } else {
+    im->bind_pointers();
+    im->count = f.count;
+    im->ef_search = f.ef_search;
+    im->upper_used = f.upper_used;
+    im->entry_point = f.entry;
+    im->max_level = f.max_level;
+    im->rng_state = f.rng;
+    check_graph(*im, f, tomb.data(), path);
+    im->deleted.resize(im->capacity, 0);
+  }
+  const hgd_graph_view v = im->device_view();
+  hgd_graph* g = nullptr;
+  hgd_stream* st = stream;
+  stream = nullptr;  // finish consumes it, also on failure
+  if (hgd_stream_finish(st, &v, &g) != HGD_OK)
+    throw std::runtime_error(std::string("load_to_device: ") + hgd_last_error());
+  im->device = device;
+  hgd_graph_set_launch_mode(g, im->launch_mode);
+  im->dev = g;
+  im->dev_stale = false;
   return Index(std::move(im));
 }
 

@@ -34,6 +34,37 @@ __global__ void inv_norm_kernel(const float* __restrict__ qs, uint32_t nq, uint3
   out[q] = norm > 0.0 ? __double2float_rn(1.0 / sqrt(norm)) : 1.0f;
 }
 
+// Layer 0 from the file's layout (per node: count, then M0 ids) into rows of
+// l0s ids padded with kNoId; the count is clamped to M0 (the host validates
+// it before the graph is used).  Grid-stride over all (node, slot) pairs.
+__global__ void relayout_l0_kernel(const uint32_t* __restrict__ raw, uint64_t n, uint32_t M0, uint32_t* __restrict__ l0,
+                                   uint32_t l0s) {
+  const uint64_t total = n * l0s;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t node = i / l0s;
+    const uint32_t j = static_cast<uint32_t>(i - node * l0s);
+    const uint32_t* src = raw + node * (1ull + M0);
+    const uint32_t cnt = min(__ldg(src), M0);
+    l0[i] = j < cnt ? __ldg(src + 1 + j) : hg::kNoId;
+  }
+}
+
+// Whether some layer-0 list (M0 <= 32) holds an id twice: one warp per list,
+// one id per lane, __match_any_sync over the lanes (idle lanes hold values
+// no id takes: ids are below 2^32 - 64).
+__global__ void l0_dup_kernel(const uint32_t* __restrict__ raw, uint64_t n, uint32_t M0, uint32_t* __restrict__ flag) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
+  for (uint64_t node = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5; node < n; node += warps) {
+    const uint32_t* src = raw + node * (1ull + M0);
+    const uint32_t cnt = min(__ldg(src), M0);
+    const uint32_t id = static_cast<uint32_t>(lane) < cnt ? __ldg(src + 1 + lane) : 0xFFFFFFFFu - lane;
+    const uint32_t same = __match_any_sync(0xFFFFFFFFu, id);
+    if (__any_sync(0xFFFFFFFFu, __popc(same) > 1) && lane == 0) atomicOr(flag, 1u);
+  }
+}
+
 // Label-space BitsetFilter words -> id-space bits: bit id set iff
 // labels[id] < num_bits and that label's bit is set (filter.hpp:39-41).
 __global__ void translate_filter_kernel(const uint64_t* __restrict__ words, uint64_t num_bits,
@@ -94,6 +125,19 @@ cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bi
                                     uint32_t* out, cudaStream_t st) {
   const uint32_t out_words = (n + 31) / 32 + 1;
   translate_filter_kernel<<<(out_words + 255) / 256, 256, 0, st>>>(label_words, num_bits, labels, n, out, out_words);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_relayout_l0(const uint32_t* raw, uint64_t n, uint32_t M0, uint32_t* l0, uint32_t l0s, uint32_t* dup,
+                               cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const uint64_t total = n * l0s;
+  const unsigned blocks = static_cast<unsigned>(std::min<uint64_t>((total + 255) / 256, 152ull * 64));
+  relayout_l0_kernel<<<blocks, 256, 0, st>>>(raw, n, M0, l0, l0s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !dup) return e;
+  const unsigned wblocks = static_cast<unsigned>(std::min<uint64_t>((n + 7) / 8, 152ull * 64));
+  l0_dup_kernel<<<wblocks, 256, 0, st>>>(raw, n, M0, dup);
   return cudaGetLastError();
 }
 

@@ -78,6 +78,7 @@ def lib():
         L.hg_last_error.restype = C.c_char_p
         L.hg_index_create.argtypes = [sz, i32, sz, sz, sz, u64, C.POINTER(vp)]
         L.hg_index_load.argtypes = [C.c_char_p, i32, C.POINTER(vp)]
+        L.hg_index_load_device.argtypes = [C.c_char_p, i32, i32, C.POINTER(vp)]
         L.hg_index_save.argtypes = [vp, C.c_char_p]
         L.hg_index_free.argtypes = [vp]
         L.hg_index_add_batch.argtypes = [vp, vp, vp, sz, sz]
@@ -298,9 +299,15 @@ class Index:
             self._h = None
 
     @staticmethod
-    def load(path, mmap: bool = False) -> "Index":
+    def load(path, mmap: bool = False, device=None) -> "Index":
+        """Index::load.  device=N also builds the graph on CUDA device N in the
+        same pass (the file's sections streamed through pinned staging
+        buffers while they are read and hashed)."""
         h = C.c_void_p()
-        _check(lib().hg_index_load(str(path).encode(), 1 if mmap else 0, C.byref(h)))
+        if device is None:
+            _check(lib().hg_index_load(str(path).encode(), 1 if mmap else 0, C.byref(h)))
+        else:
+            _check(lib().hg_index_load_device(str(path).encode(), 1 if mmap else 0, int(device), C.byref(h)))
         return Index(_handle=h)
 
     def save(self, path):

@@ -111,6 +111,12 @@ class Index {
 
   void save(const std::string& path) const;
   static Index load(const std::string& path, bool mmap = false);
+  /// load() with the device graph built in the same pass (no counterpart in
+  /// the reference): the vectors, layer 0 and labels are streamed to `device`
+  /// through pinned staging buffers while the file is read and hashed, and
+  /// layer 0 is laid out on the device.  Same validation and errors as
+  /// load(); mmap = true keeps the host arrays in the read-only mapping.
+  static Index load_to_device(const std::string& path, int device, bool mmap = false);
 
   /// CUDA device the graph is mirrored to (default 0); call before the first search.
   void set_device(int device);

@@ -11,6 +11,7 @@
  * Reference interface each entry point replaces (paths within hnsw-engine):
  *   hg_index_create        Index(const Params&)                 include/hnsw/index.hpp:39; src/index.cpp:48-67
  *   hg_index_load          Index::load(path, mmap)              include/hnsw/index.hpp:86; src/persist.cpp:476-541
+ *   hg_index_load_device   Index::load with the device graph built while the file is read (no counterpart)
  *   hg_index_save          Index::save                          include/hnsw/index.hpp:83; src/persist.cpp:421-474
  *   hg_index_free          ~Index                               include/hnsw/index.hpp:40
  *   hg_index_add_batch     Index::add_batch                     include/hnsw/index.hpp:50; src/index.cpp:273-306
@@ -111,6 +112,10 @@ const char* hg_last_error(void);
 int hg_index_create(size_t dim, int metric, size_t M, size_t ef_construction, size_t max_elements, uint64_t seed,
                     hg_index** out);
 int hg_index_load(const char* path, int mmap, hg_index** out);
+/* hg_index_load, and the graph mirrored to `device` in the same pass: the
+ * vectors, layer 0 and labels go to the device through pinned staging
+ * buffers as they are read and hashed.  Same validation and errors. */
+int hg_index_load_device(const char* path, int mmap, int device, hg_index** out);
 int hg_index_save(const hg_index* idx, const char* path);
 void hg_index_free(hg_index* idx);
 int hg_index_add_batch(hg_index* idx, const float* vecs, const uint64_t* labels, size_t n, size_t num_threads);

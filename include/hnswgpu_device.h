@@ -141,6 +141,26 @@ typedef struct {
 } hgd_search_args;
 
 int hgd_graph_upload(const hgd_graph_view* view, int device, int order, hgd_graph** out);
+
+/* Streamed upload: the device graph built from FORMAT v1 sections as a
+ * loader reads them, the host-to-device copies overlapped with the reads.
+ * hgd_stream_begin takes the sizes of the view (count, dim, padded_dim, M,
+ * metric, max_level, entry_point; its pointers are not read) and allocates
+ * the device arrays and a ring of pinned staging buffers of chunk_bytes.
+ * hgd_stream_buffer hands out the next staging buffer (after its previous
+ * copy has ended); the loader fills it and passes it back with
+ * hgd_stream_submit: section 0 (vectors), 1 (level0 in the file's layout) or
+ * 2 (labels), at a byte offset into that section.  A buffer must not be
+ * touched after its submit.  hgd_stream_finish takes the whole view (host
+ * pointers, once the loader has validated the file), lays layer 0 out on the
+ * device, builds the small parts and returns the graph; hgd_stream_abort
+ * drops everything.  Every section 0-2 byte must be submitted exactly once. */
+typedef struct hgd_stream hgd_stream;
+int hgd_stream_begin(const hgd_graph_view* sizes, int device, int order, uint64_t chunk_bytes, hgd_stream** out);
+int hgd_stream_buffer(hgd_stream* s, void** buf, uint64_t* cap);
+int hgd_stream_submit(hgd_stream* s, int section, uint64_t offset, uint64_t bytes);
+int hgd_stream_finish(hgd_stream* s, const hgd_graph_view* view, hgd_graph** out);
+void hgd_stream_abort(hgd_stream* s);
 int hgd_graph_set_deleted(hgd_graph* g, uint32_t id, int deleted);
 int hgd_graph_set_order(hgd_graph* g, int order);
 void hgd_graph_free(hgd_graph* g);
