@@ -78,6 +78,9 @@ struct MmaParams {
   const uint32_t* const* allow_tab;
   const int32_t* fsel;
   const uint32_t* alive;
+  // per query: the tightest bound any CTA has found so far (order-preserving
+  // key bits, 0xFFFFFFFF none), shared by all splits of the query
+  uint32_t* gkey;
   uint32_t n, nq, kchunks, cap, k, nbt, tiles_q, splits, tps;
   uint32_t trig;  // a lane's buffer is compacted once it could pass trig - 32 keys (<= cap)
   int l2;
@@ -387,6 +390,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool over = false;
       for (uint32_t bt = b0; bt < b1; ++bt, ++acc_i) {
         const uint32_t ab = acc_i & 1u, aph = (acc_i >> 1) & 1u;
+        // the bound of the other splits of this query (a split's k-th
+        // smallest + the margin bounds the k-th over all rows from above)
+        if (live_q && !over) {
+          const uint32_t gk = *reinterpret_cast<volatile const uint32_t*>(P.gkey + q);
+          if (gk != 0xFFFFFFFFu) thr = fminf(thr, dist_of_key_bits(gk));
+        }
         // one lane waits, the warp follows its answer (tcgen05.ld needs the whole warp)
         int got = 0;
         if (lane == 0) got = mbar_wait(tfull(ab), aph, &abort_flag, P.err) ? 1 : 0;
@@ -470,6 +479,8 @@ __global__ void __launch_bounds__(kThreads, 1)
               if (cnt + 32u > P.cap) {  // the margin keeps too many rows: give this query up
                 over = true;
                 thr = -__int_as_float(0x7f800000);
+              } else {
+                atomicMin(P.gkey + q, okey(lthr));  // publish this split's bound
               }
             }
           }
@@ -1260,6 +1271,8 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     if ((e = sc.pool.ensure(static_cast<size_t>(nq) * pool_cap * 4)) != cudaSuccess) break;
     if ((e = sc.pool_n.ensure(nq * 4ull)) != cudaSuccess) break;
     if ((e = sc.err.ensure(16)) != cudaSuccess) break;
+    if ((e = sc.gkey.ensure(nq * 4ull)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(sc.gkey.p, 0xFF, nq * 4ull, st)) != cudaSuccess) break;
     __half* q16 = sc.q16.as<__half>();
     float *qc = sc.qc.as<float>(), *qm = sc.qm.as<float>(), *qq = sc.qq.as<float>();
     uint64_t* buf = sc.buf.as<uint64_t>();
@@ -1286,6 +1299,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     P.buf = buf;
     P.cnt = cnt;
     P.err = derr;
+    P.gkey = sc.gkey.as<uint32_t>();
     P.n = r.n;
     P.nq = nq;
     P.kchunks = s->kp / BK;
@@ -1764,6 +1778,8 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     if ((e = sc->pool.ensure(static_cast<size_t>(n_r) * pool_cap * 4)) != cudaSuccess) break;
     if ((e = sc->pool_n.ensure(n_r * 4ull)) != cudaSuccess) break;
     if ((e = sc->err.ensure(16)) != cudaSuccess) break;
+    if ((e = sc->gkey.ensure(n_r * 4ull)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(sc->gkey.p, 0xFF, n_r * 4ull, st)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(sc->cnt.p, 0, static_cast<size_t>(splits) * n_r * 4, st)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(sc->err.p, 0, 16, st)) != cudaSuccess) break;
     what = "gather kernel";
@@ -1791,6 +1807,7 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     P.allow_tab = a.allow_tab;
     P.fsel = a.fsel;
     P.alive = a.alive;
+    P.gkey = sc->gkey.as<uint32_t>();
     P.n = r.n;
     P.nq = n_r;
     P.kchunks = s->kp / BK;
