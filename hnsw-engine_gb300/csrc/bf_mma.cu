@@ -52,7 +52,8 @@ constexpr int BK = 64;   // FP16 elements per K chunk: one 128-byte swizzle atom
 constexpr int kStages = 4;
 constexpr uint32_t kABytes = BM * BK * 2;
 constexpr uint32_t kBBytes = BN * BK * 2;
-constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-5 epilogue
+constexpr int kEpiWarps = 8;   // two per TMEM lane quarter, each over half of a tile's rows
+constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-9 epilogue
 constexpr uint32_t kTmemCols = 512;
 constexpr size_t kSmem = kStages * (kABytes + kBBytes) + 1024;
 constexpr uint32_t kOver = 0xFFFFFFFFu;
@@ -70,8 +71,8 @@ struct MmaParams {
   const uint32_t* allow;  // bits over rows or null
   const float* qc;        // nq_pad: s = xn + acc * qc
   const float* qm;        // nq_pad: selection margin 2E
-  uint64_t* buf;          // splits x nq x cap candidate keys
-  uint32_t* cnt;          // splits x nq: candidates kept, or kOver
+  uint64_t* buf;          // (2 x splits) x nq x cap candidate keys: one set per half tile
+  uint32_t* cnt;          // (2 x splits) x nq: candidates kept, or kOver
   uint32_t* err;          // [0] pipeline wait expired
   // per-query filters (routed graph queries): bits over rows of filter
   // fsel[q] (-1 none) instead of `allow`; tombstones over rows
@@ -193,6 +194,33 @@ __device__ __forceinline__ void sp_mma(float (&c)[4], uint32_t a0, uint32_t a1, 
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
+// Packed FP32 pairs (sm_100+): each lane is the scalar op's IEEE result.
+__device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
+  unsigned long long pa, pb, pc, pd;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pa) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pb) : "f"(b.x), "f"(b.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pc) : "f"(c.x), "f"(c.y));
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(pd) : "l"(pa), "l"(pb), "l"(pc));
+  float2 d;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(pd));
+  return d;
+}
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+  unsigned long long pa, pb, pd;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pa) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pb) : "f"(b.x), "f"(b.y));
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(pd) : "l"(pa), "l"(pb));
+  float2 d;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(pd));
+  return d;
+}
+// Three-input minimum; a NaN input is skipped, as fminf skips it.
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
 __device__ __forceinline__ float dist_of_key_bits(uint32_t kb) {
   const uint32_t u = (kb & 0x80000000u) ? (kb & 0x7FFFFFFFu) : ~kb;
   return __uint_as_float(u);
@@ -275,7 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(tfull(b), 1);
-      mbar_init(tempty(b), 4);
+      mbar_init(tempty(b), kEpiWarps);
     }
     mbar_init(mdone, 1);
     abort_flag = 0u;
@@ -369,8 +397,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // ---- epilogue: one query per thread (TMEM lane), 256 rows per tile ----
+    // ---- epilogue: one query per thread (TMEM lane); a warp scores half of a
+    // tile's 256 rows (chunks 4 * half .. 4 * half + 3), keeping its own
+    // candidate buffers (sub-split 2 * split + half) ----
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);
+    const uint32_t half = static_cast<uint32_t>(warp - 2) / 4u;
+    const uint32_t c_begin = half * (BN / 64), c_end = c_begin + BN / 64;
     const uint32_t row_in_tile = quarter * 32u + static_cast<uint32_t>(lane);
     uint32_t acc_i = 0;
     bool ok = true;
@@ -383,7 +415,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t* allow_q = P.fsel ? (fq >= 0 ? P.allow_tab[fq] : nullptr) : P.allow;
       const float cq = P.qc[q];
       const float margin = P.qm[q];
-      uint64_t* bufp = P.buf + (static_cast<size_t>(sp) * P.nq + (live_q ? q : 0)) * P.cap;
+      const uint32_t sub = 2u * sp + half;
+      uint64_t* bufp = P.buf + (static_cast<size_t>(sub) * P.nq + (live_q ? q : 0)) * P.cap;
       uint32_t cnt = 0;
       uint32_t lim = P.trig;  // compaction point: the threshold tightens early
       float thr = __int_as_float(0x7f800000);
@@ -405,24 +438,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tc_fence_after();
         const uint32_t taddr = tmem + ((quarter * 32u) << 16) + ab * BN;
-        // Software-pipelined over the tile's 8 chunks of 32 rows: the TMEM
-        // load and the global loads (row norms, filter and tombstone words)
-        // of chunk ch + 1 are in flight while chunk ch is scored.
+        // Software-pipelined over the warp's 4 chunks of 32 rows: the TMEM
+        // load and the filter and tombstone words of chunk ch + 1 are in
+        // flight while chunk ch is scored.
         uint32_t ra[32], rb[32];
-        float xa[32], xb[32];
         uint32_t va = 0, vb = 0;
-        auto fetch = [&](uint32_t ch, uint32_t (&r)[32], float (&xs)[32], uint32_t& valid) {
+        auto fetch = [&](uint32_t ch, uint32_t (&r)[32], uint32_t& valid) {
           tmem_ld32_async(taddr + ch * 32u, r);
-          const uint32_t j0 = bt * BN + ch * 32u;  // < n_pad: xn holds n_pad entries
-          const float4* x4 = reinterpret_cast<const float4*>(P.xn + j0);
-#pragma unroll
-          for (int v = 0; v < 8; ++v) {
-            const float4 t = __ldg(x4 + v);
-            xs[4 * v] = t.x;
-            xs[4 * v + 1] = t.y;
-            xs[4 * v + 2] = t.z;
-            xs[4 * v + 3] = t.w;
-          }
+          const uint32_t j0 = bt * BN + ch * 32u;
           valid = 0u;
           if (j0 < P.n && live_q && !over) {  // padding rows of the last tile stay masked
             valid = P.n - j0 >= 32u ? 0xFFFFFFFFu : ((1u << (P.n - j0)) - 1u);
@@ -430,28 +453,45 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (P.alive) valid &= __ldg(P.alive + (j0 >> 5));
           }
         };
-        auto score = [&](uint32_t ch, const uint32_t (&r)[32], const float (&xs)[32], uint32_t valid) {
+        auto score = [&](uint32_t ch, const uint32_t (&r)[32], uint32_t valid) {
+          // the chunk's row norms: the same 128 bytes for the whole warp, and
+          // for the CTA's other warps on these rows (L1)
+          float xs[32];
+          {
+            const float4* x4 = reinterpret_cast<const float4*>(P.xn + bt * BN + ch * 32u);  // < n_pad
+#pragma unroll
+            for (int v = 0; v < 8; ++v) {
+              const float4 t = __ldg(x4 + v);
+              xs[4 * v] = t.x;
+              xs[4 * v + 1] = t.y;
+              xs[4 * v + 2] = t.z;
+              xs[4 * v + 3] = t.w;
+            }
+          }
           const uint32_t j0 = bt * BN + ch * 32u;
           if (over) valid = 0u;  // set by a compaction of an earlier chunk
-          float sv[32];
+          float sv[32];  // two rows per packed FP32 instruction (each lane rounded as a scalar op)
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const float acc = __uint_as_float(r[c]);
-            sv[c] = P.l2 ? __fmaf_rn(acc, cq, xs[c]) : __fmul_rn(acc, cq);
+          for (int c = 0; c < 32; c += 2) {
+            const float2 v = P.l2 ? fma2_rn(make_float2(__uint_as_float(r[c]), __uint_as_float(r[c + 1])),
+                                            make_float2(cq, cq), make_float2(xs[c], xs[c + 1]))
+                                  : mul2_rn(make_float2(__uint_as_float(r[c]), __uint_as_float(r[c + 1])),
+                                            make_float2(cq, cq));
+            sv[c] = v.x;
+            sv[c + 1] = v.y;
           }
-          if (valid != 0xFFFFFFFFu) {  // masked rows become NaN: never <= thr, ignored by fminf
+          if (valid != 0xFFFFFFFFu) {  // masked rows become NaN: never <= thr, skipped by min
 #pragma unroll
             for (int c = 0; c < 32; ++c)
               if (!((valid >> c) & 1u)) sv[c] = __int_as_float(0x7fffffff);
           }
-          float g8[4];  // minima of the four 8-row groups, each a 3-level tree
+          float g8[4];  // minima of the four 8-row groups (three-input min)
 #pragma unroll
           for (int g = 0; g < 4; ++g) {
-            const float a0 = fminf(sv[8 * g], sv[8 * g + 4]), a1 = fminf(sv[8 * g + 1], sv[8 * g + 5]);
-            const float a2 = fminf(sv[8 * g + 2], sv[8 * g + 6]), a3 = fminf(sv[8 * g + 3], sv[8 * g + 7]);
-            g8[g] = fminf(fminf(a0, a2), fminf(a1, a3));
+            const float* v = sv + 8 * g;
+            g8[g] = min3f(min3f(v[0], v[1], v[2]), min3f(v[3], v[4], v[5]), fminf(v[6], v[7]));
           }
-          const float mn = fminf(fminf(g8[0], g8[1]), fminf(g8[2], g8[3]));
+          const float mn = min3f(g8[0], g8[1], fminf(g8[2], g8[3]));
           if (mn <= thr) {  // rare once the threshold has settled
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
@@ -487,25 +527,25 @@ __global__ void __launch_bounds__(kThreads, 1)
         };
         // tcgen05.ld / wait::ld are .sync.aligned: the warp is converged at each
         __syncwarp();
-        fetch(0, ra, xa, va);
+        fetch(c_begin, ra, va);
         tmem_wait(ra);
 #pragma unroll 1
-        for (uint32_t ch = 0; ch < BN / 32; ch += 2) {
+        for (uint32_t ch = c_begin; ch < c_end; ch += 2) {
           __syncwarp();
-          fetch(ch + 1, rb, xb, vb);
-          score(ch, ra, xa, va);
+          fetch(ch + 1, rb, vb);
+          score(ch, ra, va);
           __syncwarp();
           tmem_wait(rb);
-          if (ch + 2 < BN / 32) fetch(ch + 2, ra, xa, va);
-          score(ch + 1, rb, xb, vb);
+          if (ch + 2 < c_end) fetch(ch + 2, ra, va);
+          score(ch + 1, rb, vb);
           __syncwarp();
-          if (ch + 2 < BN / 32) tmem_wait(ra);
+          if (ch + 2 < c_end) tmem_wait(ra);
         }
         __syncwarp();
         tc_fence_before();
         if (lane == 0) mbar_arrive(tempty(ab));
       }
-      if (ok && live_q) P.cnt[static_cast<size_t>(sp) * P.nq + q] = (over && !P.lenient) ? kOver : cnt;
+      if (ok && live_q) P.cnt[static_cast<size_t>(sub) * P.nq + q] = (over && !P.lenient) ? kOver : cnt;
     }
   }
   __syncwarp();
@@ -1222,8 +1262,9 @@ void store_free(Store* s) {
 // splits on ties; the candidate buffers stay within 1 GiB.
 void choose_splits(uint32_t tiles_q, uint32_t nbt, uint32_t sms, uint32_t k, uint64_t bytes_per_split,
                    uint32_t* splits_out, uint32_t* tps_out) {
-  const uint32_t s0 = std::min<uint32_t>(nbt, std::max<uint32_t>(1, (sms + tiles_q - 1) / tiles_q));
-  uint32_t s_hi = std::min<uint32_t>(nbt, 4u * s0);
+  const uint32_t s0 = std::min<uint32_t>(std::min<uint32_t>(nbt, kSelMaxSplits / 2),
+                                         std::max<uint32_t>(1, (sms + tiles_q - 1) / tiles_q));
+  uint32_t s_hi = std::min<uint32_t>(std::min<uint32_t>(nbt, kSelMaxSplits / 2), 4u * s0);  // 2 buffer sets per split
   while (s_hi > s0 && static_cast<uint64_t>(s_hi) * bytes_per_split > (1ull << 30)) --s_hi;
   const uint64_t overhead = 64u + 2u * static_cast<uint64_t>(k);
   uint64_t best = ~0ull;
@@ -1250,9 +1291,9 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
   const uint32_t nbt = s->n_pad / BN;
   const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
   uint32_t splits = 1, tps = nbt;
-  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, static_cast<uint64_t>(nq_pad) * cap * 8, &splits,
-                &tps);
-  const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(splits * cap, 32), 32));
+  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, 2ull * nq_pad * cap * 8, &splits, &tps);
+  const uint32_t subs = 2 * splits;  // candidate buffers per query: one per (split, half tile)
+  const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(subs * cap, 32), 32));
   uint32_t p2max = 1;
   while (p2max < pool_cap) p2max <<= 1;
 
@@ -1266,8 +1307,8 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     if ((e = sc.qc.ensure(nq_pad * 4ull)) != cudaSuccess) break;
     if ((e = sc.qm.ensure(nq_pad * 4ull)) != cudaSuccess) break;
     if ((e = sc.qq.ensure(nq_pad * 4ull)) != cudaSuccess) break;
-    if ((e = sc.buf.ensure(static_cast<size_t>(splits) * nq * cap * 8)) != cudaSuccess) break;
-    if ((e = sc.cnt.ensure(static_cast<size_t>(splits) * nq * 4)) != cudaSuccess) break;
+    if ((e = sc.buf.ensure(static_cast<size_t>(subs) * nq * cap * 8)) != cudaSuccess) break;
+    if ((e = sc.cnt.ensure(static_cast<size_t>(subs) * nq * 4)) != cudaSuccess) break;
     if ((e = sc.pool.ensure(static_cast<size_t>(nq) * pool_cap * 4)) != cudaSuccess) break;
     if ((e = sc.pool_n.ensure(nq * 4ull)) != cudaSuccess) break;
     if ((e = sc.err.ensure(16)) != cudaSuccess) break;
@@ -1279,7 +1320,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     uint32_t *cnt = sc.cnt.as<uint32_t>(), *pool = sc.pool.as<uint32_t>(), *pool_n = sc.pool_n.as<uint32_t>();
     uint32_t* derr = sc.err.as<uint32_t>();
     // counts of (split, query) pairs an aborted CTA never reached read as 0
-    if ((e = cudaMemsetAsync(cnt, 0, static_cast<size_t>(splits) * nq * 4, st)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(cnt, 0, static_cast<size_t>(subs) * nq * 4, st)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(derr, 0, 16, st)) != cudaSuccess) break;
     what = "query kernel";
     prep_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(nq_pad) * 32 + 255) / 256), 256, 0, st>>>(
@@ -1319,7 +1360,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "select kernel";
-    select_cta_kernel<<<nq, kSelThreads, 0, st>>>(buf, cnt, qm, qq, nq, splits, cap, k, pool, pool_cap, pool_n, derr,
+    select_cta_kernel<<<nq, kSelThreads, 0, st>>>(buf, cnt, qm, qq, nq, subs, cap, k, pool, pool_cap, pool_n, derr,
                                                   0, nullptr, nullptr, nullptr);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "rerank kernel";
@@ -1761,9 +1802,9 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
   const uint32_t nbt = s->n_pad / BN;
   const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
   uint32_t splits = 1, tps = nbt;
-  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, static_cast<uint64_t>(nq_pad) * cap * 8, &splits,
-                &tps);
-  const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(splits * cap, 32), 32));
+  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, 2ull * nq_pad * cap * 8, &splits, &tps);
+  const uint32_t subs = 2 * splits;  // candidate buffers per query: one per (split, half tile)
+  const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(subs * cap, 32), 32));
   uint32_t p2max = 1;
   while (p2max < pool_cap) p2max <<= 1;
   cudaError_t e = cudaSuccess;
@@ -1773,14 +1814,14 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     if ((e = sc->qc.ensure(nq_pad * 4ull)) != cudaSuccess) break;
     if ((e = sc->qm.ensure(nq_pad * 4ull)) != cudaSuccess) break;
     if ((e = sc->qq.ensure(nq_pad * 4ull)) != cudaSuccess) break;
-    if ((e = sc->buf.ensure(static_cast<size_t>(splits) * n_r * cap * 8)) != cudaSuccess) break;
-    if ((e = sc->cnt.ensure(static_cast<size_t>(splits) * n_r * 4)) != cudaSuccess) break;
+    if ((e = sc->buf.ensure(static_cast<size_t>(subs) * n_r * cap * 8)) != cudaSuccess) break;
+    if ((e = sc->cnt.ensure(static_cast<size_t>(subs) * n_r * 4)) != cudaSuccess) break;
     if ((e = sc->pool.ensure(static_cast<size_t>(n_r) * pool_cap * 4)) != cudaSuccess) break;
     if ((e = sc->pool_n.ensure(n_r * 4ull)) != cudaSuccess) break;
     if ((e = sc->err.ensure(16)) != cudaSuccess) break;
     if ((e = sc->gkey.ensure(n_r * 4ull)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(sc->gkey.p, 0xFF, n_r * 4ull, st)) != cudaSuccess) break;
-    if ((e = cudaMemsetAsync(sc->cnt.p, 0, static_cast<size_t>(splits) * n_r * 4, st)) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(sc->cnt.p, 0, static_cast<size_t>(subs) * n_r * 4, st)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(sc->err.p, 0, 16, st)) != cudaSuccess) break;
     what = "gather kernel";
     gather_queries_kernel<<<static_cast<unsigned>((static_cast<uint64_t>(n_r) * 32 + 255) / 256), 256, 0, st>>>(
@@ -1828,7 +1869,7 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     what = "select kernel";
     select_cta_kernel<<<n_r, kSelThreads, 0, st>>>(sc->buf.as<uint64_t>(), sc->cnt.as<uint32_t>(), sc->qm.as<float>(),
-                                                   sc->qq.as<float>(), n_r, splits, cap, k, sc->pool.as<uint32_t>(),
+                                                   sc->qq.as<float>(), n_r, subs, cap, k, sc->pool.as<uint32_t>(),
                                                    pool_cap, sc->pool_n.as<uint32_t>(), sc->err.as<uint32_t>(), 1, a.kq,
                                                    a.qlist, nullptr);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
