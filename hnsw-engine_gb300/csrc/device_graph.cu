@@ -45,6 +45,7 @@ cudaError_t launch_bucket(const uint32_t* efq, const uint32_t* kq, uint32_t nq, 
                           const uint8_t* skip);
 cudaError_t launch_translate_filter(const uint64_t* label_words, uint64_t num_bits, const uint64_t* labels, uint32_t n,
                                     uint32_t* out, cudaStream_t st);
+int build_graph(hgd_build_args* a, int device, std::string* err);
 cudaError_t launch_relayout_l0(const uint32_t* raw, uint64_t n, uint32_t M0, uint32_t* l0, uint32_t l0s, uint32_t* dup,
                                cudaStream_t st);
 }  // namespace hg
@@ -413,6 +414,12 @@ struct hgd_stream {
 extern "C" {
 
 const char* hgd_last_error(void) { return g_err.c_str(); }
+
+int hgd_build_graph(hgd_build_args* args, int device) {
+  std::string err;
+  const int rc = hg::build_graph(args, device, &err);
+  return rc == HGD_OK ? rc : fail(rc, err);
+}
 
 int hgd_graph_upload(const hgd_graph_view* v, int device, int order, hgd_graph** out) {
   if (!v || !out) return fail(HGD_EINVAL, "hgd_graph_upload: null argument");

@@ -28,6 +28,7 @@
 // for a whole insertion only by a node that becomes the new top.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <exception>
 #include <functional>
@@ -315,6 +316,64 @@ void insert_batch(Index::Impl& g, const float* vecs, const uint64_t* labels, std
   worker();  // the calling thread works too
   for (auto& t : pool) t.join();
   if (err) std::rethrow_exception(err);
+}
+
+GpuBuildStats insert_batch_gpu(Index::Impl& g, const float* vecs, const uint64_t* labels, std::size_t n,
+                               const GpuBuildOptions& opt) {
+  // the GPU builder's limits, checked before the index changes
+  if (g.count + n >= (std::size_t{1} << 24))
+    throw std::invalid_argument("add_batch_gpu: the GPU builder takes fewer than 2^24 nodes");
+  if (g.M > 32) throw std::invalid_argument("add_batch_gpu: the GPU builder takes M <= 32");
+  if (g.padded_dim > 1024) throw std::invalid_argument("add_batch_gpu: the GPU builder takes dim <= 1024");
+  if (g.ef_construction > 1024)
+    throw std::invalid_argument("add_batch_gpu: the GPU builder takes ef_construction <= 1024");
+  if (!(opt.wave_fraction >= 0.0)) throw std::invalid_argument("add_batch_gpu: wave_fraction must be >= 0");
+  const std::size_t old_count = g.count, old_upper = g.upper_used;
+  const uint64_t old_rng = g.rng_state;
+  const uint32_t first = store_batch(g, vecs, labels, n);
+  hgd_build_args a{};
+  a.count = g.count;
+  a.first = first;
+  a.dim = g.dim;
+  a.padded_dim = g.padded_dim;
+  a.M = g.M;
+  a.ef_construction = g.ef_construction;
+  a.metric = static_cast<int32_t>(g.params.metric);
+  a.max_level = g.max_level;
+  a.entry_point = g.entry_point;
+  a.wave_min = opt.wave_min;
+  a.wave_max = opt.wave_max;
+  a.wave_fraction = opt.wave_fraction;
+  a.vectors = g.vecs;
+  a.level0 = g.l0;
+  a.upper = g.upper;
+  a.upper_words = g.upper_used;
+  a.upper_offset = g.upper_offset.data();
+  a.levels = g.levels;
+  const auto t0 = std::chrono::steady_clock::now();
+  const int rc = hgd_build_graph(&a, opt.device >= 0 ? opt.device : g.device);
+  const auto t1 = std::chrono::steady_clock::now();
+  if (rc != HGD_OK) {
+    // undo the store: labels, count, upper blocks and the level draws
+    const std::string msg = hgd_last_error();
+    for (std::size_t i = old_count; i < g.count; ++i) {
+      g.label_to_id.erase(g.label_store[i]);
+      g.list0(static_cast<uint32_t>(i))[0] = 0;
+    }
+    std::fill(g.upper_store.begin() + static_cast<std::ptrdiff_t>(old_upper), g.upper_store.end(), 0u);
+    g.count = old_count;
+    g.upper_used = old_upper;
+    g.rng_state = old_rng;
+    if (rc == HGD_EINVAL) throw std::invalid_argument("add_batch_gpu: " + msg);
+    throw std::runtime_error("add_batch_gpu: " + msg);
+  }
+  g.entry_point = a.entry_point;
+  g.max_level = a.max_level;
+  GpuBuildStats st;
+  st.waves = a.waves;
+  st.dropped_proposals = a.dropped_proposals;
+  st.seconds = std::chrono::duration<double>(t1 - t0).count();
+  return st;
 }
 
 }  // namespace hnsw::gb

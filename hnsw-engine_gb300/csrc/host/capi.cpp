@@ -142,6 +142,26 @@ int hg_index_add_batch(hg_index* idx, const float* vecs, const uint64_t* labels,
   });
 }
 
+int hg_index_add_batch_gpu(hg_index* idx, const float* vecs, const uint64_t* labels, size_t n,
+                           hg_build_options* opt) {
+  return guarded([&] {
+    if (!idx) throw std::invalid_argument("add_batch: null index");
+    hnsw::GpuBuildOptions o;
+    if (opt) {
+      o.device = opt->device;
+      o.wave_fraction = opt->wave_fraction;
+      o.wave_min = opt->wave_min;
+      o.wave_max = opt->wave_max;
+    }
+    const hnsw::GpuBuildStats st = idx->index.add_batch_gpu(vecs, labels, n, o);
+    if (opt) {
+      opt->waves = st.waves;
+      opt->dropped_proposals = st.dropped_proposals;
+      opt->seconds = st.seconds;
+    }
+  });
+}
+
 int hg_index_search(const hg_index* idx, const float* q, size_t k, size_t ef, const hg_filter* filter,
                     hg_neighbor* out, size_t* n_out) {
   return guarded([&] {

@@ -190,6 +190,11 @@ namespace hnsw::gb {
 // CPU graph construction (build.cpp): stores a validated batch and links it
 // into the graph with `threads` workers (0 = all hardware threads)
 void insert_batch(Index::Impl& g, const float* vecs, const uint64_t* labels, std::size_t n, std::size_t threads);
+// GPU graph construction (build.cpp + build_graph.cu): stores the batch as
+// insert_batch does, then links it on the GPU; on failure the index is left
+// as it was
+GpuBuildStats insert_batch_gpu(Index::Impl& g, const float* vecs, const uint64_t* labels, std::size_t n,
+                               const GpuBuildOptions& opt);
 
 // launch-shape autotuner (tune.cpp): times candidate shapes per ef bucket on
 // a sample of queries, installs the fastest and returns the table as JSON

@@ -74,13 +74,10 @@ Index& Index::operator=(Index&&) noexcept = default;
 
 void Index::add(const float* vec, uint64_t label) { add_batch(vec, &label, 1, 1); }
 
-void Index::add_batch(const float* vecs, const uint64_t* labels, std::size_t n, std::size_t num_threads) {
-  if (n == 0) return;
-  if (vecs == nullptr || labels == nullptr) throw std::invalid_argument("add_batch: null input");
-  std::unique_lock<std::shared_mutex> lk(impl_->api_mutex);
-  Impl& im = *impl_;
+namespace {
+// every label is checked before the index changes: new, and once per batch
+void check_new_labels(const Index::Impl& im, const uint64_t* labels, std::size_t n) {
   if (im.read_only) throw std::runtime_error("index is read-only (memory-mapped); load without mmap to modify");
-  // every label is checked before the index changes: new, and once per batch
   std::unordered_set<uint64_t> batch;
   batch.reserve(n);
   for (std::size_t i = 0; i < n; ++i) {
@@ -89,9 +86,31 @@ void Index::add_batch(const float* vecs, const uint64_t* labels, std::size_t n, 
     if (!batch.insert(labels[i]).second)
       throw std::invalid_argument("add_batch: duplicate label " + std::to_string(labels[i]) + " in batch");
   }
+}
+}  // namespace
+
+void Index::add_batch(const float* vecs, const uint64_t* labels, std::size_t n, std::size_t num_threads) {
+  if (n == 0) return;
+  if (vecs == nullptr || labels == nullptr) throw std::invalid_argument("add_batch: null input");
+  std::unique_lock<std::shared_mutex> lk(impl_->api_mutex);
+  Impl& im = *impl_;
+  check_new_labels(im, labels, n);
   gb::insert_batch(im, vecs, labels, n, num_threads);
   std::lock_guard<std::mutex> g(im.dev_mutex);
   im.dev_stale = true;
+}
+
+GpuBuildStats Index::add_batch_gpu(const float* vecs, const uint64_t* labels, std::size_t n,
+                                   const GpuBuildOptions& opt) {
+  if (n == 0) return {};
+  if (vecs == nullptr || labels == nullptr) throw std::invalid_argument("add_batch: null input");
+  std::unique_lock<std::shared_mutex> lk(impl_->api_mutex);
+  Impl& im = *impl_;
+  check_new_labels(im, labels, n);
+  const GpuBuildStats st = gb::insert_batch_gpu(im, vecs, labels, n, opt);
+  std::lock_guard<std::mutex> g(im.dev_mutex);
+  im.dev_stale = true;
+  return st;
 }
 
 void Index::mark_deleted(uint64_t label) {

@@ -57,6 +57,11 @@ class _Request(C.Structure):
                 ("reserved", C.c_uint32), ("filter", C.POINTER(_Filter)), ("out", C.c_void_p)]
 
 
+class _BuildOptions(C.Structure):
+    _fields_ = [("device", C.c_int32), ("wave_min", C.c_uint32), ("wave_max", C.c_uint32), ("waves", C.c_uint32),
+                ("wave_fraction", C.c_double), ("dropped_proposals", C.c_uint64), ("seconds", C.c_double)]
+
+
 class _ServerStats(C.Structure):
     _fields_ = [("requests", C.c_uint64), ("queries", C.c_uint64), ("batches", C.c_uint64),
                 ("memory_waits", C.c_uint64), ("elapsed_s", C.c_double), ("qps", C.c_double),
@@ -82,6 +87,7 @@ def lib():
         L.hg_index_save.argtypes = [vp, C.c_char_p]
         L.hg_index_free.argtypes = [vp]
         L.hg_index_add_batch.argtypes = [vp, vp, vp, sz, sz]
+        L.hg_index_add_batch_gpu.argtypes = [vp, vp, vp, sz, C.POINTER(_BuildOptions)]
         L.hg_index_search.argtypes = [vp, vp, sz, sz, C.POINTER(_Filter), vp, C.POINTER(sz)]
         L.hg_index_search_batch.argtypes = [vp, vp, sz, sz, sz, vp, sz, C.POINTER(_Filter)]
         L.hg_index_search_batch_ex.argtypes = [vp, vp, sz, sz, sz, vp, C.POINTER(_BatchOptions)]
@@ -321,6 +327,23 @@ class Index:
             raise ValueError(f"vectors: expected shape (n, {self.dim})")
         labels = _to_labels(ids, v.shape[0], len(self))
         _check(lib().hg_index_add_batch(self._h, _ptr(v), _ptr(labels), v.shape[0], num_threads))
+
+    def add_gpu(self, vectors, ids=None, device: int = -1, wave_fraction: float = 0.0, wave_min: int = 0,
+                wave_max: int = 0) -> dict:
+        """add with the graph linking on the GPU (no counterpart in the
+        reference): same validation, stored rows, labels and levels as add;
+        the graph is judged on recall, not identity.  Returns the waves
+        launched, the reverse edges dropped and the linking's wall time."""
+        v = _float_matrix(vectors, "vectors")
+        if v.ndim == 1:
+            v = v.reshape(1, -1)
+        if v.shape[1] != self.dim:
+            raise ValueError(f"vectors: expected shape (n, {self.dim})")
+        labels = _to_labels(ids, v.shape[0], len(self))
+        o = _BuildOptions(device=int(device), wave_min=int(wave_min), wave_max=int(wave_max),
+                          wave_fraction=float(wave_fraction))
+        _check(lib().hg_index_add_batch_gpu(self._h, _ptr(v), _ptr(labels), v.shape[0], C.byref(o)))
+        return {"waves": int(o.waves), "dropped_proposals": int(o.dropped_proposals), "seconds": float(o.seconds)}
 
     def _queries(self, queries):
         q = _float_matrix(queries, "queries")

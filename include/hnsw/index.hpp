@@ -73,6 +73,22 @@ struct SearchOptions {
   uint32_t filter_scan_mode = 0;
 };
 
+/// Graph construction on the GPU (Index::add_batch_gpu; no counterpart in
+/// the reference).  New nodes are linked in waves that search the graph
+/// built so far, one warp per node; a wave holds at most wave_fraction of the
+/// nodes already linked (at least wave_min, at most wave_max).
+struct GpuBuildOptions {
+  int device = -1;             ///< CUDA device; -1 = the index's (set_device)
+  double wave_fraction = 0.0;  ///< 0 = 0.02
+  uint32_t wave_min = 0;       ///< 0 = 1
+  uint32_t wave_max = 0;       ///< 0 = four times the warps the GPU keeps resident
+};
+struct GpuBuildStats {
+  uint32_t waves = 0;                ///< kernel waves launched
+  uint64_t dropped_proposals = 0;    ///< reverse edges beyond a list's per-wave inbox
+  double seconds = 0.0;              ///< wall time of the GPU linking (upload to download)
+};
+
 class Index {
  public:
   explicit Index(const Params& params);
@@ -84,6 +100,14 @@ class Index {
 
   void add(const float* vec, uint64_t label);
   void add_batch(const float* vecs, const uint64_t* labels, std::size_t n, std::size_t num_threads = 0);
+  /// add_batch with the linking on the GPU (no counterpart in the reference;
+  /// replaces src/index.cpp:273-306's parallel link loop).  The same
+  /// validation, errors, stored rows, labels and levels as add_batch; the
+  /// graph differs from a CPU build's (as a threaded build's does) and is
+  /// judged on recall.  Limits: size() + n < 2^24, M <= 32, dim <= 1024,
+  /// ef_construction <= 1024 (std::invalid_argument beyond them).
+  GpuBuildStats add_batch_gpu(const float* vecs, const uint64_t* labels, std::size_t n,
+                              const GpuBuildOptions& opt = {});
 
   std::vector<Neighbor> search(const float* q, std::size_t k, std::size_t ef = 0, const Filter* f = nullptr) const;
   /// num_threads is accepted for source compatibility; the GPU runs all queries.

@@ -15,6 +15,7 @@
  *   hg_index_save          Index::save                          include/hnsw/index.hpp:83; src/persist.cpp:421-474
  *   hg_index_free          ~Index                               include/hnsw/index.hpp:40
  *   hg_index_add_batch     Index::add_batch                     include/hnsw/index.hpp:50; src/index.cpp:273-306
+ *   hg_index_add_batch_gpu Index::add_batch with the linking on the GPU  src/index.cpp:145-306 (no counterpart call)
  *   hg_index_search        Index::search                        include/hnsw/index.hpp:55; src/search_layer.cpp:173-178
  *   hg_index_search_batch  Index::search_batch                  include/hnsw/index.hpp:59; src/search_layer.cpp:180-194
  *   hg_index_search_batch_ex  search_batch with per-query ef/k/filter (one reference call per group)
@@ -119,6 +120,26 @@ int hg_index_load_device(const char* path, int mmap, int device, hg_index** out)
 int hg_index_save(const hg_index* idx, const char* path);
 void hg_index_free(hg_index* idx);
 int hg_index_add_batch(hg_index* idx, const float* vecs, const uint64_t* labels, size_t n, size_t num_threads);
+
+/* add_batch with the graph linking on the GPU (no counterpart in the
+ * reference).  The same validation, errors, stored rows, labels and levels
+ * as hg_index_add_batch; new nodes are linked in waves that search the graph
+ * built so far, one warp per node, with the reverse edges merged per list
+ * after each wave.  The graph is not the CPU build's (as a threaded build's
+ * is not); it is judged on recall.  Limits: size + n < 2^24, M <= 32,
+ * dim <= 1024, ef_construction <= 1024 (HG_EINVAL beyond them).  opt may be
+ * NULL; its out fields report the waves and the reverse edges dropped. */
+typedef struct {
+  int32_t device;              /* CUDA device, -1 = the index's */
+  uint32_t wave_min;           /* smallest wave, 0 = 1 */
+  uint32_t wave_max;           /* largest wave, 0 = four times the resident warps */
+  uint32_t waves;              /* out */
+  double wave_fraction;        /* new nodes per wave / nodes already linked, 0 = 0.02 */
+  uint64_t dropped_proposals;  /* out */
+  double seconds;              /* out: wall time of the GPU linking */
+} hg_build_options;
+int hg_index_add_batch_gpu(hg_index* idx, const float* vecs, const uint64_t* labels, size_t n,
+                           hg_build_options* opt);
 
 int hg_index_search(const hg_index* idx, const float* q, size_t k, size_t ef, const hg_filter* filter,
                     hg_neighbor* out, size_t* n_out);

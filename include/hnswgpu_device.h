@@ -12,6 +12,7 @@
  *   hgd_graph_set_deleted the tombstone write of mark_deleted  src/index.cpp:308-318
  *   hgd_search            search_unlocked over a batch         src/search_layer.cpp:146-194
  *   hgd_bruteforce        BruteForceIndex::search_batch        src/brute_force.cpp:34-69
+ *   hgd_build_graph       the linking half of add_batch        src/index.cpp:145-306
  */
 #ifndef HNSWGPU_DEVICE_H
 #define HNSWGPU_DEVICE_H
@@ -209,6 +210,37 @@ int hgd_flat_set_path(hgd_flat* f, int path);
 int hgd_flat_last_path(const hgd_flat* f);
 int hgd_bruteforce(hgd_flat* f, const float* queries, uint64_t nq, uint32_t k, const hgd_bitset* filter, void* out,
                    void* stream);
+
+/* Graph construction on the GPU: links nodes [first, count) into the graph
+ * of nodes [0, first) -- the reference's Alg. 1 insertion with the Alg. 4
+ * heuristic (src/index.cpp:127-241), in waves of new nodes that search the
+ * graph built so far, one warp per node, with reverse edges merged per list
+ * after each wave.  The host has stored the nodes already (rows prepared,
+ * levels drawn, upper blocks placed: src/index.cpp:101-121); level0 and
+ * upper are updated in place, entry_point / max_level on return.  The graph
+ * is not the sequential build's (new nodes of one wave do not see each
+ * other); it is judged on recall.  Limits: count < 2^24, 2 <= M <= 32,
+ * padded_dim <= 1024, ef_construction <= 1024. */
+typedef struct {
+  uint64_t count;               /* nodes stored */
+  uint64_t first;               /* first node to link */
+  uint64_t dim, padded_dim, M, ef_construction;
+  int32_t metric;               /* HGD_METRIC_* (cosine rows are unit vectors) */
+  int32_t max_level;            /* in/out: top level of the graph (-1: empty) */
+  uint32_t entry_point;         /* in/out: 0xFFFFFFFF for an empty graph */
+  uint32_t wave_min;            /* smallest wave (0: 1) */
+  uint32_t wave_max;            /* largest wave (0: four times the resident warps) */
+  uint32_t waves;               /* out: waves launched */
+  double wave_fraction;         /* new nodes per wave / nodes already linked (0: 0.02) */
+  const float* vectors;         /* count x padded_dim (host) */
+  uint32_t* level0;             /* count x (1 + 2M): [n, ids...] (host, in/out) */
+  uint32_t* upper;              /* upper_words (host, in/out) */
+  uint64_t upper_words;
+  const uint64_t* upper_offset; /* count: word offset of a node's level-1 block */
+  const uint8_t* levels;        /* count */
+  uint64_t dropped_proposals;   /* out: reverse edges beyond a list's per-wave inbox (64) */
+} hgd_build_args;
+int hgd_build_graph(hgd_build_args* args, int device);
 
 const char* hgd_last_error(void);
 

@@ -1,0 +1,146 @@
+"""Graph construction on the GPU (Index.add_gpu, hg_index_add_batch_gpu).
+
+The reference links new nodes on the CPU (src/index.cpp:145-306: Alg. 1
+with the Alg. 4 heuristic and re-chosen reverse edges).  The GPU builder
+stores the same rows, labels and levels (the host's store step draws the
+levels exactly as the reference) and links them in waves, one warp per new
+node.  Its graph is not the sequential build's -- new nodes of one wave do
+not see each other, as concurrent inserters of a threaded reference build
+do not -- so it is judged the way a threaded build is:
+
+* on recall@10 against exact k-NN, next to the CPU build of the same data
+  (the reference's single-threaded graph byte for byte), at every ef;
+* on the invariants the reference's loader checks (ids in range, neighbours
+  on the layer, degree caps): the built index is saved and loaded back;
+* on the plain search staying id-exact with the reference on this graph too:
+  the GPU's answers on the GPU-built file equal the oracle's.
+"""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+EFS = (10, 20, 40, 80, 160)
+
+
+def exact_knn(base, q, k, metric):
+    b = base.astype(np.float64)
+    x = q.astype(np.float64)
+    if metric == "cosine":
+        b = b / np.maximum(np.linalg.norm(b, axis=1, keepdims=True), 1e-300)
+        x = x / np.maximum(np.linalg.norm(x, axis=1, keepdims=True), 1e-300)
+    if metric == "l2":
+        d = (x * x).sum(1)[:, None] - 2.0 * x @ b.T + (b * b).sum(1)[None, :]
+    else:
+        d = 1.0 - x @ b.T
+    return np.argsort(d, axis=1, kind="stable")[:, :k]
+
+
+def recall(labels, gt):
+    hit = 0
+    for row, g in zip(labels, gt):
+        hit += len(set(row.tolist()) & set(g.tolist()))
+    return hit / gt.size
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["c1", "c3s", "c4s"])
+def test_recall_next_to_cpu_build(hg, oracle, graphs, tmp_path, name):
+    base, q, metric, M, efc = graphs.data(name)
+    cpu = hg.Index.load(graphs.path(name))
+    gpu = hg.Index(base.shape[1], metric, M, efc)
+    st = gpu.add_gpu(base)
+    assert st["waves"] > 1
+    path = tmp_path / f"{name}_gpu.idx"
+    gpu.save(path)
+    back = hg.Index.load(path)  # the loader's graph checks
+    assert len(back) == base.shape[0]
+    assert back.max_level == cpu.max_level  # the same level draws
+    gt = exact_knn(base, q, 10, metric)
+    for ef in EFS:
+        rc = recall(cpu.search_raw(q, 10, ef)["label"].astype(np.int64), gt)
+        rg = recall(back.search_raw(q, 10, ef)["label"].astype(np.int64), gt)
+        assert rg >= rc - 0.01, f"{name} ef={ef}: GPU-built {rg:.4f} vs CPU-built {rc:.4f}"
+    # the plain search is exact on this graph as on any: the oracle agrees
+    rec = back.search_raw(q, 10, 40)
+    ol, od = oracle.OracleIndex(path).search_batch(q, 10, 40)
+    np.testing.assert_array_equal(rec["label"], ol)
+    assert rec["distance"].tobytes() == od.tobytes()
+
+
+@pytest.mark.gpu
+def test_incremental_batches(hg, graphs, tmp_path):
+    """CPU-built nodes, then two GPU batches with explicit labels: the same
+    recall as one CPU build, and lookups by label work."""
+    base, q, metric, M, efc = graphs.data("c1")
+    n = base.shape[0]
+    ix = hg.Index(base.shape[1], metric, M, efc)
+    ix.add(base[:3000], ids=np.arange(3000) + 7, num_threads=1)
+    ix.add_gpu(base[3000:12000], ids=np.arange(3000, 12000) + 7)
+    ix.add_gpu(base[12000:], ids=np.arange(12000, n) + 7, wave_fraction=0.05)
+    assert len(ix) == n and 7 in ix and (n + 6) in ix
+    np.testing.assert_array_equal(ix.get_vector(12007), base[12000])
+    path = tmp_path / "inc.idx"
+    ix.save(path)
+    back = hg.Index.load(path)
+    cpu = hg.Index.load(graphs.path("c1"))
+    gt = exact_knn(base, q, 10, metric)
+    for ef in (20, 80):
+        rc = recall(cpu.search_raw(q, 10, ef)["label"].astype(np.int64), gt)
+        rg = recall(back.search_raw(q, 10, ef)["label"].astype(np.int64) - 7, gt)
+        assert rg >= rc - 0.01, f"ef={ef}: {rg:.4f} vs {rc:.4f}"
+
+
+@pytest.mark.gpu
+def test_small_and_degenerate(hg, tmp_path):
+    """One node, a few nodes, identical vectors, wave sizes forced to extremes."""
+    rng = np.random.default_rng(5)
+    one = hg.Index(16, "l2", 4, 20)
+    one.add_gpu(rng.random((1, 16), dtype=np.float32))
+    assert len(one) == 1 and one.max_level >= 0
+    few = hg.Index(16, "l2", 4, 20)
+    x = rng.random((7, 16), dtype=np.float32)
+    few.add_gpu(x)
+    lab, _ = few.search(x, k=7, ef=20)
+    assert sorted(lab[0].tolist()) == list(range(7))  # 7 nodes: every one reachable
+    same = hg.Index(8, "l2", 4, 16)
+    same.add_gpu(np.ones((300, 8), np.float32), wave_max=16)
+    lab, dist = same.search(np.ones((1, 8), np.float32), k=5, ef=16)
+    assert (dist == 0).all() and (lab >= 0).all()
+    big = hg.Index(32, "ip", 8, 64)
+    data = rng.standard_normal((5000, 32)).astype(np.float32)
+    st = big.add_gpu(data, wave_fraction=0.5, wave_min=64)
+    assert st["waves"] < 200
+    p = tmp_path / "big.idx"
+    big.save(p)
+    hg.Index.load(p)
+
+
+def test_limits_leave_the_index_unchanged(hg):
+    """Shapes the GPU builder does not take are refused before anything is
+    stored (no GPU needed): M above 32, dim above 1024, bad wave fraction,
+    duplicate or existing labels, a read-only index."""
+    x = np.zeros((4, 16), np.float32)
+    wide = hg.Index(16, "l2", 40, 100)
+    with pytest.raises(ValueError, match="M <= 32"):
+        wide.add_gpu(x)
+    assert len(wide) == 0
+    tall = hg.Index(1040, "l2", 8, 100)
+    with pytest.raises(ValueError, match="dim <= 1024"):
+        tall.add_gpu(np.zeros((2, 1040), np.float32))
+    assert len(tall) == 0
+    ok = hg.Index(16, "l2", 8, 100)
+    with pytest.raises(ValueError, match="wave_fraction"):
+        ok.add_gpu(x, wave_fraction=-1.0)
+    with pytest.raises(ValueError, match="duplicate label"):
+        ok.add_gpu(x, ids=[1, 2, 2, 3])
+    assert len(ok) == 0
+    ro = hg.Index.load(GOLD / "five.idx", mmap=True)
+    n = len(ro)
+    with pytest.raises(RuntimeError, match="read-only"):
+        ro.add_gpu(np.zeros((1, ro.dim), np.float32), ids=[10**6])
+    assert len(ro) == n
