@@ -399,15 +399,47 @@ def run_ours(args, rank, world, local):
     }
     if rank == 0 and world == 1:
         result["cpu_baseline"] = cpu_baseline(ix, gpath, queries, plain_ef)
+        if not args.no_build:
+            result["build"] = run_build(ix, base, sample, gt, build_s, build_how)
         del ix
         if not args.no_batched:
             result["batched_200k"] = run_batched_200k(local, use_graph)
+            result["filtered_200k"] = run_filtered_200k(local)
         if not args.no_serving:
             result["serving"] = run_serving(local, gpath)
         if not args.no_precision:
             result["precision"] = run_precision(local)
         result["load"] = run_load(gpath, queries[:1])
     return result
+
+
+def run_build(ix_ref, base, sample, gt, ref_s, ref_how):
+    """Graph construction on the GPU (Index.add_gpu) over the headline's 1M
+    rows, against the reference's add_batch on all host threads (timed when
+    the bench built the file in this run): wall time, and recall@10 of the
+    plain FP32 walk on both graphs at several ef over the recall sample."""
+    import hnswgpu
+    import workloads
+
+    g = hnswgpu.Index(HEAD_DIM, "l2", M, EFC)
+    t = time.perf_counter()
+    st = g.add_gpu(base)
+    wall = time.perf_counter() - t
+    rows = []
+    for ef in (16, 32, 48, 96):
+        r_ref = workloads.recall_at_k(ix_ref.search_raw(sample, HEAD_K, ef)["label"].astype(np.int64), gt)
+        r_gpu = workloads.recall_at_k(g.search_raw(sample, HEAD_K, ef)["label"].astype(np.int64), gt)
+        rows.append({"ef": ef, "recall_at_10_reference_graph": round(r_ref, 4),
+                     "recall_at_10_gpu_graph": round(r_gpu, 4)})
+    del g
+    return {"workload": f"the headline rows: n={HEAD_N} d={HEAD_DIM} M={M} efC={EFC}",
+            "gpu_add_batch_s": round(wall, 3), "gpu_linking_s": round(st["seconds"], 3), "waves": st["waves"],
+            "dropped_proposals": st["dropped_proposals"],
+            "reference_add_batch_s": round(ref_s, 2) if ref_how == "built" else None,
+            "reference_threads": os.cpu_count(),
+            "note": "gpu_add_batch_s covers the host store, the upload, the linking and the download; "
+                    "recall of the plain walk, ground truth exact k-NN",
+            "recall": rows}
 
 
 def run_load(gpath, q1):
@@ -544,6 +576,90 @@ def run_batched_200k(local, use_graph=True):
 
 
 # ---------------------------------------------------------------------------
+# cosine with filters and deletes at 200k: per-query k / ef / filter
+# ---------------------------------------------------------------------------
+C3_N, C3_DIM, C3_CENTERS, C3_NQ = 200_000, 100, 1000, 10_000
+C3_EFS, C3_KS = (40, 100, 200, 400), (10, 100)
+
+
+def run_filtered_200k(local):
+    """200,000 x 100 unit vectors (cosine), 1% of the labels deleted (seed 2),
+    10,000 queries, half filtered to label % 10 == 0, k in {10, 100} and ef in
+    {40..400} per query: one GPU call (plain FP32) against the reference's
+    search_batch, one call per (filtered, k, ef) group; ids and distances
+    compared, recall@10 against exact k-NN over the allowed live rows."""
+    import hnswgpu
+    import refcore
+    import workloads
+
+    base, queries = workloads.unit_mixture(C3_N, C3_DIM, C3_CENTERS, C3_NQ)
+    gpath, build_s, how = bench_graph("cos-200k", base, "cosine")
+    dels = workloads.random_deletes(C3_N, 0.01, seed=2)
+    keep = np.arange(C3_N) % 10 == 0
+    fw = workloads.mask_to_words(keep)
+    rng = np.random.default_rng(3)
+    filt = rng.random(C3_NQ) < 0.5
+    ks = rng.choice(np.array(C3_KS, dtype=np.uint32), C3_NQ)
+    efs = rng.choice(np.array(C3_EFS, dtype=np.uint32), C3_NQ)
+    fsel = np.where(filt, 0, -1).astype(np.int32)
+    kmax = max(C3_KS)
+    ix = hnswgpu.Index.load(gpath)
+    ix.set_device(local)
+    for lab in dels:
+        ix.mark_deleted(int(lab))
+    bits = [hnswgpu.Bitset(fw, C3_N)]
+    times = []
+    for i in range(4):  # the first call uploads the graph and warms up
+        t = time.perf_counter()
+        rec = ix.search_batch_ex(queries, kmax, ef_per_query=efs, k_per_query=ks, filters=bits, filter_of_query=fsel)
+        if i:
+            times.append(time.perf_counter() - t)
+    gpu_s = statistics.median(times)
+
+    rx = refcore.RefIndex(gpath)
+    for lab in dels:
+        rx.mark_deleted(int(lab))
+    rbits = refcore.Bitset(fw, C3_N)
+    threads = os.cpu_count() or 1
+    groups, batches = [], []
+    for f in (False, True):
+        for k in C3_KS:
+            for ef in C3_EFS:
+                g = np.nonzero((filt == f) & (ks == k) & (efs == ef))[0]
+                if g.size:
+                    groups.append((g, k))
+                    batches.append((queries[g], int(k), int(ef), rbits if f else None))
+    ref_time_batches(rx, batches, threads)  # warm-up
+    el, outs = ref_time_batches(rx, batches, threads)
+    ids = dist = 0
+    for (g, k), o in zip(groups, outs):
+        got = rec[g, :k]
+        ids += int((got["label"] != o["label"]).sum())
+        dist += int((got["distance"].view(np.uint32) != o["distance"].view(np.uint32)).sum())
+    # recall@10 against exact k-NN over the rows each query may return
+    alive = np.ones(C3_N, dtype=bool)
+    alive[dels.astype(np.int64)] = False
+    bf = hnswgpu.BruteForceIndex(C3_DIM, "cosine")
+    bf.add(base)
+    hit = 0
+    for f in (False, True):
+        g = np.nonzero(filt == f)[0]
+        gt = bf.search_raw(queries[g], 10, filter=alive & keep if f else alive)["label"].astype(np.int64)
+        hit += workloads.recall_at_k(rec[g, :10]["label"].astype(np.int64), gt) * g.size
+    del bf
+    return {"workload": f"cosine-200k: n={C3_N} d={C3_DIM} unit vectors ({C3_CENTERS} centres, noise 0.3) M={M} "
+                        f"efC={EFC} (reference add_batch), 1% deleted, {C3_NQ} queries, half filtered to "
+                        f"label % 10 == 0, k in {list(C3_KS)}, ef in {list(C3_EFS)} per query",
+            "graph_seconds": round(build_s, 1), "graph": how,
+            "qps": round(C3_NQ / gpu_s, 1), "note": "one host call (copies included), median of 3",
+            "recall_at_10": round(hit / C3_NQ, 4),
+            "reference_qps": round(C3_NQ / el, 1),
+            "reference": f"search_batch per (filtered, k, ef) group ({len(batches)} calls), {threads} threads, "
+                         f"simd {refcore.isa()}",
+            "parity_vs_reference": {"queries": C3_NQ, "id_mismatches": ids, "distance_bit_mismatches": dist}}
+
+
+# ---------------------------------------------------------------------------
 # serving at 1M
 # ---------------------------------------------------------------------------
 SERVE_REQUESTS = 20_000
@@ -551,6 +667,7 @@ SERVE_LOADS = (0.25, 0.5, 0.75, 1.0)
 SERVE_FILTERS = 16  # pool of distinct random 10%-density bitsets
 SERVE_RECALL_REQUESTS = 2000
 SERVE_PLAIN_REQUESTS = 500
+SERVE_PARITY_REQUESTS = 1000  # requests also answered by the reference's search_batch
 SERVE_FORMS = (
     # name, server options (batch slots and batch size: 4 x 8,192 queries
     # unless given; smaller batches trade peak for latency)
@@ -649,6 +766,27 @@ def run_serving(local, gpath):
         return round(r_all / sample_q, 4), round(r10 / max(n10, 1), 4)
 
     plain_recall = recall(lambda q, k: plain[q, :k]["label"].astype(np.int64))
+
+    # the reference's own search_batch, one call per request (its k, ef and
+    # filter), over the first requests: ids and distance bits against the
+    # batched plain answers (and below against the served FP32 answers)
+    import refcore
+
+    rx = refcore.RefIndex(gpath)
+    ref_bits = [refcore.Bitset(workloads.mask_to_words(m), HEAD_N) for m in masks]
+    ref_rows = [rx.search_batch(requests[i][0], requests[i][1], requests[i][2], threads=0,
+                                filt=ref_bits[fsel[i]] if fsel[i] >= 0 else None)
+                for i in range(SERVE_PARITY_REQUESTS)]
+    del rx
+
+    def vs_reference(rows_of_request):
+        ids = dist = 0
+        for i in range(SERVE_PARITY_REQUESTS):
+            got, ref = rows_of_request(i), ref_rows[i]
+            ids += int((got["label"] != ref["label"]).any(1).sum())
+            dist += int((got["distance"].view(np.uint32) != ref["distance"].view(np.uint32)).any(1).sum())
+        return {"requests": SERVE_PARITY_REQUESTS, "queries": int(offs[SERVE_PARITY_REQUESTS]),
+                "id_mismatches": ids, "distance_bit_mismatches": dist}
     out = {"workload": f"serving-L2-1M: the headline graph, {SERVE_REQUESTS} requests, {total_q} queries, 1..256 "
                        f"queries/request log-uniform, k in {{1,10,100}}, ef in {{16..512 step 16}}, 20% with a "
                        f"10%-density bitset (pool of {SERVE_FILTERS})",
@@ -657,7 +795,9 @@ def run_serving(local, gpath):
                "qps": round(per_request_qps, 1), "requests": SERVE_PLAIN_REQUESTS,
                "note": "one search_batch call per request (the reference API: one k / ef / filter per call)"},
            "batched_fp32_search_batch_ex": {"qps": round(plain_qps, 1), "recall_at_k": plain_recall[0],
-                                            "recall_at_10": plain_recall[1], "queries_per_call": chunk}}
+                                            "recall_at_10": plain_recall[1], "queries_per_call": chunk,
+                                            "parity_vs_reference": vs_reference(
+                                                lambda i: plain[offs[i]:offs[i + 1], :ks[i]])}}
     for name, opts in SERVE_FORMS:
         srv = hnswgpu.Server(ix, **{"max_inflight": 4, "max_batch_queries": 8192, **opts})
         srv.replay(requests[:2000], np.zeros(2000))  # warm-up: encodes the copy, sizes the staging
@@ -670,6 +810,7 @@ def run_serving(local, gpath):
                 "loads": []}
         if same is not None:
             form["identical_to_plain_search_batch"] = bool(same)
+            form["parity_vs_reference"] = vs_reference(lambda i: outs[i])
         mean_q = total_q / SERVE_REQUESTS
         for load in SERVE_LOADS:
             rate = load * peak["qps"] / mean_q  # requests per second
@@ -699,6 +840,7 @@ def run_serving(local, gpath):
 # ---------------------------------------------------------------------------
 PREC_N, PREC_DIM, PREC_NQ = 200_000, 960, 5_000
 PREC_EFS = (40, 64, 128, 256, 512, 1024)
+PREC_PARITY_EFS = (40, 128, 512)
 
 
 def run_precision(local):
@@ -745,6 +887,7 @@ def run_precision(local):
     out = {"workload": f"precision-L2-960: n={PREC_N} d={PREC_DIM} M={M} efC={EFC} (reference add_batch), "
                        f"{PREC_NQ} queries, k={HEAD_K}",
            "graph_seconds": round(build_s, 1), "graph": how, "traversal_distance_error_vs_fp64": trav, "variants": {}}
+    plain_rows = {}
     for name, prec in (("fp32", 0), ("fp16_rerank", 1), ("fp8_rerank", 2)):
         rows = []
         for ef in PREC_EFS:
@@ -763,10 +906,22 @@ def run_precision(local):
             got = rec["label"].astype(np.int64)
             d64 = ((b64[got] - q64[:, None, :]) ** 2).sum(-1)
             rel = np.abs(rec["distance"].astype(np.float64) - d64) / np.maximum(d64, 1e-30)
+            if prec == 0 and ef in PREC_PARITY_EFS:
+                plain_rows[ef] = rec.copy()
             rows.append({"ef": ef, "qps": round(PREC_NQ / (statistics.median(ms) / 1e3), 1),
                          "recall_at_10": round(workloads.recall_at_k(got, gt), 4),
                          "dist_mean_rel_err_vs_fp64": float(rel.mean()), "dist_max_rel_err_vs_fp64": float(rel.max())})
         out["variants"][name] = rows
+    # the plain FP32 path against the reference's own search_batch on all
+    # queries: ids and distance bits
+    import refcore
+
+    rx = refcore.RefIndex(gpath)
+    out["fp32_parity_vs_reference"] = []
+    for ef, rec in plain_rows.items():
+        out["fp32_parity_vs_reference"].append({"ef": ef, "queries": PREC_NQ,
+                                                **parity(rec, rx.search_batch(queries, HEAD_K, ef, threads=0))})
+    del rx
     best = max(r["recall_at_10"] for r in out["variants"]["fp32"])
     out["recall_target_reached"] = best >= RECALL_TARGET
     out["largest_ef"] = PREC_EFS[-1]
@@ -841,6 +996,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 200k mixed-ef block")
     ap.add_argument("--no-serving", action="store_true", help="skip the 1M serving block")
     ap.add_argument("--no-precision", action="store_true", help="skip the d=960 precision block")
+    ap.add_argument("--no-build", action="store_true", help="skip the GPU graph-construction block")
     ap.add_argument("--launch", choices=["graph", "streams"], default="graph",
                     help="timed steps: one CUDA-graph replay, or kernel launches (for a profiler)")
     args = ap.parse_args()

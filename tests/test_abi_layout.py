@@ -20,7 +20,7 @@ def test_ctypes_structs_match_the_c_header(hg, tmp_path):
         pytest.skip("no C compiler")
     pairs = [(hg._Filter, "hg_filter"), (hg._BatchOptions, "hg_batch_options"),
              (hg._ServerConfig, "hg_server_config"), (hg._Request, "hg_request"),
-             (hg._ServerStats, "hg_server_stats")]
+             (hg._ServerStats, "hg_server_stats"), (hg._BuildOptions, "hg_build_options")]
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "hnswgpu.h"', "int main(void) {"]
     for py, c in pairs:
         lines.append(f'  printf("{c} size %zu\\n", sizeof({c}));')
