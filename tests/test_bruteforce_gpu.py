@@ -124,3 +124,31 @@ def test_auto_path_uses_tensor_cores(hg, graphs):
     bf.add(base)
     bf.search_raw(q[:10], 10)
     assert bf.last_path == 2
+
+
+def test_seeded_thresholds_large_k(hg, oracle):
+    """k >= 64 over >= 2,048 queries: the GEMM first runs a bound pass that
+    keeps each (query, half tile)'s smallest score, and every query's scan
+    starts from the k-th smallest of those minima plus its margin.  Float
+    data (margin path) with and without a filter, and integer data with many
+    ties (exact mode), against the oracle."""
+    import workloads
+
+    rng = np.random.default_rng(13)
+    base = rng.normal(size=(30_000, 48)).astype(np.float32)
+    q = rng.normal(size=(2_100, 48)).astype(np.float32)
+    bf = _bf(hg, 48, "l2", base, 2)
+    rec = bf.search_raw(q, 100)
+    ol, od = oracle.bruteforce(base, q, 100, "l2")
+    _eq(rec, ol.astype(np.int64), od, "seeded k=100")
+    _answered(bf, 2)
+    fw = workloads.label_filter_bits(30_000, lambda x: x % 5 == 1)
+    rec = bf.search_raw(q, 64, filter=hg.Bitset(fw, 30_000))
+    ol, od = oracle.bruteforce(base, q, 64, "l2", filt=(fw, 30_000))
+    _eq(rec, ol.astype(np.int64), od, "seeded k=64 filtered")
+    ints = rng.integers(0, 8, size=(6000, 16)).astype(np.float32)
+    qi = rng.integers(0, 8, size=(2_500, 16)).astype(np.float32)
+    bi = _bf(hg, 16, "l2", ints, 2)
+    rec = bi.search_raw(qi, 80)
+    ol, od = oracle.bruteforce(ints, qi, 80, "l2")
+    _eq(rec, ol.astype(np.int64), od, "seeded ties")

@@ -135,3 +135,25 @@ def test_filter_scan_mode_is_validated(hg, graphs):
     with pytest.raises(ValueError):
         ix.search_batch_ex(np.zeros((1, 128), np.float32), 1, 16, precision=2, filter_scan=0.1,
                            filter_scan_mode="rows")
+
+
+def test_routed_every_row_seeded_large_k(hg, oracle, graphs):
+    """2,100 routed queries at k = 100 over every row: the scan's thresholds
+    are seeded by the bound pass; answers are the exact k nearest allowed,
+    live rows."""
+    import workloads
+
+    base, q, *_ = graphs.data("c1")
+    n = base.shape[0]
+    ix = hg.Index.load(graphs.path("c1"))
+    for lab in (3, 4000, 12345):
+        ix.mark_deleted(lab)
+    rare = _mask(n, lambda i: i % 16 == 5)
+    qq = np.concatenate([q, q, q[:100]])
+    out = ix.search_batch_ex(qq, 100, 128, filters=[rare], filter_of_query=np.zeros(qq.shape[0], np.int32),
+                             precision=2, filter_scan=0.1, filter_scan_mode="every_row")
+    live = rare.copy()
+    live[[3, 4000, 12345]] = False
+    ol, od = oracle.bruteforce(base, qq, 100, "l2", filt=(workloads.mask_to_words(live), n))
+    np.testing.assert_array_equal(out["label"], ol)
+    assert out["distance"].tobytes() == od.tobytes()
