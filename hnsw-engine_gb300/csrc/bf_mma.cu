@@ -52,8 +52,21 @@ constexpr int BK = 64;   // FP16 elements per K chunk: one 128-byte swizzle atom
 constexpr int kStages = 4;
 constexpr uint32_t kABytes = BM * BK * 2;
 constexpr uint32_t kBBytes = BN * BK * 2;
-constexpr int kEpiWarps = 8;   // two per TMEM lane quarter, each over half of a tile's rows
-constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-9 epilogue
+// Epilogue warps per CTA: EPI = 8 (two per TMEM lane quarter, each over
+// half of a tile's rows, chunks software-pipelined) for scans of few query
+// tiles, EPI = 16 (four per quarter, a quarter of the rows each, 96
+// registers) for many: warp 0 is the TMA producer, warp 1 issues the MMAs
+// and owns TMEM, warps 2 .. EPI + 1 score.
+template <int EPI>
+struct Epi {
+  static constexpr int kWarps = EPI;
+  static constexpr uint32_t kParts = EPI / 4;           // column parts of a tile
+  static constexpr uint32_t kPartCols = BN / kParts;    // tile rows per warp
+  static constexpr uint32_t kPartChunks = kPartCols / 32;
+  static constexpr int kThreads = 64 + 32 * EPI;
+};
+// scans of at least this many query tiles use the sixteen-warp epilogue
+constexpr uint32_t kWideEpiTiles = 8;
 constexpr uint32_t kTmemCols = 512;
 constexpr size_t kSmem = kStages * (kABytes + kBBytes) + 1024;
 constexpr uint32_t kOver = 0xFFFFFFFFu;
@@ -71,7 +84,7 @@ struct MmaParams {
   const uint32_t* allow;  // bits over rows or null
   const float* qc;        // nq_pad: s = xn + acc * qc
   const float* qm;        // nq_pad: selection margin 2E
-  uint64_t* buf;          // (2 x splits) x nq x cap candidate keys: one set per half tile
+  uint64_t* buf;          // (parts x splits) x nq x cap candidate keys: one set per tile part
   uint32_t* cnt;          // (2 x splits) x nq: candidates kept, or kOver
   uint32_t* err;          // [0] pipeline wait expired
   // per-query filters (routed graph queries): bits over rows of filter
@@ -86,8 +99,8 @@ struct MmaParams {
   uint32_t trig;  // a lane's buffer is compacted once it could pass trig - 32 keys (<= cap)
   int l2;
   int lenient;  // keep the buffer of a query whose candidates overflow (approximate answer) instead of failing
-  // bound pass: keep nothing; write each (half tile, query)'s smallest score
-  // to mins[(2 * row tile + half) * nq_pad + q] (+inf if no row is allowed)
+  // bound pass: keep nothing; write each (tile part, query)'s smallest score
+  // to mins[(parts * row tile + part) * nq_pad + q] (+inf if no row is allowed)
   int bound_pass;
   float* mins;
   uint32_t nq_pad;
@@ -291,8 +304,12 @@ __device__ __noinline__ uint32_t warp_compact(uint64_t* b, uint32_t cnt, uint32_
   return w;
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+template <int EPI>
+__global__ void __launch_bounds__(Epi<EPI>::kThreads, 1)
     bf_mma_kernel(const __grid_constant__ CUtensorMap map_q, const __grid_constant__ CUtensorMap map_x, MmaParams P) {
+  constexpr int kEpiWarps = Epi<EPI>::kWarps;
+  constexpr uint32_t kParts = Epi<EPI>::kParts, kPartCols = Epi<EPI>::kPartCols;
+  constexpr uint32_t kPartChunks = Epi<EPI>::kPartChunks;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[2 * kStages + 5];
   __shared__ uint32_t tmem_slot;
@@ -409,12 +426,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // ---- epilogue: one query per thread (TMEM lane); a warp scores half of a
-    // tile's 256 rows (chunks 4 * half .. 4 * half + 3), keeping its own
-    // candidate buffers (sub-split 2 * split + half) ----
+    // ---- epilogue: one query per thread (TMEM lane); a warp scores one part
+    // of a tile's 256 rows, chunks kPartChunks * part .. kPartChunks *
+    // (part + 1) - 1, keeping its own candidate buffers (sub-split kParts *
+    // split + part) ----
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);
-    const uint32_t half = static_cast<uint32_t>(warp - 2) / 4u;
-    const uint32_t c_begin = half * (BN / 64), c_end = c_begin + BN / 64;
+    const uint32_t part = static_cast<uint32_t>(warp - 2) / 4u;
+    const uint32_t c_begin = part * kPartChunks, c_end = c_begin + kPartChunks;
     const uint32_t row_in_tile = quarter * 32u + static_cast<uint32_t>(lane);
     uint32_t acc_i = 0;
     bool ok = true;
@@ -427,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t* allow_q = P.fsel ? (fq >= 0 ? P.allow_tab[fq] : nullptr) : P.allow;
       const float cq = P.qc[q];
       const float margin = P.qm[q];
-      const uint32_t sub = 2u * sp + half;
+      const uint32_t sub = kParts * sp + part;
       uint64_t* bufp = P.buf + (static_cast<size_t>(sub) * P.nq + (live_q ? q : 0)) * P.cap;
       uint32_t cnt = 0;
       uint32_t lim = P.trig;  // compaction point: the threshold tightens early
@@ -436,9 +454,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool over = false;
       for (uint32_t bt = b0; bt < b1; ++bt, ++acc_i) {
         const uint32_t ab = acc_i & 1u, aph = (acc_i >> 1) & 1u;
-        float tmin = __int_as_float(0x7f800000);  // bound pass: the half tile's smallest score
-        if (bt + 1 < b1 && lane < 4)  // the next tile's row norms of this half (512 bytes) into L1
-          asm volatile("prefetch.global.L1 [%0];" ::"l"(P.xn + (bt + 1) * BN + half * 128u + lane * 32u));
+        float tmin = __int_as_float(0x7f800000);  // bound pass: the part's smallest score
+        if (bt + 1 < b1 && lane < static_cast<int>(kPartCols / 32))  // the next tile's row norms of this part into L1
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(P.xn + (bt + 1) * BN + part * kPartCols + lane * 32u));
         // the bound of the other splits of this query (a split's k-th
         // smallest + the margin bounds the k-th over all rows from above)
         if (live_q && !over && !P.bound_pass) {
@@ -454,11 +472,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tc_fence_after();
         const uint32_t taddr = tmem + ((quarter * 32u) << 16) + ab * BN;
-        // Software-pipelined over the warp's 4 chunks of 32 rows: the TMEM
-        // load and the filter and tombstone words of chunk ch + 1 are in
-        // flight while chunk ch is scored.
-        uint32_t ra[32], rb[32];
-        uint32_t va = 0, vb = 0;
         auto fetch = [&](uint32_t ch, uint32_t (&r)[32], uint32_t& valid) {
           tmem_ld32_async(taddr + ch * 32u, r);
           const uint32_t j0 = bt * BN + ch * 32u;
@@ -543,25 +556,43 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         };
         // tcgen05.ld / wait::ld are .sync.aligned: the warp is converged at each
-        __syncwarp();
-        fetch(c_begin, ra, va);
-        tmem_wait(ra);
+        if constexpr (kPartChunks >= 4) {
+          // two warps per scheduler: the TMEM load and the filter and
+          // tombstone words of chunk ch + 1 are in flight while chunk ch is
+          // scored
+          uint32_t ra[32], rb[32];
+          uint32_t va = 0, vb = 0;
+          __syncwarp();
+          fetch(c_begin, ra, va);
+          tmem_wait(ra);
 #pragma unroll 1
-        for (uint32_t ch = c_begin; ch < c_end; ch += 2) {
-          __syncwarp();
-          fetch(ch + 1, rb, vb);
-          score(ch, ra, va);
-          __syncwarp();
-          tmem_wait(rb);
-          if (ch + 2 < c_end) fetch(ch + 2, ra, va);
-          score(ch + 1, rb, vb);
-          __syncwarp();
-          if (ch + 2 < c_end) tmem_wait(ra);
+          for (uint32_t ch = c_begin; ch < c_end; ch += 2) {
+            __syncwarp();
+            fetch(ch + 1, rb, vb);
+            score(ch, ra, va);
+            __syncwarp();
+            tmem_wait(rb);
+            if (ch + 2 < c_end) fetch(ch + 2, ra, va);
+            score(ch + 1, rb, vb);
+            __syncwarp();
+            if (ch + 2 < c_end) tmem_wait(ra);
+          }
+        } else {
+          // four warps per scheduler hide the loads; one chunk in registers
+#pragma unroll 1
+          for (uint32_t ch = c_begin; ch < c_end; ++ch) {
+            __syncwarp();
+            uint32_t ra[32];
+            uint32_t va = 0;
+            fetch(ch, ra, va);
+            tmem_wait(ra);
+            score(ch, ra, va);
+          }
         }
         __syncwarp();
         tc_fence_before();
         if (lane == 0) mbar_arrive(tempty(ab));
-        if (P.bound_pass) P.mins[(2ull * bt + half) * P.nq_pad + qt * BM + row_in_tile] = tmin;
+        if (P.bound_pass) P.mins[(static_cast<uint64_t>(kParts) * bt + part) * P.nq_pad + qt * BM + row_in_tile] = tmin;
       }
       if (ok && live_q && !P.bound_pass) P.cnt[static_cast<size_t>(sub) * P.nq + q] = (over && !P.lenient) ? kOver : cnt;
     }
@@ -1050,7 +1081,7 @@ __device__ float exact_dist_avx512(const float* __restrict__ x, const float* q, 
 // inv[q] when inv is given).  Shared memory: the query (dim rounded up to 4)
 // and p2max keys.
 // After the bound pass: per query, an upper bound of the k-th smallest of
-// its half-tile minima -- each minimum is a different row's score, so k rows
+// its tile-part minima -- each minimum is a different row's score, so k rows
 // score at or below it, and the bound plus the margin bounds the k-th
 // distance over all rows -- published as the query's starting threshold
 // (gkey).  Two 8-bit radix passes over the order-preserving keys find the
@@ -1323,6 +1354,18 @@ void store_free(Store* s) {
   delete s;
 }
 
+cudaError_t open_mma_limits() {
+  cudaError_t e = open_smem_limit(reinterpret_cast<const void*>(bf_mma_kernel<8>));
+  return e == cudaSuccess ? open_smem_limit(reinterpret_cast<const void*>(bf_mma_kernel<16>)) : e;
+}
+
+cudaError_t launch_mma(bool wide, unsigned grid, const CUtensorMap& map_q, const CUtensorMap& map_x,
+                       const MmaParams& P, cudaStream_t st) {
+  if (wide) bf_mma_kernel<16><<<grid, Epi<16>::kThreads, kSmem, st>>>(map_q, map_x, P);
+  else bf_mma_kernel<8><<<grid, Epi<8>::kThreads, kSmem, st>>>(map_q, map_x, P);
+  return cudaGetLastError();
+}
+
 // Row splits of the scan (work items = query tiles x splits on a persistent
 // grid of one CTA per SM): from the count that gives one item per SM up to
 // four times it, the one with the shortest critical path, waves x (row tiles
@@ -1332,10 +1375,10 @@ void store_free(Store* s) {
 // thresholds, and the select kernel reads every split's candidates.  Fewest
 // splits on ties; the candidate buffers stay within 1 GiB.
 void choose_splits(uint32_t tiles_q, uint32_t nbt, uint32_t sms, uint32_t k, uint64_t bytes_per_split,
-                   uint32_t* splits_out, uint32_t* tps_out, bool seeded = false) {
-  const uint32_t s0 = std::min<uint32_t>(std::min<uint32_t>(nbt, kSelMaxSplits / 2),
+                   uint32_t* splits_out, uint32_t* tps_out, bool seeded, uint32_t parts) {
+  const uint32_t s0 = std::min<uint32_t>(std::min<uint32_t>(nbt, kSelMaxSplits / parts),
                                          std::max<uint32_t>(1, (sms + tiles_q - 1) / tiles_q));
-  uint32_t s_hi = std::min<uint32_t>(std::min<uint32_t>(nbt, kSelMaxSplits / 2), 4u * s0);  // 2 buffer sets per split
+  uint32_t s_hi = std::min<uint32_t>(std::min<uint32_t>(nbt, kSelMaxSplits / parts), 4u * s0);  // parts buffer sets per split
   while (s_hi > s0 && static_cast<uint64_t>(s_hi) * bytes_per_split > (1ull << 30)) --s_hi;
   // seeded thresholds (the bound pass) do not restart with each item
   const uint64_t overhead = seeded ? 16u : 64u + 2u * static_cast<uint64_t>(k);
@@ -1363,15 +1406,18 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
   const uint32_t nbt = s->n_pad / BN;
   const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
   uint32_t splits = 1, tps = nbt;
-  // the bound pass (the GEMM once more, keeping only each half tile's
+  // the bound pass (the GEMM once more, keeping only each tile part's
   // smallest score per query) seeds every query's threshold before the scan.
   // It pays where appends dominate -- large k over many queries (10k x 200k
   // rows at k = 100: 19% faster; at k = 10 and for few queries the second
   // GEMM costs more than it saves) -- while its minima fit 1 GiB.
-  const uint64_t mins_bytes = 2ull * nbt * nq_pad * 4;
+  const bool wide = tiles_q >= kWideEpiTiles;
+  const uint32_t parts = wide ? Epi<16>::kParts : Epi<8>::kParts;
+  const uint64_t mins_bytes = static_cast<uint64_t>(parts) * nbt * nq_pad * 4;
   const bool seeded = k >= 64 && nq_pad >= 2048 && mins_bytes <= (1ull << 30);
-  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, 2ull * nq_pad * cap * 8, &splits, &tps, seeded);
-  const uint32_t subs = 2 * splits;  // candidate buffers per query: one per (split, half tile)
+  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, static_cast<uint64_t>(parts) * nq_pad * cap * 8,
+                &splits, &tps, seeded, parts);
+  const uint32_t subs = parts * splits;  // candidate buffers per query: one per (split, tile part)
   const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(subs * cap, 32), 32));
   uint32_t p2max = 1;
   while (p2max < pool_cap) p2max <<= 1;
@@ -1432,8 +1478,7 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     P.tps = tps;
     P.l2 = r.metric == HGD_METRIC_L2 ? 1 : 0;
     what = "tensor kernel";
-    if ((e = open_smem_limit(reinterpret_cast<const void*>(bf_mma_kernel))) != cudaSuccess)
-      break;
+    if ((e = open_mma_limits()) != cudaSuccess) break;
     const uint32_t items = tiles_q * splits;
     const unsigned grid = std::min<uint32_t>(items, static_cast<uint32_t>(s->sms));
     if (seeded) {
@@ -1444,14 +1489,12 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
       B.bound_pass = 1;
       B.mins = sc.mins.as<float>();
       B.nq_pad = nq_pad;
-      bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, B);
-      if ((e = cudaGetLastError()) != cudaSuccess) break;
-      bound_select_kernel<<<nq_pad / 32, kBndThreads, 0, st>>>(B.mins, nq, nq_pad, 2 * nbt, k, qm, P.gkey);
+      if ((e = launch_mma(wide, grid, map_q, s->map_x, B, st)) != cudaSuccess) break;
+      bound_select_kernel<<<nq_pad / 32, kBndThreads, 0, st>>>(B.mins, nq, nq_pad, parts * nbt, k, qm, P.gkey);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
       what = "tensor kernel";
     }
-    bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);
-    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    if ((e = launch_mma(wide, grid, map_q, s->map_x, P, st)) != cudaSuccess) break;
     what = "select kernel";
     select_cta_kernel<<<nq, kSelThreads, 0, st>>>(buf, cnt, qm, qq, nq, subs, cap, k, pool, pool_cap, pool_n, derr,
                                                   0, nullptr, nullptr, nullptr);
@@ -1895,15 +1938,18 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
   const uint32_t nbt = s->n_pad / BN;
   const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
   uint32_t splits = 1, tps = nbt;
-  // the bound pass (the GEMM once more, keeping only each half tile's
+  // the bound pass (the GEMM once more, keeping only each tile part's
   // smallest score per query) seeds every query's threshold before the scan.
   // It pays where appends dominate -- large k over many queries (10k x 200k
   // rows at k = 100: 19% faster; at k = 10 and for few queries the second
   // GEMM costs more than it saves) -- while its minima fit 1 GiB.
-  const uint64_t mins_bytes = 2ull * nbt * nq_pad * 4;
+  const bool wide = tiles_q >= kWideEpiTiles;
+  const uint32_t parts = wide ? Epi<16>::kParts : Epi<8>::kParts;
+  const uint64_t mins_bytes = static_cast<uint64_t>(parts) * nbt * nq_pad * 4;
   const bool seeded = k >= 64 && nq_pad >= 2048 && mins_bytes <= (1ull << 30);
-  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, 2ull * nq_pad * cap * 8, &splits, &tps, seeded);
-  const uint32_t subs = 2 * splits;  // candidate buffers per query: one per (split, half tile)
+  choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, static_cast<uint64_t>(parts) * nq_pad * cap * 8,
+                &splits, &tps, seeded, parts);
+  const uint32_t subs = parts * splits;  // candidate buffers per query: one per (split, tile part)
   const uint32_t pool_cap = std::min<uint32_t>(kMaxPool, round_up(std::max<uint32_t>(subs * cap, 32), 32));
   uint32_t p2max = 1;
   while (p2max < pool_cap) p2max <<= 1;
@@ -1962,8 +2008,7 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     P.l2 = r.metric == HGD_METRIC_L2 ? 1 : 0;
     P.lenient = 1;
     what = "tensor kernel";
-    if ((e = open_smem_limit(reinterpret_cast<const void*>(bf_mma_kernel))) != cudaSuccess)
-      break;
+    if ((e = open_mma_limits()) != cudaSuccess) break;
     const unsigned grid = std::min<uint32_t>(tiles_q * splits, static_cast<uint32_t>(s->sms));
     if (seeded) {
       // k_stride bounds every routed query's k: its bound is safe for each
@@ -1974,14 +2019,12 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
       B.bound_pass = 1;
       B.mins = sc->mins.as<float>();
       B.nq_pad = nq_pad;
-      bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, B);
-      if ((e = cudaGetLastError()) != cudaSuccess) break;
-      bound_select_kernel<<<nq_pad / 32, kBndThreads, 0, st>>>(B.mins, n_r, nq_pad, 2 * nbt, k, P.qm, P.gkey);
+      if ((e = launch_mma(wide, grid, map_q, s->map_x, B, st)) != cudaSuccess) break;
+      bound_select_kernel<<<nq_pad / 32, kBndThreads, 0, st>>>(B.mins, n_r, nq_pad, parts * nbt, k, P.qm, P.gkey);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
       what = "tensor kernel";
     }
-    bf_mma_kernel<<<grid, kThreads, kSmem, st>>>(map_q, s->map_x, P);
-    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    if ((e = launch_mma(wide, grid, map_q, s->map_x, P, st)) != cudaSuccess) break;
     what = "select kernel";
     select_cta_kernel<<<n_r, kSelThreads, 0, st>>>(sc->buf.as<uint64_t>(), sc->cnt.as<uint32_t>(), sc->qm.as<float>(),
                                                    sc->qq.as<float>(), n_r, subs, cap, k, sc->pool.as<uint32_t>(),
