@@ -96,7 +96,8 @@ struct MmaParams {
   // key bits, 0xFFFFFFFF none), shared by all splits of the query
   uint32_t* gkey;
   uint32_t n, nq, kchunks, cap, k, nbt, tiles_q, splits, tps;
-  uint32_t trig;  // a lane's buffer is compacted once it could pass trig - 32 keys (<= cap)
+  uint32_t trig;   // a lane's buffer is compacted once it could pass trig - 32 keys (<= cap)
+  uint32_t trig0;  // the same for a sub-split's first compaction (its threshold starts at +inf)
   int l2;
   int lenient;  // keep the buffer of a query whose candidates overflow (approximate answer) instead of failing
   // bound pass: keep nothing; write each (tile part, query)'s smallest score
@@ -104,6 +105,7 @@ struct MmaParams {
   int bound_pass;
   float* mins;
   uint32_t nq_pad;
+  uint32_t tstep;  // row tiles taken: those with bt % tstep == 0 (the bound pass samples; 1 = all)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -245,8 +247,9 @@ __device__ __forceinline__ float dist_of_key_bits(uint32_t kb) {
 }
 
 // The warp compacts the candidate buffer of one of its lanes: a bound T with
-// at least k and at most k + 32 keys of b[0..cnt) at or below it (or the
-// exact k-th smallest, if the key bits allow no such bound) is found by
+// at least k and at most k + 32 keys of b[0..cnt) at or below it (at most k,
+// i.e. the k-th smallest, when cnt <= 64; the exact k-th smallest, if the
+// key bits allow no such bound) is found by
 // bisection on the order-preserving key bits, then the keys within T + margin
 // are kept.  The buffer (cnt <= 2 * kMaxK + 64) is held in registers, up to 18
 // keys per lane; only the ceil(cnt / 32) register slots that hold keys are
@@ -273,7 +276,10 @@ __device__ __noinline__ uint32_t warp_compact(uint64_t* b, uint32_t cnt, uint32_
   lo = __reduce_min_sync(kFull, lo);
   hi = __reduce_max_sync(kFull, hi);
   uint32_t chi = cnt;  // keys at or below hi
-  while (lo < hi && chi > k + 32u) {
+  // a bound with up to k + 32 keys under it is good enough for a large
+  // buffer; a small one (a first compaction) is cheap to cut to the k-th
+  const uint32_t slack = cnt <= 64u ? 0u : 32u;
+  while (lo < hi && chi > k + slack) {
     const uint32_t mid = lo + ((hi - lo) >> 1);
     uint32_t c = 0;
 #pragma unroll
@@ -358,7 +364,7 @@ __global__ void __launch_bounds__(Epi<EPI>::kThreads, 1)
       for (uint32_t item = blockIdx.x; ok && item < items; item += gridDim.x) {
         const uint32_t qt = item % P.tiles_q, sp = item / P.tiles_q;
         const uint32_t b0 = sp * P.tps, b1 = min(P.nbt, b0 + P.tps);
-        for (uint32_t bt = b0; ok && bt < b1; ++bt) {
+        for (uint32_t bt = (b0 + P.tstep - 1) / P.tstep * P.tstep; ok && bt < b1; bt += P.tstep) {
           for (uint32_t kc = 0; kc < P.kchunks; ++kc) {
             if (!mbar_wait(empty(stage), phase ^ 1u, &abort_flag, P.err)) {
               ok = false;
@@ -392,7 +398,7 @@ __global__ void __launch_bounds__(Epi<EPI>::kThreads, 1)
       for (uint32_t item = blockIdx.x; ok && item < items; item += gridDim.x) {
         const uint32_t sp = item / P.tiles_q;
         const uint32_t b0 = sp * P.tps, b1 = min(P.nbt, b0 + P.tps);
-        for (uint32_t bt = b0; ok && bt < b1; ++bt, ++acc_i) {
+        for (uint32_t bt = (b0 + P.tstep - 1) / P.tstep * P.tstep; ok && bt < b1; bt += P.tstep, ++acc_i) {
           const uint32_t ab = acc_i & 1u, aph = (acc_i >> 1) & 1u;
           if (!mbar_wait(tempty(ab), aph ^ 1u, &abort_flag, P.err)) {
             ok = false;
@@ -448,15 +454,15 @@ __global__ void __launch_bounds__(Epi<EPI>::kThreads, 1)
       const uint32_t sub = kParts * sp + part;
       uint64_t* bufp = P.buf + (static_cast<size_t>(sub) * P.nq + (live_q ? q : 0)) * P.cap;
       uint32_t cnt = 0;
-      uint32_t lim = P.trig;  // compaction point: the threshold tightens early
+      uint32_t lim = P.trig0;  // compaction point: the threshold tightens early
       // the bound pass keeps no row: no score is at or below -inf
       float thr = P.bound_pass ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
       bool over = false;
-      for (uint32_t bt = b0; bt < b1; ++bt, ++acc_i) {
+      for (uint32_t bt = (b0 + P.tstep - 1) / P.tstep * P.tstep; bt < b1; bt += P.tstep, ++acc_i) {
         const uint32_t ab = acc_i & 1u, aph = (acc_i >> 1) & 1u;
         float tmin = __int_as_float(0x7f800000);  // bound pass: the part's smallest score
-        if (bt + 1 < b1 && lane < static_cast<int>(kPartCols / 32))  // the next tile's row norms of this part into L1
-          asm volatile("prefetch.global.L1 [%0];" ::"l"(P.xn + (bt + 1) * BN + part * kPartCols + lane * 32u));
+        if (bt + P.tstep < b1 && lane < static_cast<int>(kPartCols / 32))  // the next tile's row norms of this part into L1
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(P.xn + (bt + P.tstep) * BN + part * kPartCols + lane * 32u));
         // the bound of the other splits of this query (a split's k-th
         // smallest + the margin bounds the k-th over all rows from above)
         if (live_q && !over && !P.bound_pass) {
@@ -592,7 +598,8 @@ __global__ void __launch_bounds__(Epi<EPI>::kThreads, 1)
         __syncwarp();
         tc_fence_before();
         if (lane == 0) mbar_arrive(tempty(ab));
-        if (P.bound_pass) P.mins[(static_cast<uint64_t>(kParts) * bt + part) * P.nq_pad + qt * BM + row_in_tile] = tmin;
+        if (P.bound_pass)
+          P.mins[(static_cast<uint64_t>(kParts) * (bt / P.tstep) + part) * P.nq_pad + qt * BM + row_in_tile] = tmin;
       }
       if (ok && live_q && !P.bound_pass) P.cnt[static_cast<size_t>(sub) * P.nq + q] = (over && !P.lenient) ? kOver : cnt;
     }
@@ -1354,6 +1361,19 @@ void store_free(Store* s) {
   delete s;
 }
 
+// Row-tile step of the bound pass: the largest power of two that still
+// samples about 96 row tiles (192 for k >= 64) and at least 4k tile-part
+// minima per query.  Measured on 200k and 1M rows: 8 and 32 at k = 10, 4 and
+// 8-16 at k = 100 (host calls within 5% of the best step).
+uint32_t bound_step(uint32_t nbt, uint32_t k, uint32_t parts) {
+  const uint32_t want = k >= 64 ? 192u : 96u;
+  uint32_t step = 1;
+  while (step < 1024u && nbt / (2 * step) >= want &&
+         static_cast<uint64_t>(parts) * (nbt / (2 * step)) >= 4ull * k)
+    step *= 2;
+  return step;
+}
+
 cudaError_t open_mma_limits() {
   cudaError_t e = open_smem_limit(reinterpret_cast<const void*>(bf_mma_kernel<8>));
   return e == cudaSuccess ? open_smem_limit(reinterpret_cast<const void*>(bf_mma_kernel<16>)) : e;
@@ -1406,15 +1426,18 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
   const uint32_t nbt = s->n_pad / BN;
   const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
   uint32_t splits = 1, tps = nbt;
-  // the bound pass (the GEMM once more, keeping only each tile part's
-  // smallest score per query) seeds every query's threshold before the scan.
-  // It pays where appends dominate -- large k over many queries (10k x 200k
-  // rows at k = 100: 19% faster; at k = 10 and for few queries the second
-  // GEMM costs more than it saves) -- while its minima fit 1 GiB.
+  // the bound pass (the GEMM over every tstep-th row tile, keeping only each
+  // tile part's smallest score per query) seeds every query's threshold
+  // before the scan, for batches of many query tiles while its minima fit
+  // 1 GiB (10k x 200k rows, k = 10: 2.20 -> 1.51 ms per call; 4,096 x 1M:
+  // 2.49 -> 1.93 ms; for few queries a second launch costs more than it
+  // saves).
   const bool wide = tiles_q >= kWideEpiTiles;
   const uint32_t parts = wide ? Epi<16>::kParts : Epi<8>::kParts;
-  const uint64_t mins_bytes = static_cast<uint64_t>(parts) * nbt * nq_pad * 4;
-  const bool seeded = k >= 64 && nq_pad >= 2048 && mins_bytes <= (1ull << 30);
+  const uint32_t tstep = bound_step(nbt, k, parts);
+  const uint32_t nbt_s = (nbt + tstep - 1) / tstep;  // row tiles the bound pass samples
+  const uint64_t mins_bytes = static_cast<uint64_t>(parts) * nbt_s * nq_pad * 4;
+  const bool seeded = wide && (tstep > 1 || k >= 64) && mins_bytes <= (1ull << 30);
   choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, static_cast<uint64_t>(parts) * nq_pad * cap * 8,
                 &splits, &tps, seeded, parts);
   const uint32_t subs = parts * splits;  // candidate buffers per query: one per (split, tile part)
@@ -1471,6 +1494,10 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
     P.kchunks = s->kp / BK;
     P.cap = cap;
     P.trig = std::min<uint32_t>(cap, std::max<uint32_t>(96, round_up(2 * k + 64, 32)));
+    // a small k compacts first after one appended chunk: every sub-split's
+    // threshold starts at +inf, so its first rows all pass
+    P.trig0 = k <= 31 ? 63u : P.trig;
+    P.tstep = 1;
     P.k = k;
     P.nbt = nbt;
     P.tiles_q = tiles_q;
@@ -1489,8 +1516,9 @@ cudaError_t search(Store* s, const Rows& r, const float* queries, const float* i
       B.bound_pass = 1;
       B.mins = sc.mins.as<float>();
       B.nq_pad = nq_pad;
+      B.tstep = tstep;
       if ((e = launch_mma(wide, grid, map_q, s->map_x, B, st)) != cudaSuccess) break;
-      bound_select_kernel<<<nq_pad / 32, kBndThreads, 0, st>>>(B.mins, nq, nq_pad, parts * nbt, k, qm, P.gkey);
+      bound_select_kernel<<<nq_pad / 32, kBndThreads, 0, st>>>(B.mins, nq, nq_pad, parts * nbt_s, k, qm, P.gkey);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
       what = "tensor kernel";
     }
@@ -1938,15 +1966,18 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
   const uint32_t nbt = s->n_pad / BN;
   const uint32_t cap = std::max<uint32_t>(256, round_up(2 * k + 64, 32));
   uint32_t splits = 1, tps = nbt;
-  // the bound pass (the GEMM once more, keeping only each tile part's
-  // smallest score per query) seeds every query's threshold before the scan.
-  // It pays where appends dominate -- large k over many queries (10k x 200k
-  // rows at k = 100: 19% faster; at k = 10 and for few queries the second
-  // GEMM costs more than it saves) -- while its minima fit 1 GiB.
+  // the bound pass (the GEMM over every tstep-th row tile, keeping only each
+  // tile part's smallest score per query) seeds every query's threshold
+  // before the scan, for batches of many query tiles while its minima fit
+  // 1 GiB (10k x 200k rows, k = 10: 2.20 -> 1.51 ms per call; 4,096 x 1M:
+  // 2.49 -> 1.93 ms; for few queries a second launch costs more than it
+  // saves).
   const bool wide = tiles_q >= kWideEpiTiles;
   const uint32_t parts = wide ? Epi<16>::kParts : Epi<8>::kParts;
-  const uint64_t mins_bytes = static_cast<uint64_t>(parts) * nbt * nq_pad * 4;
-  const bool seeded = k >= 64 && nq_pad >= 2048 && mins_bytes <= (1ull << 30);
+  const uint32_t tstep = bound_step(nbt, k, parts);
+  const uint32_t nbt_s = (nbt + tstep - 1) / tstep;  // row tiles the bound pass samples
+  const uint64_t mins_bytes = static_cast<uint64_t>(parts) * nbt_s * nq_pad * 4;
+  const bool seeded = wide && (tstep > 1 || k >= 64) && mins_bytes <= (1ull << 30);
   choose_splits(tiles_q, nbt, static_cast<uint32_t>(s->sms), k, static_cast<uint64_t>(parts) * nq_pad * cap * 8,
                 &splits, &tps, seeded, parts);
   const uint32_t subs = parts * splits;  // candidate buffers per query: one per (split, tile part)
@@ -2000,6 +2031,10 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
     P.kchunks = s->kp / BK;
     P.cap = cap;
     P.trig = std::min<uint32_t>(cap, std::max<uint32_t>(96, round_up(2 * k + 64, 32)));
+    // a small k compacts first after one appended chunk: every sub-split's
+    // threshold starts at +inf, so its first rows all pass
+    P.trig0 = k <= 31 ? 63u : P.trig;
+    P.tstep = 1;
     P.k = k;
     P.nbt = nbt;
     P.tiles_q = tiles_q;
@@ -2019,8 +2054,9 @@ cudaError_t search_routed(Store* s, const Rows& r, const RoutedArgs& a, Scratch*
       B.bound_pass = 1;
       B.mins = sc->mins.as<float>();
       B.nq_pad = nq_pad;
+      B.tstep = tstep;
       if ((e = launch_mma(wide, grid, map_q, s->map_x, B, st)) != cudaSuccess) break;
-      bound_select_kernel<<<nq_pad / 32, kBndThreads, 0, st>>>(B.mins, n_r, nq_pad, parts * nbt, k, P.qm, P.gkey);
+      bound_select_kernel<<<nq_pad / 32, kBndThreads, 0, st>>>(B.mins, n_r, nq_pad, parts * nbt_s, k, P.qm, P.gkey);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
       what = "tensor kernel";
     }
