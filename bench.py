@@ -553,6 +553,15 @@ def run_batched_200k(local, use_graph=True):
     bf = hnswgpu.BruteForceIndex(HEAD_DIM, "l2")
     bf.add(base)
     gt = bf.search_raw(queries, HEAD_K)["label"].astype(np.int64)
+    # the tensor-core brute force itself: host calls (copies, bound pass,
+    # scan, select and exact rerank), median of 5
+    bf_ms = []
+    for _ in range(5):
+        t = time.perf_counter()
+        bf.search_raw(queries, HEAD_K)
+        bf_ms.append((time.perf_counter() - t) * 1e3)
+    bf_ms = statistics.median(bf_ms)
+    bf_path = bf.last_path
     del bf
     threads = os.cpu_count() or 1
     rx = refcore.RefIndex(gpath)
@@ -572,7 +581,11 @@ def run_batched_200k(local, use_graph=True):
             "noalloc": {**noalloc, "ef": 80, "note": "device-resident batch; the allocation-free call runs on a "
                                                       "fixed 48 warps"},
             "reference": f"search_batch per ef group, {threads} threads, simd {refcore.isa()}",
-            "parity_vs_reference": {"queries": B2_NQ, **parity(gpu, ref)}}
+            "parity_vs_reference": {"queries": B2_NQ, **parity(gpu, ref)},
+            "bruteforce": {"what": f"exact k-NN of the {B2_NQ} queries over the {B2_N} rows, k={HEAD_K}, one host "
+                                   f"call (copies included), median of 5",
+                           "ms": round(bf_ms, 3), "path": "tensor cores" if bf_path == 2 else "CUDA-core scan",
+                           "tflops_effective": round(2.0 * B2_NQ * B2_N * HEAD_DIM / (bf_ms / 1e3) / 1e12, 1)}}
 
 
 # ---------------------------------------------------------------------------
