@@ -32,7 +32,7 @@ class _OracleIndex:
 
     def search_batch_ex(self, q, k, ef_per_query=None, k_per_query=None):
         labels, dists = self.ox.search_batch(q, k, 0, ef_per_query=ef_per_query, k_per_query=k_per_query)
-        rec = np.zeros(labels.shape, dtype=[("label", "<u8"), ("distance", "<f4"), ("pad", "<u4")])
+        rec = np.zeros(labels.shape, dtype=[("label", "<u8"), ("distance", "<f4"), ("reserved", "<u4")])
         rec["label"], rec["distance"] = labels, dists
         return rec
 
