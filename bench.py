@@ -421,23 +421,30 @@ def run_build(ix_ref, base, sample, gt, ref_s, ref_how):
     import hnswgpu
     import workloads
 
-    g = hnswgpu.Index(HEAD_DIM, "l2", M, EFC)
-    t = time.perf_counter()
-    st = g.add_gpu(base)
-    wall = time.perf_counter() - t
+    def build(**kw):
+        g = hnswgpu.Index(HEAD_DIM, "l2", M, EFC)
+        t = time.perf_counter()
+        st = g.add_gpu(base, **kw)
+        return g, time.perf_counter() - t, st
+
+    g, wall, st = build()
+    gp, wall_p, st_p = build(wave_fraction=0.1, peers=True)
     rows = []
     for ef in (16, 32, 48, 96):
         r_ref = workloads.recall_at_k(ix_ref.search_raw(sample, HEAD_K, ef)["label"].astype(np.int64), gt)
         r_gpu = workloads.recall_at_k(g.search_raw(sample, HEAD_K, ef)["label"].astype(np.int64), gt)
+        r_peer = workloads.recall_at_k(gp.search_raw(sample, HEAD_K, ef)["label"].astype(np.int64), gt)
         rows.append({"ef": ef, "recall_at_10_reference_graph": round(r_ref, 4),
-                     "recall_at_10_gpu_graph": round(r_gpu, 4)})
-    del g
+                     "recall_at_10_gpu_graph": round(r_gpu, 4), "recall_at_10_gpu_graph_peers": round(r_peer, 4)})
+    del g, gp
     return {"workload": f"the headline rows: n={HEAD_N} d={HEAD_DIM} M={M} efC={EFC}",
             "gpu_add_batch_s": round(wall, 3), "gpu_linking_s": round(st["seconds"], 3), "waves": st["waves"],
             "dropped_proposals": st["dropped_proposals"],
+            "gpu_peers": {"options": "wave_fraction 0.1, peer linking", "add_batch_s": round(wall_p, 3),
+                          "linking_s": round(st_p["seconds"], 3), "waves": st_p["waves"]},
             "reference_add_batch_s": round(ref_s, 2) if ref_how == "built" else None,
             "reference_threads": os.cpu_count(),
-            "note": "gpu_add_batch_s covers the host store, the upload, the linking and the download; "
+            "note": "add_batch_s covers the host store, the upload, the linking and the download; "
                     "recall of the plain walk, ground truth exact k-NN",
             "recall": rows}
 

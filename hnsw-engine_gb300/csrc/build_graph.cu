@@ -449,6 +449,104 @@ __global__ void __launch_bounds__(32 * kWarps) insert_kernel(BuildParams P, uint
 }
 
 // ---------------------------------------------------------------------------
+// 1b. peers: new nodes of the wave that chose the same old neighbours
+// ---------------------------------------------------------------------------
+// A new node did not see the other new nodes of its wave while it searched.
+// The proposals in its chosen neighbours' inboxes name exactly the new nodes
+// that chose the same neighbours -- the wave's nodes nearest to it.  Each
+// new node re-chooses its own list by Alg. 4 from its neighbours plus those
+// peers (up to kPeerCap of them) and proposes itself to the peers it keeps,
+// so the reverse-edge merge links the wave's nodes to each other as a
+// sequential build would.  This lets waves be larger at the same recall.
+constexpr int kPeerCap = 96;  // peers considered per (node, layer); with M <= 32 own ids, 128 keys
+
+__host__ __device__ inline uint32_t peer_warp_bytes(uint32_t pd) {
+  // row | keys + two merge buffers (128 each) | ids | distances | kept ids, distances
+  return 4u * pd + 24u * 128u + 4u * 128u + 4u * 128u + 8u * kMaxDegree;
+}
+
+template <bool L2>
+__global__ void __launch_bounds__(32 * kWarps) peer_kernel(BuildParams P, uint32_t a, uint32_t b, int top) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const uint32_t node = a + blockIdx.x * kWarps + static_cast<uint32_t>(wib);
+  if (node >= b) return;
+  unsigned char* base = smem + static_cast<size_t>(wib) * peer_warp_bytes(P.pd);
+  float* row = reinterpret_cast<float*>(base);
+  uint64_t* ka = reinterpret_cast<uint64_t*>(base + 4u * P.pd);
+  uint64_t* kb = ka + 128;
+  uint64_t* kc = kb + 128;
+  uint32_t* ids = reinterpret_cast<uint32_t*>(kc + 128);
+  float* dist = reinterpret_cast<float*>(ids + 128);
+  uint32_t* kid = reinterpret_cast<uint32_t*>(dist + 128);
+  float* kd = reinterpret_cast<float*>(kid + kMaxDegree);
+  {
+    const float4* src = reinterpret_cast<const float4*>(P.vecs + static_cast<size_t>(node) * P.pd);
+    float4* dst = reinterpret_cast<float4*>(row);
+    for (uint32_t f = lane; f < (P.pd >> 2); f += 32) dst[f] = __ldg(src + f);
+  }
+  __syncwarp();
+  const int level = P.levels[node];
+  for (int lc = min(level, top); lc >= 0; --lc) {
+    uint32_t* own = list_of(P, node, lc);
+    const int nk = static_cast<int>(min(own[0], P.M));
+    // the peers: every proposer in the own neighbours' inboxes but this node
+    int np = 0;
+    for (int j = 0; j < nk && np < kPeerCap; ++j) {
+      const uint32_t s = slot_of(P, own[1 + j], lc);
+      const int cnt = static_cast<int>(min(P.inbox_n[s], kInboxCap));
+      for (int t0 = 0; t0 < cnt && np < kPeerCap; t0 += 32) {
+        const int t = t0 + lane;
+        uint32_t pid = kNoId;
+        if (t < cnt) pid = static_cast<uint32_t>(P.inbox[static_cast<size_t>(s) * kInboxCap + t]);
+        const bool take = pid != kNoId && pid != node;
+        const uint32_t bal = __ballot_sync(kFull, take);
+        const int at = np + __popc(bal & ((1u << lane) - 1u));
+        // (peer << 32 | position): unique keys for the sort, peers adjacent
+        if (take && at < kPeerCap) ka[at] = (static_cast<uint64_t>(pid) << 32) | static_cast<uint32_t>(at);
+        np = min(kPeerCap, np + __popc(bal));
+      }
+    }
+    __syncwarp();
+    if (np == 0) continue;
+    // unique peers (a peer may have chosen several of the same neighbours)
+    const uint64_t* sorted = sort_small(ka, kb, kc, np, lane);
+    int nu = 0;
+    for (int b0 = 0; b0 < np; b0 += 32) {
+      const int i = b0 + lane;
+      const bool first = i < np && (i == 0 || (sorted[i] >> 32) != (sorted[i - 1] >> 32));
+      const uint32_t bal = __ballot_sync(kFull, first);
+      if (first) ids[nu + __popc(bal & ((1u << lane) - 1u))] = static_cast<uint32_t>(sorted[i] >> 32);
+      nu += __popc(bal);
+    }
+    for (int j = lane; j < nk; j += 32) ids[nu + j] = own[1 + j];
+    __syncwarp();
+    const int nc = nu + nk;
+    row_dists<L2>(P, row, ids, nc, dist, lane);
+    for (int j = lane; j < nc; j += 32) ka[j] = sk::mkkey(dist[j], ids[j]);
+    __syncwarp();
+    const uint64_t* cand = sort_small(ka, kb, kc, nc, lane);
+    const int nkept = select_neighbours<L2, 0>(P, cand, nc, static_cast<int>(P.M), kid, kd, lane);
+    for (int j = lane; j < nkept; j += 32) own[1 + j] = kid[j];
+    __syncwarp();
+    if (lane == 0) own[0] = static_cast<uint32_t>(nkept);
+    // proposals to the kept peers (new nodes of this wave); the old
+    // neighbours hold this node's proposal already
+    for (int j = lane; j < nkept; j += 32) {
+      const uint32_t t = kid[j];
+      if (t < a || t >= b) continue;
+      const uint32_t sl = slot_of(P, t, lc);
+      const uint32_t pos = atomicAdd(P.inbox_n + sl, 1u);
+      if (pos == 0) P.touched[atomicAdd(P.touched_n, 1u)] = sl;
+      if (pos < kInboxCap) P.inbox[static_cast<size_t>(sl) * kInboxCap + pos] = sk::mkkey(kd[j], node);
+      else atomicAdd(P.dropped, 1ull);
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // 2. merge the proposals of each touched (node, layer) into its list
 // ---------------------------------------------------------------------------
 template <bool L2>
@@ -682,8 +780,12 @@ int build_graph(hgd_build_args* a, int device, std::string* err) {
   const size_t link_smem = static_cast<size_t>(kWarps) * link_warp_bytes(pd);
   auto* ins = P.l2 ? insert_kernel<true> : insert_kernel<false>;
   auto* lnk = P.l2 ? link_kernel<true> : link_kernel<false>;
+  auto* peer = P.l2 ? peer_kernel<true> : peer_kernel<false>;
+  const size_t peer_smem = static_cast<size_t>(kWarps) * peer_warp_bytes(pd);
+  const bool peers = a->peers != 0;
   if ((e = open_smem_limit(reinterpret_cast<const void*>(ins))) != cudaSuccess ||
-      (e = open_smem_limit(reinterpret_cast<const void*>(lnk))) != cudaSuccess)
+      (e = open_smem_limit(reinterpret_cast<const void*>(lnk))) != cudaSuccess ||
+      (e = open_smem_limit(reinterpret_cast<const void*>(peer))) != cudaSuccess)
     return bad(HGD_ECUDA, cudaGetErrorString(e));
   int link_blocks = 0;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&link_blocks, lnk, 32 * kWarps, link_smem)) != cudaSuccess)
@@ -697,7 +799,9 @@ int build_graph(hgd_build_args* a, int device, std::string* err) {
   // waves: [a, b) joins the graph of nodes [0, a)
   const double frac = a->wave_fraction > 0.0 ? a->wave_fraction : 0.02;
   const uint64_t wmin = a->wave_min ? a->wave_min : 1;
-  const uint64_t wmax = a->wave_max ? a->wave_max : static_cast<uint64_t>(ins_blocks) * sms * kWarps * 4;
+  // largest wave: four (peer linking: sixteen) rounds of the resident warps
+  const uint64_t wmax =
+      a->wave_max ? a->wave_max : static_cast<uint64_t>(ins_blocks) * sms * kWarps * (a->peers ? 16 : 4);
   uint32_t entry = a->entry_point;
   int top = a->max_level;
   uint32_t at = first;
@@ -712,6 +816,7 @@ int build_graph(hgd_build_args* a, int device, std::string* err) {
     const uint32_t b = static_cast<uint32_t>(std::min<uint64_t>(at + w, count));
     const uint32_t blocks = (b - at + kWarps - 1) / kWarps;
     ins<<<blocks, 32 * kWarps, ins_smem, st>>>(P, at, b, entry, top);
+    if (peers && b - at > 1) peer<<<blocks, 32 * kWarps, peer_smem, st>>>(P, at, b, top);
     lnk<<<link_blocks, 32 * kWarps, link_smem, st>>>(P);
     if ((e = cudaMemsetAsync(d_small, 0, 4, st)) != cudaSuccess) return bad(HGD_ECUDA, cudaGetErrorString(e));
     if ((e = cudaGetLastError()) != cudaSuccess) return bad(HGD_ECUDA, std::string("launch: ") + cudaGetErrorString(e));

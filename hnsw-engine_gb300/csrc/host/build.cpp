@@ -344,6 +344,7 @@ GpuBuildStats insert_batch_gpu(Index::Impl& g, const float* vecs, const uint64_t
   a.wave_min = opt.wave_min;
   a.wave_max = opt.wave_max;
   a.wave_fraction = opt.wave_fraction;
+  a.peers = opt.peers ? 1 : 0;
   a.vectors = g.vecs;
   a.level0 = g.l0;
   a.upper = g.upper;

@@ -152,6 +152,7 @@ int hg_index_add_batch_gpu(hg_index* idx, const float* vecs, const uint64_t* lab
       o.wave_fraction = opt->wave_fraction;
       o.wave_min = opt->wave_min;
       o.wave_max = opt->wave_max;
+      o.peers = opt->peers != 0;
     }
     const hnsw::GpuBuildStats st = idx->index.add_batch_gpu(vecs, labels, n, o);
     if (opt) {

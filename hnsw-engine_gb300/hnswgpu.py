@@ -59,7 +59,8 @@ class _Request(C.Structure):
 
 class _BuildOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("wave_min", C.c_uint32), ("wave_max", C.c_uint32), ("waves", C.c_uint32),
-                ("wave_fraction", C.c_double), ("dropped_proposals", C.c_uint64), ("seconds", C.c_double)]
+                ("wave_fraction", C.c_double), ("dropped_proposals", C.c_uint64), ("seconds", C.c_double),
+                ("peers", C.c_int32), ("reserved", C.c_int32)]
 
 
 class _ServerStats(C.Structure):
@@ -329,7 +330,7 @@ class Index:
         _check(lib().hg_index_add_batch(self._h, _ptr(v), _ptr(labels), v.shape[0], num_threads))
 
     def add_gpu(self, vectors, ids=None, device: int = -1, wave_fraction: float = 0.0, wave_min: int = 0,
-                wave_max: int = 0) -> dict:
+                wave_max: int = 0, peers: bool = False) -> dict:
         """add with the graph linking on the GPU (no counterpart in the
         reference): same validation, stored rows, labels and levels as add;
         the graph is judged on recall, not identity.  Returns the waves
@@ -341,7 +342,7 @@ class Index:
             raise ValueError(f"vectors: expected shape (n, {self.dim})")
         labels = _to_labels(ids, v.shape[0], len(self))
         o = _BuildOptions(device=int(device), wave_min=int(wave_min), wave_max=int(wave_max),
-                          wave_fraction=float(wave_fraction))
+                          wave_fraction=float(wave_fraction), peers=1 if peers else 0)
         _check(lib().hg_index_add_batch_gpu(self._h, _ptr(v), _ptr(labels), v.shape[0], C.byref(o)))
         return {"waves": int(o.waves), "dropped_proposals": int(o.dropped_proposals), "seconds": float(o.seconds)}
 

@@ -81,7 +81,10 @@ struct GpuBuildOptions {
   int device = -1;             ///< CUDA device; -1 = the index's (set_device)
   double wave_fraction = 0.0;  ///< 0 = 0.02
   uint32_t wave_min = 0;       ///< 0 = 1
-  uint32_t wave_max = 0;       ///< 0 = four times the warps the GPU keeps resident
+  uint32_t wave_max = 0;       ///< 0 = four (peers: sixteen) times the warps the GPU keeps resident
+  /// each new node re-chooses its list among the nodes of its wave that
+  /// chose the same neighbours (links a wave's nodes to each other)
+  bool peers = false;
 };
 struct GpuBuildStats {
   uint32_t waves = 0;                ///< kernel waves launched

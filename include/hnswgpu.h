@@ -132,11 +132,14 @@ int hg_index_add_batch(hg_index* idx, const float* vecs, const uint64_t* labels,
 typedef struct {
   int32_t device;              /* CUDA device, -1 = the index's */
   uint32_t wave_min;           /* smallest wave, 0 = 1 */
-  uint32_t wave_max;           /* largest wave, 0 = four times the resident warps */
+  uint32_t wave_max;           /* largest wave, 0 = four (peers: sixteen) times the resident warps */
   uint32_t waves;              /* out */
   double wave_fraction;        /* new nodes per wave / nodes already linked, 0 = 0.02 */
   uint64_t dropped_proposals;  /* out */
   double seconds;              /* out: wall time of the GPU linking */
+  int32_t peers;               /* 1: each new node re-chooses its list among its wave's nodes that
+                                  chose the same neighbours (larger waves at equal recall) */
+  int32_t reserved;
 } hg_build_options;
 int hg_index_add_batch_gpu(hg_index* idx, const float* vecs, const uint64_t* labels, size_t n,
                            hg_build_options* opt);

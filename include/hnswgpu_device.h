@@ -229,7 +229,7 @@ typedef struct {
   int32_t max_level;            /* in/out: top level of the graph (-1: empty) */
   uint32_t entry_point;         /* in/out: 0xFFFFFFFF for an empty graph */
   uint32_t wave_min;            /* smallest wave (0: 1) */
-  uint32_t wave_max;            /* largest wave (0: four times the resident warps) */
+  uint32_t wave_max;            /* largest wave (0: four times the resident warps, sixteen with peers) */
   uint32_t waves;               /* out: waves launched */
   double wave_fraction;         /* new nodes per wave / nodes already linked (0: 0.02) */
   const float* vectors;         /* count x padded_dim (host) */
@@ -239,6 +239,9 @@ typedef struct {
   const uint64_t* upper_offset; /* count: word offset of a node's level-1 block */
   const uint8_t* levels;        /* count */
   uint64_t dropped_proposals;   /* out: reverse edges beyond a list's per-wave inbox (64) */
+  int32_t peers;                /* 1: each new node re-chooses its list among its wave's nodes that
+                                   chose the same neighbours (larger waves at equal recall) */
+  int32_t reserved;
 } hgd_build_args;
 int hgd_build_graph(hgd_build_args* args, int device);
 
