@@ -297,8 +297,8 @@ __global__ void __launch_bounds__(128, 6) beam_kernel(SearchParams P, const floa
   uint64_t* const resA = beamB + P.R;                 // FILT only
   uint64_t* const resB = resA + P.R;                  // FILT only
   uint64_t* const stage = FILT ? resB + P.R : resA;  // accepted keys
-  uint64_t* const est = stage + 32 * kBeamMaxE;       // eligible accepted keys (FILT)
-  uint32_t* const fid = reinterpret_cast<uint32_t*>(est + 32 * kBeamMaxE);
+  uint64_t* const est = stage + 32 * kBeamMaxE;       // eligible accepted keys (FILT only)
+  uint32_t* const fid = reinterpret_cast<uint32_t*>((FILT ? est : stage) + 32 * kBeamMaxE);
   float* const fdist = reinterpret_cast<float*>(fid + 32 * kBeamMaxE);
   for (uint32_t i = lane; i < P.H; i += 32) hash[i] = 0u;  // epoch 0: every slot free
   __syncwarp();

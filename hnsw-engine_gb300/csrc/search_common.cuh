@@ -95,11 +95,11 @@ struct BucketSpec {
 
 // The beam walk (search_beam.cuh): lists per step at most, and its per-warp
 // shared layout: hash[H] | beam A, B [R each] | (filtered) results A, B
-// [R each] | stage, eligible stage [32 E each] | fresh ids [32 E] | fresh
-// distances [32 E] (also the query staging area: 128 floats).
+// [R each] | stage [32 E] | (filtered) eligible stage [32 E] | fresh ids
+// [32 E] | fresh distances [32 E] (also the query staging area: 128 floats).
 constexpr int kBeamMaxE = 4;
 __host__ __device__ inline uint32_t beam_warp_bytes(uint32_t H, uint32_t R, bool filt) {
-  return 4u * H + 16u * R + (filt ? 16u * R : 0u) + 2u * 8u * 32u * kBeamMaxE + 8u * 32u * kBeamMaxE;
+  return 4u * H + 16u * R + (filt ? 16u * R : 0u) + (filt ? 2u : 1u) * 8u * 32u * kBeamMaxE + 8u * 32u * kBeamMaxE;
 }
 // A query's visited-hash size in the beam walk: the smallest power of two
 // >= 1024 whose 5/8 load holds twice its beam and a step's lists.  A
