@@ -19,9 +19,13 @@ C ABI with pinned host buffers, copies inside the timed region;
 `config.plain_fp32`: the plain FP32 search_batch (the reference's algorithm,
 id-exact) measured the same way.  `cpu_baseline` and `--impl reference` time
 the reference's own Index::search_batch on the host cores.  Secondary blocks:
-`batched_200k` (mixed ef in one launch), `serving` (continuous batching at
-1M: p50 / p99 / p999), `precision` (d = 960: FP32 / FP16 / FP8 error and
-recall).
+`batched_200k` (mixed ef in one launch; the tensor-core brute force),
+`filtered_200k` (cosine with filters and deletes, mixed k / ef),
+`serving` (continuous batching at 1M: p50 / p99 / p999), `precision`
+(d = 960: FP32 / FP16 / FP8 error and recall), `build` (the graph linked on
+the GPU against the reference's add_batch), `load` (file to searchable
+device graph).  Every block compares the plain GPU answers with the
+reference's on the same graph file (id and distance-bit mismatches).
 """
 from __future__ import annotations
 
