@@ -25,9 +25,12 @@
 // New nodes of one wave do not see each other during their searches (they
 // are linked to each other through later waves' reverse edges and lists),
 // so waves are kept a small fraction of the graph they join: the first
-// nodes are linked one per wave, later waves grow with the graph.  The graph
-// differs from a sequential build, as a threaded reference build does; it is
-// judged on recall.
+// nodes are linked one per wave, later waves grow with the graph.  With
+// peer linking (optional), peer_kernel runs between the two: each new node
+// re-chooses its list among its neighbours and the wave's nodes that chose
+// the same neighbours, which lets waves be larger.  The graph differs from a
+// sequential build, as a threaded reference build does; it is judged on
+// recall.
 //
 // Distances are FP32, eight lanes per row (16-byte loads, a three-step
 // shuffle reduction); the order of the sum is not the reference's (the
