@@ -631,6 +631,13 @@ def run_filtered_200k(local):
     ix.set_device(local)
     for lab in dels:
         ix.mark_deleted(int(lab))
+    # launch shapes tuned on other queries of the same process (seed 2; the
+    # tuner takes per-query ef, not filters)
+    _, sample = workloads.unit_mixture(C3_N, C3_DIM, C3_CENTERS, 4096, qseed=2)
+    t = time.perf_counter()
+    ix.autotune(sample, k=max(C3_KS), ef_max=max(C3_EFS), precision=0,
+                ef_per_query=np.random.default_rng(4).choice(np.array(C3_EFS, dtype=np.uint32), 4096))
+    tune_s = time.perf_counter() - t
     bits = [hnswgpu.Bitset(fw, C3_N)]
     times = []
     for i in range(4):  # the first call uploads the graph and warms up
@@ -675,7 +682,9 @@ def run_filtered_200k(local):
                         f"efC={EFC} (reference add_batch), 1% deleted, {C3_NQ} queries, half filtered to "
                         f"label % 10 == 0, k in {list(C3_KS)}, ef in {list(C3_EFS)} per query",
             "graph_seconds": round(build_s, 1), "graph": how,
-            "qps": round(C3_NQ / gpu_s, 1), "note": "one host call (copies included), median of 3",
+            "qps": round(C3_NQ / gpu_s, 1), "note": "one host call (copies included), median of 3; launch "
+                                                     "shapes autotuned on 4,096 other queries first",
+            "autotune_s": round(tune_s, 1),
             "recall_at_10": round(hit / C3_NQ, 4),
             "reference_qps": round(C3_NQ / el, 1),
             "reference": f"search_batch per (filtered, k, ef) group ({len(batches)} calls), {threads} threads, "

@@ -34,15 +34,16 @@ def int_mixture(n: int, d: int, clusters: int, nq: int, sigma: float = 20.0, qse
     return base, queries
 
 
-def unit_mixture(n: int, d: int, clusters: int, nq: int, noise: float = 0.3):
-    """Unit-normalised mixture around random unit centres (cosine)."""
+def unit_mixture(n: int, d: int, clusters: int, nq: int, noise: float = 0.3, qseed: int = 1):
+    """Unit-normalised mixture around random unit centres (cosine); queries
+    from seed `qseed` (1 for every benchmark workload)."""
     r0 = np.random.default_rng(0)
     centers = r0.normal(size=(clusters, d))
     centers /= np.linalg.norm(centers, axis=1, keepdims=True)
     c = r0.integers(0, clusters, size=n)
     base = centers[c] + r0.normal(0.0, noise, size=(n, d))
     base /= np.linalg.norm(base, axis=1, keepdims=True)
-    r1 = np.random.default_rng(1)
+    r1 = np.random.default_rng(qseed)
     cq = r1.integers(0, clusters, size=nq)
     queries = centers[cq] + r1.normal(0.0, noise, size=(nq, d))
     queries /= np.linalg.norm(queries, axis=1, keepdims=True)
