@@ -832,17 +832,22 @@ int build_graph(hgd_build_args* a, int device, std::string* err) {
     at = b;
     ++a->waves;
   }
+  // the lists come back into staging copies; the caller's arrays change only
+  // once every kernel and copy has succeeded
   uint32_t flags[2] = {0, 0};
   unsigned long long dropped = 0;
+  std::vector<uint32_t> l0_back(static_cast<size_t>(count) * l0_stride);
+  std::vector<uint32_t> up_back(a->upper_words);
   if ((e = cudaMemcpyAsync(flags, d_small, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(&dropped, d_dropped, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-      (e = cudaMemcpyAsync(a->level0, d_l0, static_cast<size_t>(count) * l0_stride * 4, cudaMemcpyDeviceToHost, st)) !=
-          cudaSuccess ||
-      (e = (a->upper_words ? cudaMemcpyAsync(a->upper, d_up, a->upper_words * 4, cudaMemcpyDeviceToHost, st)
+      (e = cudaMemcpyAsync(l0_back.data(), d_l0, l0_back.size() * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = (a->upper_words ? cudaMemcpyAsync(up_back.data(), d_up, a->upper_words * 4, cudaMemcpyDeviceToHost, st)
                            : cudaSuccess)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return bad(HGD_ECUDA, std::string("build: ") + cudaGetErrorString(e));
   if (flags[1] & kErrSteps) return bad(HGD_ERUNTIME, "a layer search exceeded its step bound");
+  std::copy(l0_back.begin(), l0_back.end(), a->level0);
+  std::copy(up_back.begin(), up_back.end(), a->upper);
   a->entry_point = entry;
   a->max_level = top;
   a->dropped_proposals = dropped;

@@ -217,7 +217,8 @@ int hgd_bruteforce(hgd_flat* f, const float* queries, uint64_t nq, uint32_t k, c
  * graph built so far, one warp per node, with reverse edges merged per list
  * after each wave.  The host has stored the nodes already (rows prepared,
  * levels drawn, upper blocks placed: src/index.cpp:101-121); level0 and
- * upper are updated in place, entry_point / max_level on return.  The graph
+ * upper are rewritten, and entry_point / max_level set, only when the call
+ * succeeds (the lists come back into staging copies first).  The graph
  * is not the sequential build's (new nodes of one wave do not see each
  * other); it is judged on recall.  Limits: count < 2^24, 2 <= M <= 32,
  * padded_dim <= 1024, ef_construction <= 1024. */
